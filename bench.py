@@ -1,0 +1,338 @@
+#!/usr/bin/env python3
+"""Benchmark of the linear-response neutrino force correction step on GB300.
+
+One "step" = add_nu_power_to_rhogrid on a synthetic r2c grid: bin the grid into the
+power spectrum (K1), advance delta_nu over the stored delta_tot history (K2), multiply
+every mode by the neutrino correction (K3).  Default workload: N=512 grid
+(512x512x257 complex64), 256 log k bins, 256-row history from a=0.01 to a=1.0,
+3 degenerate 0.1 eV neutrinos, box 512 Mpc/h.
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gb300|reference]
+
+Prints one JSON line.  value = grid modes processed per second (whole job) with the
+grid resident in HBM; e2e = the same through the C ABI with the grid in pinned host
+memory (host->device and device->host copies inside the timed region).
+"""
+import argparse
+import json
+import math
+import os
+import subprocess
+import sys
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, os.path.join(ROOT, "kspace-neutrinos_gb300"))
+
+import numpy as np  # noqa: E402
+
+import workloads as W  # noqa: E402
+
+METRIC = "k-modes/s & HBM GB/s per step, plain vs fwd+adjoint; batched solves/s; err vs FP64"
+UNIT = "k-modes/s"
+
+
+def peaks():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            p = json.load(f)
+        return float(p["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+class ClockSampler:
+    """nvidia-smi clocks/throttle reasons sampled every 200 ms while running."""
+
+    def __init__(self, gpu_index=0):
+        self.gpu = gpu_index
+        self.proc = None
+        self.lines = []
+
+    def __enter__(self):
+        q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+             "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+             "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.gpu), "--query-gpu=" + q,
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except Exception:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def __exit__(self, *a):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except Exception:
+                self.proc.kill()
+
+    def summary(self):
+        sm, mx, reasons = [], 0.0, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            f = [x.strip() for x in ln.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                mx = max(mx, float(f[2]))
+            except ValueError:
+                continue
+            for n, v in zip(names, f[5:9]):
+                if v.lower() == "active":
+                    reasons.add(n)
+        return {"sm_mhz": float(np.median(sm)) if sm else None, "sm_max_mhz": mx or None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def setup_workload(cfg, device_grid=True, seed=0):
+    N, nb, L = cfg["N"], cfg["nbins"], cfg["L"]
+    count, keff_grid = W.geometry(N, nb)
+    m = count > 0
+    kphys = keff_grid[m] * 2 * math.pi / L
+    sf, dt = W.history(kphys, cfg["Na"], cfg["a_end"])
+    logk, T = W.transfer_table(float(sum(cfg["MNu"])))
+    return dict(kphys=kphys, sf=sf, dt=dt, logk=logk, T=T, nk=int(m.sum()))
+
+
+def time_max(cfg, nsteps):
+    """TimeMax sizing the history table (namax = ceil(100 (TimeMax - a0)) + 2,
+    delta_tot_table.c:36) for the synthetic history plus the steps run."""
+    return 0.01 + (cfg["Na"] + nsteps + 6) / 100.0
+
+
+def step_times(cfg, w, steps):
+    """Scale factors: the first call at a_end+0.01 commits a row; later calls advance
+    by 0.001 (provisional row dropped), so each timed step does the same work."""
+    a0 = cfg["a_end"] + 0.01
+    return [a0 + 0.001 * i for i in range(steps)]
+
+
+def run_gb300(args, cfg):
+    import torch
+    import kspace_gpu as kg
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    torch.cuda.set_device(local)
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+    N, nb, L = cfg["N"], cfg["nbins"], cfg["L"]
+    nz = N // 2 + 1
+    slab0 = N * rank // world
+    nslab = N * (rank + 1) // world - slab0
+    wl = setup_workload(cfg)
+    nsteps = args.warmup + args.steps
+    TimeMax = time_max(cfg, 2 * nsteps + 2)
+    k = kg.make_instance(cfg["MNu"], 0.01, 0.7, 0.3, nb, TimeMax, wl["logk"], wl["T"],
+                         UnitLength_in_cm=W.UNIT_LENGTH_MPC, device=local)
+    k.set_nu_state(wl["sf"], wl["dt"])
+    stream = torch.cuda.Stream()
+    k.set_stream(stream)
+    if world > 1:
+        import torch.distributed as dist
+
+        def allreduce(buf):
+            t = torch.from_numpy(buf.copy()).cuda()
+            dist.all_reduce(t)
+            buf[:] = t.cpu().numpy()
+        k.set_allreduce(allreduce)
+    full = W.make_grid_torch(N, L, seed=1, device="cuda")
+    grid = full[slab0:slab0 + nslab].contiguous()
+    del full
+    G = nslab * N * nz
+    bytes_grid = 8 * G
+    a_list = step_times(cfg, None, nsteps)
+    # warm-up (includes the integrator initialisation and one committed row)
+    for i in range(args.warmup):
+        k.add_nu_power_to_rhogrid(a_list[i], L, grid, N, slab0, nslab)
+    torch.cuda.synchronize()
+    k.set_profiling(True)
+    launches0 = k.launch_count()
+    stage = np.zeros(4)
+    ev0 = torch.cuda.Event(enable_timing=True)
+    ev1 = torch.cuda.Event(enable_timing=True)
+    if world > 1:
+        dist.barrier()
+    torch.cuda.synchronize()
+    with ClockSampler(local) as clk:
+        ev0.record(stream)
+        for i in range(args.steps):
+            k.add_nu_power_to_rhogrid(a_list[args.warmup + i], L, grid, N, slab0, nslab)
+            stage += np.array(k.stage_times())
+        ev1.record(stream)
+        torch.cuda.synchronize()
+    launches = k.launch_count() - launches0
+    t_dev = ev0.elapsed_time(ev1) / 1e3
+    if world > 1:
+        tt = torch.tensor([t_dev], device="cuda")
+        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
+        t_dev = float(tt.item())
+    ms_per_step = 1e3 * t_dev / args.steps
+    value = world * G * args.steps / t_dev if world > 1 else G * args.steps / t_dev
+    if world > 1:
+        value = N * N * nz * args.steps / t_dev
+    k.set_profiling(False)
+    # e2e through the C ABI with host buffers (pinned)
+    host = torch.empty((nslab, N, nz), dtype=torch.complex64, pin_memory=True)
+    host.copy_(grid.cpu())
+    a_e2e = [a_list[-1] + 0.001 * (i + 1) for i in range(args.warmup + args.steps)]
+    for i in range(args.warmup):
+        k.add_nu_power_to_rhogrid(a_e2e[i], L, host.numpy(), N, slab0, nslab)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for i in range(args.steps):
+        k.add_nu_power_to_rhogrid(a_e2e[args.warmup + i], L, host.numpy(), N, slab0, nslab)
+    t_e2e = time.perf_counter() - t0
+    if world > 1:
+        tt = torch.tensor([t_e2e], device="cuda")
+        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
+        t_e2e = float(tt.item())
+    e2e_value = (N * N * nz if world > 1 else G) * args.steps / t_e2e
+    # roofline of the dominant grid kernel
+    hbm, peak_kind = peaks()
+    k1_ms, k2_ms, k3_ms = stage[0] / args.steps, stage[1] / args.steps, stage[2] / args.steps
+    k1_gbs = bytes_grid / (k1_ms * 1e-3) / 1e9 if k1_ms > 0 else None
+    k3_gbs = 2 * bytes_grid / (k3_ms * 1e-3) / 1e9 if k3_ms > 0 else None
+    if k3_ms >= k1_ms:
+        dom = {"kernel": "k_correct_tma (grid multiply)", "bytes": 2 * bytes_grid, "ms": k3_ms, "gbs": k3_gbs}
+    else:
+        dom = {"kernel": "k_bin_power_tma (binning)", "bytes": bytes_grid, "ms": k1_ms, "gbs": k1_gbs}
+    traffic = None
+    try:
+        with open(os.path.join(ROOT, "profiles", "traffic.json")) as f:
+            traffic = json.load(f).get(dom["kernel"].split()[0])
+    except Exception:
+        pass
+    res = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": ms_per_step, "higher_is_better": True,
+        "scaling": "strong" if world > 1 else "weak", "vs_baseline": None, "dtype": "c64 grid / f64 integrator",
+        "data": "synthetic (seeded Gaussian modes with the configured P(k); no dataset)",
+        "config": {"workload": cfg["name"], "N": N, "nbins": nb, "history_rows": cfg["Na"],
+                   "masses_eV": list(cfg["MNu"]), "box_mpc_h": L, "grid_bytes": bytes_grid,
+                   "l2": "grid (%.0f MB) larger than L2 (129 MB): no flush" % (bytes_grid / 1e6),
+                   "parallelism": "slabs" if world > 1 else "single GPU"},
+        "hbm_gbs_step": 3 * bytes_grid / (ms_per_step * 1e-3) / 1e9,
+        "stage_ms": {"binning_K1": k1_ms, "integrator_K2": k2_ms, "correction_K3": k3_ms},
+        "stage_gbs": {"K1": k1_gbs, "K3": k3_gbs},
+        "roofline": {"bound": "hbm", "kernel": dom["kernel"], "achieved": dom["gbs"], "peak": hbm,
+                     "peak_kind": peak_kind, "unit": "GB/s", "frac": (dom["gbs"] / hbm) if dom["gbs"] else None,
+                     "traffic": traffic, "algorithmic_bytes_per_launch": dom["bytes"]},
+        "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": bytes_grid,
+                "d2h_bytes_per_step": bytes_grid, "ms_per_step": 1e3 * t_e2e / args.steps},
+        "gpu_launches": launches,
+        "clocks": clk.summary(),
+    }
+    if rank == 0 and not args.no_cpu_baseline:
+        res["cpu_baseline"] = cpu_baseline(cfg, wl, args.cpu_threads, sample_steps=1)
+    k.close()
+    if world > 1:
+        dist.destroy_process_group()
+    return res if rank == 0 else None
+
+
+def cpu_baseline(cfg, wl, threads, sample_steps=1):
+    """The oracle port (the reference algorithm restated in C) on the host cores."""
+    sys.path.insert(0, os.path.join(ROOT, "tests"))
+    from oracle_lib import Oracle
+    O = Oracle()
+    threads = threads or os.cpu_count() or 1
+    N, nb, L = cfg["N"], cfg["nbins"], cfg["L"]
+    bg = O.bg(cfg["MNu"], a0=0.01, h=0.7, Omega0=0.3, UnitTime_in_s=W.UNIT_TIME)
+    TimeMax = time_max(cfg, sample_steps + 2)
+    s = O.state(bg, nb, 0.01, TimeMax, Omega0=0.3, UnitTime_in_s=W.UNIT_TIME, UnitLength_in_cm=W.UNIT_LENGTH_MPC)
+    O.set_transfer(s, wl["logk"], wl["T"])
+    assert O.set_nu_state(s, wl["sf"], wl["dt"]) == 0
+    g = W.make_grid(N, L, seed=1)
+    # initialisation call (delta_nu_last) is not timed, as on the GPU
+    st, _ = O.add_nu_power_to_rhogrid(s, cfg["a_end"] + 0.01, L, g, N, nthreads=threads, nk_alloc=nb)
+    assert st == 0, st
+    G = g.size
+    t0 = time.perf_counter()
+    stages = np.zeros(3)
+    for i in range(sample_steps):
+        st, out = O.add_nu_power_to_rhogrid(s, cfg["a_end"] + 0.011 + 0.001 * i, L, g, N, nthreads=threads,
+                                            nk_alloc=nb)
+        assert st == 0, st
+        stages += out["t_stages"]
+    dt = time.perf_counter() - t0
+    return {"value": G * sample_steps / dt, "unit": UNIT, "cores": threads, "kind": "port",
+            "sample": "%d full step(s) of the same N=%d workload (grid binning and multiply split over %d threads "
+                      "as MPI slabs; integrator once)" % (sample_steps, N, threads),
+            "stage_s": {"binning": stages[0] / sample_steps, "integrator": stages[1] / sample_steps,
+                        "multiply": stages[2] / sample_steps}}
+
+
+def run_reference(args, cfg):
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return None
+    wl = setup_workload(cfg)
+    threads = args.cpu_threads or os.cpu_count() or 1
+    sys.path.insert(0, os.path.join(ROOT, "tests"))
+    from oracle_lib import Oracle
+    O = Oracle()
+    N, nb, L = cfg["N"], cfg["nbins"], cfg["L"]
+    bg = O.bg(cfg["MNu"], a0=0.01, h=0.7, Omega0=0.3, UnitTime_in_s=W.UNIT_TIME)
+    nsteps = args.warmup + args.steps
+    TimeMax = time_max(cfg, nsteps)
+    s = O.state(bg, nb, 0.01, TimeMax, Omega0=0.3, UnitTime_in_s=W.UNIT_TIME, UnitLength_in_cm=W.UNIT_LENGTH_MPC)
+    O.set_transfer(s, wl["logk"], wl["T"])
+    assert O.set_nu_state(s, wl["sf"], wl["dt"]) == 0
+    g = W.make_grid(N, L, seed=1)
+    a_list = step_times(cfg, None, nsteps)
+    for i in range(args.warmup):
+        st, _ = O.add_nu_power_to_rhogrid(s, a_list[i], L, g, N, nthreads=threads, nk_alloc=nb)
+        assert st == 0, st
+    t0 = time.perf_counter()
+    for i in range(args.steps):
+        st, _ = O.add_nu_power_to_rhogrid(s, a_list[args.warmup + i], L, g, N, nthreads=threads, nk_alloc=nb)
+        assert st == 0, st
+    dt = time.perf_counter() - t0
+    v = g.size * args.steps / dt
+    return {"metric": METRIC, "value": v, "unit": UNIT, "impl": "reference", "n_gpus": 0, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": 1e3 * dt / args.steps, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "c64 grid / f64 integrator", "data": "synthetic",
+            "config": {"workload": cfg["name"], "N": N, "nbins": nb, "history_rows": cfg["Na"]},
+            "cpu_baseline": {"value": v, "unit": UNIT, "cores": threads, "kind": "port",
+                             "sample": "the full N=%d step, %d timed steps, binning/multiply split over %d threads "
+                                       "as MPI slabs" % (N, args.steps, threads)},
+            "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--config", default="cfg1_n512", choices=sorted(W.CONFIGS))
+    ap.add_argument("--cpu-threads", type=int, default=0)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    if args.warmup < 3:
+        args.warmup = 3
+    cfg = dict(W.CONFIGS[args.config])
+    cfg["name"] = args.config
+    if args.impl == "reference":
+        res = run_reference(args, cfg)
+    else:
+        res = run_gb300(args, cfg)
+    if res is not None:
+        print(json.dumps(res))
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,159 @@
+/* kspace_gpu.h -- C ABI of libkspace_gb300.so, the GB300 implementation of the
+ * kspace-neutrinos linear-response neutrino force correction.
+ *
+ * Plain C types only (pointers, sizes, doubles).  A context replaces the reference's
+ * process-global singletons (interface_common.c:17-26, interface_gadget.c:19-21); the
+ * reference-named drop-in entry points (add_nu_power_to_rhogrid, ...) are provided on
+ * top of this ABI by kspace_neutrinos_dropin.h / dropin/kspace_dropin.c.
+ *
+ * Every function returns a status: KSPACE_OK (0), or the reference's terminate()
+ * code for the same failure (values below 10000), or a KSPACE_ERR_* code of this
+ * library (10000 and up).  Grid pointers may be device pointers (used in place) or
+ * host pointers (copied to the device and back inside the call).  Calls on one
+ * context are not thread-safe; they run on the context's CUDA stream and return after
+ * the results are complete.
+ */
+#ifndef KSPACE_GPU_H
+#define KSPACE_GPU_H
+#include <stddef.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- status codes: reference terminate() codes ---- */
+#define KSPACE_OK 0
+#define KSPACE_ERR_NOMEM 1              /* interface_gadget.c:88 */
+#define KSPACE_ERR_KMAX 2               /* delta_tot_table.c:113-114: k beyond the transfer table */
+#define KSPACE_ERR_GRID_NAN 5           /* interface_gadget.c:183-184: correction factor is NaN */
+#define KSPACE_ERR_GSL 2001             /* integration / interpolation failure (delta_tot_table.c:70-73) */
+#define KSPACE_ERR_NK_MISMATCH 2002     /* delta_tot_table.c:203-204 */
+#define KSPACE_ERR_NK_SMALL 2003        /* delta_tot_table.c:205-206 */
+#define KSPACE_ERR_DNU_NAN 2004         /* delta_tot_table.c:239-244 */
+#define KSPACE_ERR_STATE_SHORT 2006     /* delta_tot_table.c:281 */
+#define KSPACE_ERR_STATE_START 2007     /* delta_tot_table.c:291-292 */
+#define KSPACE_ERR_NK_ALLOC 2011        /* delta_tot_table.c:97-98 */
+#define KSPACE_ERR_SAVE_OPEN 2012       /* delta_tot_table.c:317-318 */
+#define KSPACE_ERR_TRANSFER_OPEN 2019   /* transfer_init.c:19-20 */
+#define KSPACE_ERR_TRANSFER_SHORT 2021  /* transfer_init.c:78-79 */
+#define KSPACE_ERR_NO_RESUME 2023       /* delta_tot_table.c:91-92 */
+#define KSPACE_ERR_TIME_BEFORE 2024     /* delta_tot_table.c:94-95 */
+/* ---- status codes of this library ---- */
+#define KSPACE_ERR_NAMAX 2025           /* history table full (the reference writes past it) */
+#define KSPACE_ERR_CUDA 10001           /* a CUDA call failed */
+#define KSPACE_ERR_ARG 10002            /* invalid argument */
+#define KSPACE_ERR_ORDER 10003          /* call made before the state it needs exists */
+#define KSPACE_ERR_HUBBLE 10004         /* host hubble_function differs from the device model */
+#define KSPACE_ERR_TIMEOUT 10005        /* a bounded device wait expired */
+
+typedef struct kspace_ctx kspace_ctx;
+
+/* Sums `count` doubles in place across all ranks (an MPI_Allreduce with MPI_SUM).
+ * Used once per call of the grid binning, on the per-bin sums, as the reference does
+ * at powerspectrum.c:91-95.  Returns 0 on success. */
+typedef int (*kspace_allreduce_fn)(double *buf, int count, void *user);
+
+/* ---- lifecycle ---- */
+int kspace_gpu_create(kspace_ctx **ctx, int device);
+int kspace_gpu_destroy(kspace_ctx *ctx);
+const char *kspace_gpu_error_string(int status);
+/* Run on this CUDA stream (a cudaStream_t; NULL = the context's own stream). */
+int kspace_gpu_set_stream(kspace_ctx *ctx, void *cuda_stream);
+/* Multi-rank slab decomposition: reduction of the per-bin sums (NULL = one rank). */
+int kspace_gpu_set_allreduce(kspace_ctx *ctx, kspace_allreduce_fn fn, void *user);
+/* Kernel variant selection: tma (1 = TMA tile engine, 0 = plain loads), rows per CTA
+ * (128/256), pipeline stages (3/4/6), warps per block of the integrator (1..4).
+ * Values <= 0 keep the current setting. */
+int kspace_gpu_set_tuning(kspace_ctx *ctx, int tma, int rows_per_cta, int stages, int qag_warps);
+
+/* ---- background: Omega_nu(a), H(a) ----
+ * Replaces InitOmegaNu / init_omega_nu (interface_common.c:183-188, omega_nu_single.c:16-51).
+ * The Fermi-Dirac tables are integrated on the device. */
+int kspace_gpu_init_omega_nu(kspace_ctx *ctx, const double MNu[3], double TimeTransfer, double HubbleParam,
+                             double tcmb0);
+/* init_hybrid_nu (omega_nu_single.c:230-240; called from interface_common.c:80-81) */
+int kspace_gpu_init_hybrid_nu(kspace_ctx *ctx, double vcrit, double light, double nu_crit_time);
+/* Parameters of the host's hubble_function (gadget_defines.h:11), evaluated on the
+ * device as H0 sqrt(Omega_nonu/a^3 + (1-Omega0-OmegaLambda)/a^2 + OmegaLambda +
+ * Omega_nu(a) [+ Omega_g/a^4]) (delta_tot_table_test.c:33-45, gadget-2/0003 patch:38). */
+int kspace_gpu_set_hubble(kspace_ctx *ctx, double Omega0, double OmegaLambda, double UnitTime_in_s,
+                          int include_radiation);
+/* Compare the device H(a) with n samples of the host's hubble_function; returns
+ * KSPACE_ERR_HUBBLE if any relative difference exceeds rtol. */
+int kspace_gpu_check_hubble(kspace_ctx *ctx, const double *a, const double *H, int n, double rtol,
+                            double *max_rel);
+/* OmegaNu / OmegaNu_nopart / particle_nu_active (interface_common.c:29-39,190-197) */
+int kspace_gpu_omega_nu(kspace_ctx *ctx, double a, double *omega_nu, double *omega_nu_nopart);
+int kspace_gpu_particle_nu_active(kspace_ctx *ctx, double a, int *active);
+/* hubble_function as evaluated on the device model */
+int kspace_gpu_hubble(kspace_ctx *ctx, double a, double *H);
+
+/* ---- integrator state ----
+ * allocate_delta_tot_table (delta_tot_table.c:25-60) as called by allocate_kspace_memory
+ * (interface_common.c:91). */
+int kspace_gpu_alloc_table(kspace_ctx *ctx, int nk_alloc, double TimeTransfer, double TimeMax, double Omega0,
+                           double UnitTime_in_s, double UnitLength_in_cm);
+/* The transfer table of transfer_init.h:10-15: log k (internal units) and T_nu/T_nonu. */
+int kspace_gpu_set_transfer(kspace_ctx *ctx, const double *logk, const double *T_nu, int n);
+/* allocate_transfer_init_table (transfer_init.c:9-83): read a CAMB transfer file. */
+int kspace_gpu_read_transfer_file(kspace_ctx *ctx, double BoxSize, double UnitLength_in_cm,
+                                  double InputSpectrum_UnitLength_in_cm, const char *path, int *nrows);
+/* set_nu_state (interface_common.c:166-180): flat delta_tot[nk][ia] */
+int kspace_gpu_set_nu_state(kspace_ctx *ctx, const double *scalefact, const double *delta_tot, size_t nk,
+                            size_t ia);
+/* get_nu_state (interface_common.c:150-164).  Pass NULL arrays to query nk and ia. */
+int kspace_gpu_get_nu_state(kspace_ctx *ctx, double *scalefact, double *delta_tot, size_t *nk, size_t *ia);
+/* read_all_nu_state / save_all_nu_state / save_nu_power (delta_tot_table.c:254-374),
+ * same text formats. */
+int kspace_gpu_read_nu_state(kspace_ctx *ctx, const char *path);
+int kspace_gpu_save_nu_state(kspace_ctx *ctx, const char *path);
+int kspace_gpu_save_nu_power(kspace_ctx *ctx, double Time, int snapnum, const char *OutputDir);
+/* ints[0..4] = nk, nk_allocated, namax, ia, delta_tot_init_done */
+int kspace_gpu_table_info(kspace_ctx *ctx, int *ints);
+/* delta_nu_init, delta_nu_last, wavenum (each nk_alloc doubles; NULL to skip) */
+int kspace_gpu_get_vectors(kspace_ctx *ctx, double *nu_init, double *nu_last, double *wavenum);
+
+/* ---- the hot path ---- */
+/* total_powerspectrum (powerspectrum.c:33-117): outputs compacted to the non-empty
+ * bins, power normalised by |F(0)|^2 and the mode count. */
+int kspace_gpu_total_powerspectrum(kspace_ctx *ctx, int dims, const void *grid, int nrbins, int startslab,
+                                   int nslab, double *power, long long *count, double *keffs, int *nk_out);
+/* get_delta_nu_update (delta_tot_table.c:193-250): keff = k (not log k), P_cdm_sqrt =
+ * sqrt(P_cdm); writes delta_nu[nk]. */
+int kspace_gpu_get_delta_nu_update(kspace_ctx *ctx, double a, int nk, const double *keff, const double *P_cdm_sqrt,
+                                   double *delta_nu);
+/* compute_neutrino_power_from_cdm (interface_common.c:106-123): outputs the
+ * interpolation table of delta_nu/delta_cdm (log k, ratio, norm = kspace_prefac). */
+int kspace_gpu_compute_neutrino_power_from_cdm(kspace_ctx *ctx, double Time, const double *keff_in,
+                                               const double *P_cdm, const long *Nmodes, int nk_in, double *logk,
+                                               double *ratio, double *norm, int *nbins);
+/* add_nu_power_to_rhogrid (interface_gadget.c:158-194): bin, integrate, multiply every
+ * mode of the slab by 1 + norm * ratio(log|k|).  grid: fftw_complex[nslab][pmgrid][pmgrid/2+1]. */
+int kspace_gpu_add_nu_power_to_rhogrid(kspace_ctx *ctx, double Time, double BoxSize, void *grid, int pmgrid,
+                                       int slabstart_y, int nslab_y);
+/* The grid multiply alone (interface_gadget.c:163-188 with delta_pow.c:19-37) for a
+ * given interpolation table. */
+int kspace_gpu_apply_delta_pow(kspace_ctx *ctx, double BoxSize, void *grid, int pmgrid, int slabstart_y, int nslab_y,
+                               int nrbins, const double *logk, const double *ratio, int nk, double norm);
+/* compute_total_power_spectrum / save_total_power (interface_gadget.c:114-144,196-224) */
+int kspace_gpu_compute_total_power_spectrum(kspace_ctx *ctx, double Time, double BoxSize, const void *grid,
+                                            int pmgrid, int slabstart_y, int nslab_y);
+int kspace_gpu_save_total_power(kspace_ctx *ctx, double Time, int snapnum, const char *OutputDir);
+
+/* ---- diagnostics ---- */
+/* last call: nk, log k, ratio and norm of the correction (arrays of nk_alloc) */
+int kspace_gpu_last_correction(kspace_ctx *ctx, int *nk, double *logk, double *ratio, double *norm, double *dcdm,
+                               double *keff);
+/* device times (ms) of the last add_nu_power_to_rhogrid: [0] binning kernel,
+ * [1] integrator, [2] correction kernel, [3] whole call; enable with on=1 */
+int kspace_gpu_set_profiling(kspace_ctx *ctx, int on);
+int kspace_gpu_stage_times(kspace_ctx *ctx, float *ms4);
+/* QAG statistics of the last integrator call: max and total intervals */
+int kspace_gpu_qag_stats(kspace_ctx *ctx, int *max_intervals, long long *total_intervals);
+/* how many kernels this library has launched on the context (monotonic) */
+long long kspace_gpu_launch_count(kspace_ctx *ctx);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

@@ -1,0 +1,423 @@
+// ksp_device.cuh -- device-side numerics of the linear-response neutrino integrator.
+//
+// Background cosmology (Omega_nu(a) from Fermi-Dirac tables, H(a)), natural cubic
+// splines, the Fermi-Dirac kernel J(x), and a warp-cooperative QAG integrator that
+// makes the same adaptive decisions as QUADPACK's QAG with the 61-point Gauss-Kronrod
+// rule (the integrator the reference calls through GSL, delta_tot_table.c:404,597).
+// Each function names the reference file:line whose arithmetic it follows.
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+#include <float.h>
+#include "gk61_table.h"
+
+#define KSP_HD __host__ __device__ __forceinline__
+
+namespace ksp {
+
+// kspace_neutrino_const.h:9-19, gadget_defines.h:8, omega_nu_single.c:10-14,85
+constexpr int kNuSpecies = 3;
+constexpr int kNRhoTab = 200;
+constexpr int kQagLimit = 200;  // GSL_VAL
+constexpr double kLightCgs = 2.99792458e10;
+constexpr double kBolEvK = 8.61734e-5;
+constexpr double kHubble = 3.24077929e-18;
+constexpr double kHbar = 6.582119e-16;
+constexpr double kStefanBoltzmann = 5.670373e-5;
+constexpr double kGravity = 6.67408e-8;
+constexpr double kNuSw = 100.0;
+constexpr double kFloatAcc = 1e-6;
+constexpr double kPi = 3.14159265358979323846;
+constexpr double kZeta3 = 1.202056903159594;
+
+// Status bits written by kernels (host maps them to reference error codes).
+enum : unsigned {
+    kStGsl = 1u << 0,        // QAG failed / interpolation out of range  -> 2001
+    kStDnuNaN = 1u << 1,     // delta_nu is NaN                          -> 2004
+    kStGridNaN = 1u << 2,    // correction factor is NaN                 -> 5
+    kStKmax = 1u << 3,       // k beyond transfer table                  -> 2
+    kStKWarn = 1u << 4,      // k < keff_0 / 2 (reference prints to stderr, continues)
+    kStTimeout = 1u << 5,    // a bounded wait expired
+};
+
+// omega_nu_single.h:27-34: tabulated rho_nu(a) of one species (natural cubic spline in log a)
+struct RhoTable {
+    int has_table;
+    double mnu;
+    double loga[kNRhoTab], rhonu[kNRhoTab], c[kNRhoTab];
+};
+
+// omega_nu_single.h:100-113 (_omega_nu, _hybrid_nu) plus the parameters of the host's
+// hubble_function (delta_tot_table_test.c:33-45; curvature as gadget-2/0003 patch:38).
+struct Background {
+    double rhocrit, kBtnu, tcmb0, conv, omegag0;
+    int deg[kNuSpecies];
+    double mnu[kNuSpecies];
+    int hyb_enabled;
+    double nufrac_low[kNuSpecies], nu_crit_time, vcrit;
+    double Omega_nonu_H, OmegaLambda, OmegaK, hubble;
+    int radiation;
+    RhoTable tab[kNuSpecies];
+};
+
+// ------------------------------------------------------------------ splines
+// Segment i with x[i] <= v < x[i+1] (v == x[n-1] -> n-2), as GSL's bsearch.
+KSP_HD int seg_bsearch(const double* x, int n, double v) {
+    int lo = 0, hi = n - 1;
+    while (hi > lo + 1) {
+        const int mid = (lo + hi) >> 1;
+        if (x[mid] > v) hi = mid; else lo = mid;
+    }
+    return lo;
+}
+
+// Natural cubic spline (c = S''/2 at the knots) evaluated on segment i.
+KSP_HD double cspline_seg(const double* x, const double* y, const double* c, int i, double v) {
+    const double h = x[i + 1] - x[i], dx = v - x[i];
+    const double b = (y[i + 1] - y[i]) / h - h * (c[i + 1] + 2.0 * c[i]) / 3.0;
+    const double d = (c[i + 1] - c[i]) / (3.0 * h);
+    return y[i] + dx * (b + dx * (c[i] + dx * d));
+}
+
+KSP_HD double linear_seg(const double* x, const double* y, int i, double v) {
+    return y[i] + (v - x[i]) * ((y[i + 1] - y[i]) / (x[i + 1] - x[i]));
+}
+
+// Natural cubic spline coefficients by Gaussian elimination (sequential; small n).
+// scratch: 2*(n-2) doubles.  Same equations as a natural spline anywhere.
+KSP_HD void natural_spline_coeffs(const double* x, const double* y, int n, double* c, double* scratch) {
+    const int m = n - 2;
+    c[0] = 0.0;
+    c[n - 1] = 0.0;
+    if (m <= 0) return;
+    double* diag = scratch;
+    double* rhs = scratch + m;
+    for (int i = 0; i < m; i++) {
+        const double h0 = x[i + 1] - x[i], h1 = x[i + 2] - x[i + 1];
+        diag[i] = 2.0 * (h0 + h1);
+        rhs[i] = 3.0 * ((y[i + 2] - y[i + 1]) / h1 - (y[i + 1] - y[i]) / h0);
+    }
+    for (int i = 1; i < m; i++) {
+        const double off = x[i + 1] - x[i];
+        const double f = off / diag[i - 1];
+        diag[i] -= f * off;
+        rhs[i] -= f * rhs[i - 1];
+    }
+    c[m] = rhs[m - 1] / diag[m - 1];
+    for (int i = m - 1; i-- > 0;) {
+        const double off = x[i + 2] - x[i + 1];
+        c[i + 1] = (rhs[i] - off * c[i + 2]) / diag[i];
+    }
+}
+
+// ------------------------------------------------------------------ background
+// omega_nu_single.c:100-114 (rho_nu conversion factor)
+KSP_HD double rho_nu_conversion() {
+    double convert = 4 * kPi * 2;
+    const double chbar = 1. / (2 * kPi * kLightCgs * kHbar);
+    convert *= (chbar * chbar * chbar);
+    convert *= (1.60217646e-12 / kLightCgs / kLightCgs);
+    return convert;
+}
+
+// omega_nu_single.c:156-160
+KSP_HD double non_rel_rho_nu(double a, double kT, double amnu, double kTamnu2, double conv) {
+    return amnu * (kT * kT * kT) / (a * a * a * a) *
+           (1.5 * kZeta3 + kTamnu2 * 45. / 4. * 1.0369277551433704 +
+            2835. / 32. * kTamnu2 * kTamnu2 * 1.0083492773819229 +
+            80325 / 32. * kTamnu2 * kTamnu2 * kTamnu2 * 1.0020083928260826) * conv;
+}
+
+// omega_nu_single.c:164-167
+KSP_HD double rel_rho_nu(double a, double kT, double conv) {
+    const double t = kPi * kT / a, t2 = t * t;
+    return 7 * (t2 * t2) / 120. * conv;
+}
+
+// omega_nu_single.c:171-202
+KSP_HD double rho_nu(const RhoTable& T, double a, double kT, double conv) {
+    const double amnu = a * T.mnu;
+    const double kTamnu2 = (kT * kT / amnu / amnu);
+    if (kNuSw * kNuSw * kTamnu2 < 1) return non_rel_rho_nu(a, kT, amnu, kTamnu2, conv);
+    if (amnu < 1e-6 * kT) return rel_rho_nu(a, kT, conv);
+    const double loga = log(a);
+    if (!T.has_table || loga < T.loga[0]) {
+        if (amnu < 1e-4 * kT) return rel_rho_nu(a, kT, conv);
+        return non_rel_rho_nu(a, kT, amnu, kTamnu2, conv);
+    }
+    // uniform knots: guess the segment, then settle it against the stored knots
+    const double inv = (kNRhoTab - 1) / (T.loga[kNRhoTab - 1] - T.loga[0]);
+    int i = (int)((loga - T.loga[0]) * inv);
+    i = i < 0 ? 0 : (i > kNRhoTab - 2 ? kNRhoTab - 2 : i);
+    while (i > 0 && loga < T.loga[i]) i--;
+    while (i < kNRhoTab - 2 && loga >= T.loga[i + 1]) i++;
+    return cspline_seg(T.loga, T.rhonu, T.c, i, loga);
+}
+
+// omega_nu_single.c:246-257
+KSP_HD double particle_nu_fraction(const Background& B, double a, int i) {
+    if (!B.hyb_enabled) return 0;
+    if (a > B.nu_crit_time) return B.nufrac_low[i];
+    return 0;
+}
+
+// omega_nu_single.c:55-65
+KSP_HD double omega_nu(const Background& B, double a) {
+    double rhonu = 0;
+    for (int mi = 0; mi < kNuSpecies; mi++)
+        if (B.deg[mi] > 0) rhonu += B.deg[mi] * rho_nu(B.tab[mi], a, B.kBtnu, B.conv);
+    return rhonu / B.rhocrit;
+}
+
+// omega_nu_single.c:69-74
+KSP_HD double omega_nu_nopart(const Background& B, double a) {
+    return omega_nu(B, a) - omega_nu(B, 1) * particle_nu_fraction(B, a, 0) / (a * a * a);
+}
+
+// omega_nu_single.c:262-279
+KSP_HD double omega_nu_single(const Background& B, double a, int i) {
+    if (B.deg[i] == 0) {
+        for (int j = i; j >= 0; j--)
+            if (B.deg[j]) { i = j; break; }
+    }
+    const double om = rho_nu(B.tab[i], a, B.kBtnu, B.conv) / B.rhocrit;
+    double part = rho_nu(B.tab[i], 1, B.kBtnu, B.conv) / B.rhocrit;
+    part *= particle_nu_fraction(B, a, i) / (a * a * a);
+    return om - part;
+}
+
+// delta_tot_table_test.c:33-45 (+ curvature, gadget-2/0003 patch:38); Omega_g as
+// omega_nu_single.c:77-81.
+KSP_HD double hubble(const Background& B, double a) {
+    const double a3 = a * a * a;
+    double om = B.Omega_nonu_H / a3 + B.OmegaLambda;
+    if (B.OmegaK != 0.0) om += B.OmegaK / (a * a);
+    om += omega_nu(B, a);
+    if (B.radiation) om += B.omegag0 / (a3 * a);
+    return B.hubble * sqrt(om);
+}
+
+// delta_tot_table.c:613-617
+KSP_HD double get_delta_tot(double dnu, double dcdm, double OmegaNua3, double Omeganonu, double Omeganu1,
+                            double partnu) {
+    const double fcdm = 1 - OmegaNua3 / (Omeganonu + Omeganu1);
+    return fcdm * (dcdm + dnu * OmegaNua3 / (Omeganonu + Omeganu1 * partnu));
+}
+
+// ------------------------------------------------------------------ J(x)
+// delta_tot_table.c:417-428
+KSP_HD double specialJ_fit(double x) {
+    if (x <= 0.) return 1.;
+    const double x2 = x * x, x4 = x2 * x2, x8 = x4 * x4;
+    return (1. + 0.0168 * x2 + 0.0407 * x4) / (1. + 2.1734 * x2 + 1.6787 * exp(4.1811 * log(x)) + 0.1467 * x8);
+}
+
+// sin(y)/y: Taylor series 1 - y^2/6 + y^4/120 - y^6/5040 + y^8/362880 near 0.
+KSP_HD double sinc_j0(double y) {
+    if (fabs(y) < 0.05) {
+        const double t = y * y;
+        return 1.0 - t / 6.0 * (1.0 - t / 20.0 * (1.0 - t / 42.0 * (1.0 - t / 72.0)));
+    }
+    return sin(y) / y;
+}
+
+// delta_tot_table.c:431-434
+KSP_HD double II(double x, double qc, int n) {
+    return (n * n + n * n * n * qc + n * qc * x * x - x * x) * qc * sinc_j0(qc * x) +
+           (2 * n + n * n * qc + qc * x * x) * cos(qc * x);
+}
+
+// delta_tot_table.c:442-463
+KSP_HD double specialJ(double x, double qc, double nufrac_low) {
+    if (qc > 0) {
+        double integ = 0;
+        for (int n = 1; n < 20; n++) {
+            const double s = (n & 1) ? 1.0 : -1.0;  // -(-1)^n
+            const double d = n * n + x * x;
+            integ += s * exp(-n * qc) / d / d * II(x, qc, n);
+        }
+        return integ / (1.5 * kZeta3 * (1 - nufrac_low));
+    }
+    return specialJ_fit(x);
+}
+
+// ------------------------------------------------------------------ QAG (GK61)
+#ifdef __CUDACC__
+struct Gk61Nodes {  // expanded 61-node table: slot j<30: -x_j, 30<=j<60: +x_{j-30}, 60: centre
+    double x[61], wk[61], wg[61];
+};
+
+__device__ __forceinline__ void gk61_fill(Gk61Nodes& n, int tid, int nthreads) {
+    const double XK[31] = KSP_GK61_XK_INIT;
+    const double WK[31] = KSP_GK61_WK_INIT;
+    const double WG[31] = KSP_GK61_WG_INIT;
+    for (int j = tid; j < 61; j += nthreads) {
+        if (j < 30) { n.x[j] = -XK[j]; n.wk[j] = WK[j]; n.wg[j] = WG[j]; }
+        else if (j < 60) { n.x[j] = XK[j - 30]; n.wk[j] = WK[j - 30]; n.wg[j] = WG[j - 30]; }
+        else { n.x[j] = 0.0; n.wk[j] = WK[30]; n.wg[j] = 0.0; }
+    }
+}
+
+__device__ __forceinline__ double warp_sum_to0(double v) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+    return v;
+}
+__device__ __forceinline__ double bcast0(double v) { return __shfl_sync(0xffffffffu, v, 0); }
+
+// QUADPACK error estimate: err = resasc * min(1, (200 |err|/resasc)^1.5), floored at
+// 50 eps resabs (Piessens et al. 1983, qk rules).
+__device__ __forceinline__ double rescale_error(double err, double resabs, double resasc) {
+    err = fabs(err);
+    if (resasc != 0.0 && err != 0.0) {
+        const double s = pow(200.0 * err / resasc, 1.5);
+        err = s < 1.0 ? resasc * s : resasc;
+    }
+    if (resabs > DBL_MIN / (50.0 * DBL_EPSILON)) {
+        const double fl = 50.0 * DBL_EPSILON * resabs;
+        if (fl > err) err = fl;
+    }
+    return err;
+}
+
+struct GkOut { double result, abserr, resabs, resasc; };
+
+// Evaluate the GK61 rule on `nint` (1 or 2) intervals [a_t, b_t] with one warp.
+// Every lane returns identical values (sums are reduced to lane 0 and broadcast).
+template <class F>
+__device__ __forceinline__ void gk61_warp(const F& f, const Gk61Nodes& N, int nint, const double* a, const double* b,
+                                          GkOut* out) {
+    const int lane = threadIdx.x & 31;
+    double c[2], h[2];
+    for (int t = 0; t < 2; t++) {
+        c[t] = __dmul_rn(0.5, __dadd_rn(a[t], b[t]));
+        h[t] = __dmul_rn(0.5, __dsub_rn(b[t], a[t]));
+    }
+    double fv[4];
+    double rk[2] = {0, 0}, rg[2] = {0, 0}, ra[2] = {0, 0};
+    const int nslots = 61 * nint;
+#pragma unroll
+    for (int m = 0; m < 4; m++) {
+        const int s = lane + 32 * m;
+        fv[m] = 0.0;
+        if (s < nslots) {
+            const int t = s >= 61 ? 1 : 0;
+            const int j = s - 61 * t;
+            const double x = __dadd_rn(c[t], __dmul_rn(h[t], N.x[j]));
+            const double v = f(x);
+            fv[m] = v;
+            if (t == 0) { rk[0] += N.wk[j] * v; rg[0] += N.wg[j] * v; ra[0] += N.wk[j] * fabs(v); }
+            else { rk[1] += N.wk[j] * v; rg[1] += N.wg[j] * v; ra[1] += N.wk[j] * fabs(v); }
+        }
+    }
+    double mean[2];
+    for (int t = 0; t < nint; t++) {
+        rk[t] = bcast0(warp_sum_to0(rk[t]));
+        rg[t] = bcast0(warp_sum_to0(rg[t]));
+        ra[t] = bcast0(warp_sum_to0(ra[t]));
+        mean[t] = 0.5 * rk[t];
+    }
+    double rs[2] = {0, 0};
+#pragma unroll
+    for (int m = 0; m < 4; m++) {
+        const int s = lane + 32 * m;
+        if (s < nslots) {
+            const int t = s >= 61 ? 1 : 0;
+            const int j = s - 61 * t;
+            const double d = N.wk[j] * fabs(fv[m] - mean[t]);
+            if (t == 0) rs[0] += d; else rs[1] += d;
+        }
+    }
+    for (int t = 0; t < nint; t++) {
+        rs[t] = bcast0(warp_sum_to0(rs[t]));
+        const double err = (rk[t] - rg[t]) * h[t];
+        out[t].result = rk[t] * h[t];
+        out[t].resabs = ra[t] * fabs(h[t]);
+        out[t].resasc = rs[t] * fabs(h[t]);
+        out[t].abserr = rescale_error(err, out[t].resabs, out[t].resasc);
+    }
+}
+
+struct QagList {  // per-warp interval list in shared memory
+    double a[kQagLimit], b[kQagLimit], r[kQagLimit], e[kQagLimit];
+};
+
+struct QagResult { double result, abserr; int ok; int nint; };
+
+// QUADPACK QAG (Piessens et al. 1983) with the 61-point rule, run by one warp:
+// bisect the interval with the largest error estimate until the summed error is
+// below max(epsabs, epsrel |area|); QUADPACK's round-off and tiny-interval checks.
+// Same decisions as the GSL-based reference path (delta_tot_table.c:404,597).
+template <class F>
+__device__ QagResult qag_warp(const F& f, const Gk61Nodes& N, QagList& L, double a, double b, double epsabs,
+                              double epsrel, int limit) {
+    const int lane = threadIdx.x & 31;
+    QagResult R;
+    GkOut g[2];
+    double aa[2] = {a, a}, bb[2] = {b, b};
+    gk61_warp(f, N, 1, aa, bb, g);
+    if (lane == 0) { L.a[0] = a; L.b[0] = b; L.r[0] = g[0].result; L.e[0] = g[0].abserr; }
+    __syncwarp();
+    double tol = fmax(epsabs, epsrel * fabs(g[0].result));
+    const double round_off = 50 * DBL_EPSILON * g[0].resabs;
+    R.nint = 1;
+    R.result = g[0].result;
+    R.abserr = g[0].abserr;
+    if (g[0].abserr <= round_off && g[0].abserr > tol) { R.ok = 0; return R; }
+    if ((g[0].abserr <= tol && g[0].abserr != g[0].resasc) || g[0].abserr == 0.0) { R.ok = 1; return R; }
+    if (limit == 1) { R.ok = 0; return R; }
+    double area = g[0].result, errsum = g[0].abserr;
+    int n = 1, roundoff1 = 0, roundoff2 = 0, error_type = 0;
+    do {
+        // argmax of the error list (lowest index on ties)
+        double best = -1.0;
+        int bk = 0x7fffffff;
+        for (int i = lane; i < n; i += 32) {
+            const double e = L.e[i];
+            if (e > best) { best = e; bk = i; }
+        }
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) {
+            const double ob = __shfl_down_sync(0xffffffffu, best, o);
+            const int ok = __shfl_down_sync(0xffffffffu, bk, o);
+            if (ob > best || (ob == best && ok < bk)) { best = ob; bk = ok; }
+        }
+        const int k = __shfl_sync(0xffffffffu, bk, 0);
+        const double a_i = L.a[k], b_i = L.b[k], r_i = L.r[k], e_i = L.e[k];
+        const double a1 = a_i, b1 = 0.5 * (a_i + b_i), a2 = b1, b2 = b_i;
+        aa[0] = a1; bb[0] = b1; aa[1] = a2; bb[1] = b2;
+        gk61_warp(f, N, 2, aa, bb, g);
+        const double area12 = g[0].result + g[1].result, error12 = g[0].abserr + g[1].abserr;
+        errsum += error12 - e_i;
+        area += area12 - r_i;
+        if (g[0].resasc != g[0].abserr && g[1].resasc != g[1].abserr) {
+            if (fabs(r_i - area12) <= 1.0e-5 * fabs(area12) && error12 >= 0.99 * e_i) roundoff1++;
+            if (n >= 10 && error12 > e_i) roundoff2++;
+        }
+        tol = fmax(epsabs, epsrel * fabs(area));
+        if (errsum > tol) {
+            if (roundoff1 >= 6 || roundoff2 >= 20) error_type = 2;
+            const double tiny = (1 + 100 * DBL_EPSILON) * (fabs(a2) + 1000 * DBL_MIN);
+            if (fabs(a1) <= tiny && fabs(b2) <= tiny) error_type = 3;
+        }
+        __syncwarp();
+        if (lane == 0) {
+            L.b[k] = b1; L.r[k] = g[0].result; L.e[k] = g[0].abserr;
+            L.a[n] = a2; L.b[n] = b2; L.r[n] = g[1].result; L.e[n] = g[1].abserr;
+        }
+        __syncwarp();
+        n++;
+    } while (n < limit && !error_type && errsum > tol);
+    double sum = 0;
+    if (lane == 0)
+        for (int i = 0; i < n; i++) sum += L.r[i];
+    R.result = bcast0(sum);
+    R.abserr = errsum;
+    R.nint = n;
+    R.ok = errsum <= tol;
+    __syncwarp();
+    return R;
+}
+#endif  // __CUDACC__
+
+}  // namespace ksp

@@ -1,0 +1,723 @@
+// ksp_grid.cu -- the two streaming passes over the half-complex k-space grid.
+//
+// K1 (bin power, powerspectrum.c:56-89) and K3 (correction multiply,
+// interface_gadget.c:163-188) stream the slab [nslab][N][N/2+1] complex64 once each.
+// The slab is viewed as rows of 16 modes (128 bytes); a persistent CTA pulls tiles of
+// ROWS such rows into a ring of shared-memory stages with 2-D TMA loads (128-byte
+// swizzle, so that each thread reading "its" row is bank-conflict free) and, for K3,
+// writes the corrected tile back with TMA stores.  Every thread handles the 16
+// consecutive modes of one row: the mode coordinates advance incrementally, the log
+// bin comes from an approximate log2 settled exactly against integer k^2 thresholds
+// (so counts match the reference's floor(bpu log|k|) bit for bit), and K1 sums runs of
+// equal bins in registers (Kahan, FP32) before one shared-memory FP64 add per run.
+// Mode counts and sum|k| per bin depend only on the geometry and are computed once.
+#include <cuda.h>
+#include <cuda_runtime.h>
+#include <stdint.h>
+#include "ksp_internal.h"
+
+namespace ksp {
+
+// ------------------------------------------------------------------ helpers
+__device__ __forceinline__ uint32_t smem_addr(const void* p) {
+    return static_cast<uint32_t>(__cvta_generic_to_shared(p));
+}
+__device__ __forceinline__ void mbar_init_(uint64_t* bar, unsigned count) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_addr(bar)), "r"(count) : "memory");
+}
+__device__ __forceinline__ void mbar_expect_tx_(uint64_t* bar, unsigned bytes) {
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_addr(bar)), "r"(bytes)
+                 : "memory");
+}
+__device__ __forceinline__ bool mbar_try_wait_(uint64_t* bar, unsigned phase) {
+    uint32_t ok;
+    asm volatile(
+        "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}\n"
+        : "=r"(ok)
+        : "r"(smem_addr(bar)), "r"(phase)
+        : "memory");
+    return ok != 0;
+}
+__device__ __forceinline__ bool mbar_wait_bounded_(uint64_t* bar, unsigned phase) {
+    for (int it = 0; it < (1 << 22); it++)
+        if (mbar_try_wait_(bar, phase)) return true;
+    return false;
+}
+__device__ __forceinline__ void tma_load_2d(void* dst, const CUtensorMap* map, uint64_t* bar, int x, int y) {
+    asm volatile(
+        "cp.async.bulk.tensor.2d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%3, %4}], [%2];" ::
+            "r"(smem_addr(dst)),
+        "l"(reinterpret_cast<uint64_t>(map)), "r"(smem_addr(bar)), "r"(x), "r"(y)
+        : "memory");
+}
+__device__ __forceinline__ void tma_store_2d(const CUtensorMap* map, const void* src, int x, int y) {
+    asm volatile("cp.async.bulk.tensor.2d.global.shared::cta.bulk_group [%0, {%2, %3}], [%1];" ::"l"(
+                     reinterpret_cast<uint64_t>(map)),
+                 "r"(smem_addr(src)), "r"(x), "r"(y)
+                 : "memory");
+}
+__device__ __forceinline__ void bulk_commit() { asm volatile("cp.async.bulk.commit_group;" ::: "memory"); }
+__device__ __forceinline__ void bulk_wait_read_le1() { asm volatile("cp.async.bulk.wait_group.read 1;" ::: "memory"); }
+__device__ __forceinline__ void bulk_wait_all() { asm volatile("cp.async.bulk.wait_group 0;" ::: "memory"); }
+__device__ __forceinline__ void fence_async_smem() { asm volatile("fence.proxy.async.shared::cta;" ::: "memory"); }
+
+// n / d for n < 2^31: m = floor(2^s/d)+1 with s = 31 + ceil(log2 d)
+struct FastDiv {
+    uint32_t d, m;
+    int s;
+};
+static FastDiv make_fastdiv(uint32_t d) {
+    FastDiv f;
+    f.d = d;
+    int l = 0;
+    while ((1u << l) < d) l++;
+    f.s = 31 + l;
+    f.m = (uint32_t)((((unsigned __int128)1) << f.s) / d + 1);
+    return f;
+}
+__device__ __forceinline__ uint32_t fdiv(uint32_t n, const FastDiv& f) {
+    return (uint32_t)(((uint64_t)n * f.m) >> f.s);
+}
+
+struct GridArgs {
+    int N, nz, half, slab0, nrbins, nk;
+    long long nmodes, nrows16;
+    float c1;       // binsperunit * ln2 / 2: bin ~ c1 * log2(k^2)
+    float lnscale;  // log(2 pi / BoxSize) (K3)
+    FastDiv fd_nz, fd_N;
+};
+
+__device__ __forceinline__ int kval(int n, int N) { return n <= N / 2 ? n : n - N; }
+
+// reference bin of integer k^2 >= 1: max b with thresh[b] <= k2
+__device__ __forceinline__ int bin_of(int k2, float c1, const int* thr, int nb) {
+    int b = __float2int_rd(c1 * __log2f((float)k2));
+    b = b < 0 ? 0 : (b > nb - 1 ? nb - 1 : b);
+    while (b > 0 && k2 < thr[b]) b--;
+    while (b < nb - 1 && k2 >= thr[b + 1]) b++;
+    return b;
+}
+
+// Mode coordinates that advance through a row of the slab.
+struct ModeCursor {
+    int il, j, z;       // local slab, second index, z
+    int kxy2;
+    float iwxy;
+    __device__ __forceinline__ void set_row(const GridArgs& g, const float* w1) {
+        const int kx = kval(g.slab0 + il, g.N), ky = kval(j, g.N);
+        kxy2 = kx * kx + ky * ky;
+        iwxy = __fmul_rn(w1[kx < 0 ? -kx : kx], w1[ky < 0 ? -ky : ky]);
+    }
+    __device__ __forceinline__ void init(const GridArgs& g, const float* w1, long long row_base, int z_base, int add) {
+        // row_base/z_base: decoded flat mode index of the tile start; add: modes from there
+        const uint32_t o = (uint32_t)(z_base + add);
+        const uint32_t dr = fdiv(o, g.fd_nz);
+        z = (int)(o - dr * (uint32_t)g.nz);
+        const uint32_t r = (uint32_t)(row_base + dr);
+        const uint32_t i = fdiv(r, g.fd_N);
+        il = (int)i;
+        j = (int)(r - i * (uint32_t)g.N);
+        set_row(g, w1);
+    }
+    __device__ __forceinline__ void next(const GridArgs& g, const float* w1) {
+        if (++z == g.nz) {
+            z = 0;
+            if (++j == g.N) { j = 0; il++; }
+            set_row(g, w1);
+        }
+    }
+};
+
+// Coordinates for K3, which needs only k^2.
+struct KCursor {
+    int il, j, z, kxy2;
+    __device__ __forceinline__ void set_row(const GridArgs& g) {
+        const int kx = kval(g.slab0 + il, g.N), ky = kval(j, g.N);
+        kxy2 = kx * kx + ky * ky;
+    }
+    __device__ __forceinline__ void init(const GridArgs& g, long long row_base, int z_base, int add) {
+        const uint32_t o = (uint32_t)(z_base + add);
+        const uint32_t dr = fdiv(o, g.fd_nz);
+        z = (int)(o - dr * (uint32_t)g.nz);
+        const uint32_t r = (uint32_t)(row_base + dr);
+        const uint32_t i = fdiv(r, g.fd_N);
+        il = (int)i;
+        j = (int)(r - i * (uint32_t)g.N);
+        set_row(g);
+    }
+    __device__ __forceinline__ void next(const GridArgs& g) {
+        if (++z == g.nz) {
+            z = 0;
+            if (++j == g.N) { j = 0; il++; }
+            set_row(g);
+        }
+    }
+};
+
+// K1 contribution of one mode: w |F|^2 W^4, W = product of 1-D inverse windows, with
+// the reference's float arithmetic (powerspectrum.c:16-24,68,76,84).
+__device__ __forceinline__ float mode_power(float re, float im, const ModeCursor& c, const float* w1, int half) {
+    const float t = __fmul_rn(c.iwxy, w1[c.z]);
+    const float inv = __fmul_rn(t, t);
+    const float f = __fmul_rn(inv, inv);
+    const float F2 = __fadd_rn(__fmul_rn(re, re), __fmul_rn(im, im));
+    float p = __fmul_rn(F2, f);
+    if (c.z != 0 && c.z != half) p = p + p;
+    return p;
+}
+
+struct RunAcc {  // Kahan sum of a run of modes in one bin
+    int b = -1;
+    float s = 0.f, cc = 0.f;
+    __device__ __forceinline__ void add(int bin, float p, double* hist) {
+        if (bin == b) {
+            const float y = __fsub_rn(p, cc);
+            const float t = __fadd_rn(s, y);
+            cc = __fsub_rn(__fsub_rn(t, s), y);
+            s = t;
+        } else {
+            flush(hist);
+            b = bin; s = p; cc = 0.f;
+        }
+    }
+    __device__ __forceinline__ void flush(double* hist) {
+        if (b >= 0) atomicAdd(hist + b, (double)s - (double)cc);
+        b = -1;
+    }
+};
+
+// ------------------------------------------------------------------ shared-memory layout
+struct SmemPlan {
+    size_t stages_off, hist_off, thr_off, tab_off, bar_off, total;
+};
+__host__ __device__ inline SmemPlan plan_smem(int rows, int stages, int nrbins, int ntab_floats) {
+    SmemPlan p;
+    p.stages_off = 0;  // aligned to 1024 at run time (slack included)
+    size_t o = (size_t)stages * rows * 128 + 1024;
+    p.hist_off = o;
+    o += sizeof(double) * (size_t)nrbins;
+    p.thr_off = o;
+    o += sizeof(int) * (size_t)(nrbins + 1);
+    o = (o + 15) & ~size_t(15);
+    p.tab_off = o;
+    o += sizeof(float) * (size_t)ntab_floats;
+    o = (o + 15) & ~size_t(15);
+    p.bar_off = o;
+    o += sizeof(uint64_t) * (size_t)stages;
+    p.total = o;
+    return p;
+}
+
+// ------------------------------------------------------------------ K1 (TMA)
+template <int ROWS, int STAGES>
+__global__ void __launch_bounds__(ROWS) k_bin_power_tma(const __grid_constant__ CUtensorMap tmap, GridArgs g,
+                                                        const int* __restrict__ thresh, const float* __restrict__ w1g,
+                                                        const float* __restrict__ grid, double* bin_sum, double* F0sq,
+                                                        unsigned* status, int ntiles) {
+    extern __shared__ unsigned char sm_raw[];
+    __shared__ int s_abort;
+    __shared__ long long s_rowbase;
+    __shared__ int s_zbase;
+    const SmemPlan P = plan_smem(ROWS, STAGES, g.nrbins, g.nz);
+    const uint32_t base_u = smem_addr(sm_raw);
+    unsigned char* stage0 = sm_raw + ((1024 - (base_u & 1023)) & 1023);
+    double* s_hist = reinterpret_cast<double*>(sm_raw + P.hist_off);
+    int* s_thr = reinterpret_cast<int*>(sm_raw + P.thr_off);
+    float* s_w1 = reinterpret_cast<float*>(sm_raw + P.tab_off);
+    uint64_t* bars = reinterpret_cast<uint64_t*>(sm_raw + P.bar_off);
+    const int tid = threadIdx.x;
+    for (int i = tid; i < g.nrbins; i += ROWS) s_hist[i] = 0.0;
+    for (int i = tid; i <= g.nrbins; i += ROWS) s_thr[i] = thresh[i];
+    for (int i = tid; i < g.nz; i += ROWS) s_w1[i] = w1g[i];
+    if (tid == 0) {
+        s_abort = 0;
+        for (int s = 0; s < STAGES; s++) mbar_init_(&bars[s], 1);
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+    __syncthreads();
+    const int my_n = blockIdx.x < ntiles ? (ntiles - 1 - blockIdx.x) / gridDim.x + 1 : 0;
+    if (tid == 0) {
+        for (int k = 0; k < STAGES && k < my_n; k++) {
+            const int tile = blockIdx.x + k * gridDim.x;
+            mbar_expect_tx_(&bars[k], ROWS * 128);
+            tma_load_2d(stage0 + (size_t)k * ROWS * 128, &tmap, &bars[k], 0, tile * ROWS);
+        }
+    }
+    RunAcc run;
+    int k = 0;
+    for (; k < my_n; k++) {
+        const int s = k % STAGES;
+        const int tile = blockIdx.x + k * gridDim.x;
+        if (tid == 0) {
+            if (!mbar_wait_bounded_(&bars[s], (k / STAGES) & 1)) s_abort = 1;
+            const long long m = (long long)tile * ROWS * 16;
+            s_rowbase = m / g.nz;
+            s_zbase = (int)(m - s_rowbase * g.nz);
+        }
+        __syncthreads();
+        if (s_abort) break;
+        const long long row = (long long)tile * ROWS + tid;
+        if (row < g.nrows16) {
+            const unsigned char* rp = stage0 + (size_t)s * ROWS * 128 + (size_t)tid * 128;
+            ModeCursor c;
+            c.init(g, s_w1, s_rowbase, s_zbase, tid * 16);
+#pragma unroll
+            for (int u = 0; u < 8; u++) {
+                const float4 v = *reinterpret_cast<const float4*>(rp + ((u ^ (tid & 7)) << 4));
+                {
+                    const int k2 = c.kxy2 + c.z * c.z;
+                    if (k2 != 0) run.add(bin_of(k2, g.c1, s_thr, g.nrbins), mode_power(v.x, v.y, c, s_w1, g.half), s_hist);
+                    c.next(g, s_w1);
+                }
+                {
+                    const int k2 = c.kxy2 + c.z * c.z;
+                    if (k2 != 0) run.add(bin_of(k2, g.c1, s_thr, g.nrbins), mode_power(v.z, v.w, c, s_w1, g.half), s_hist);
+                    c.next(g, s_w1);
+                }
+            }
+        }
+        __syncthreads();
+        if (tid == 0 && k + STAGES < my_n) {
+            const int nt = blockIdx.x + (k + STAGES) * gridDim.x;
+            mbar_expect_tx_(&bars[s], ROWS * 128);
+            tma_load_2d(stage0 + (size_t)s * ROWS * 128, &tmap, &bars[s], 0, nt * ROWS);
+        }
+    }
+    if (s_abort) {
+        // wait (bounded) for the loads still in flight, then leave
+        if (tid == 0) {
+            atomicOr(status, kStTimeout);
+            for (int kk = k; kk < my_n && kk < k + STAGES; kk++)
+                mbar_wait_bounded_(&bars[kk % STAGES], (kk / STAGES) & 1);
+        }
+        return;
+    }
+    run.flush(s_hist);
+    // the modes after the last full 16-mode row (fewer than 16), by CTA 0
+    if (blockIdx.x == 0 && tid == 0) {
+        for (long long m = g.nrows16 * 16; m < g.nmodes; m++) {
+            const long long r = m / g.nz;
+            ModeCursor c;
+            c.z = (int)(m - r * g.nz);
+            c.il = (int)(r / g.N);
+            c.j = (int)(r - (long long)c.il * g.N);
+            c.set_row(g, s_w1);
+            const int k2 = c.kxy2 + c.z * c.z;
+            if (k2 != 0) {
+                const float re = grid[2 * m], im = grid[2 * m + 1];
+                atomicAdd(&s_hist[bin_of(k2, g.c1, s_thr, g.nrbins)], (double)mode_power(re, im, c, s_w1, g.half));
+            }
+        }
+    }
+    if (blockIdx.x == 0 && tid == 0 && g.slab0 == 0 && g.nmodes > 0) {
+        const float re = grid[0], im = grid[1];
+        *F0sq = (double)__fadd_rn(__fmul_rn(re, re), __fmul_rn(im, im));
+    }
+    __syncthreads();
+    for (int i = tid; i < g.nrbins; i += ROWS)
+        if (s_hist[i] != 0.0) atomicAdd(bin_sum + i, s_hist[i]);
+}
+
+// ------------------------------------------------------------------ K1 (plain loads)
+__global__ void k_bin_power_plain(GridArgs g, const int* __restrict__ thresh, const float* __restrict__ w1g,
+                                  const float* __restrict__ grid, double* bin_sum, double* F0sq) {
+    extern __shared__ unsigned char sm_raw[];
+    double* s_hist = reinterpret_cast<double*>(sm_raw);
+    int* s_thr = reinterpret_cast<int*>(s_hist + g.nrbins);
+    float* s_w1 = reinterpret_cast<float*>(s_thr + g.nrbins + 1);
+    for (int i = threadIdx.x; i < g.nrbins; i += blockDim.x) s_hist[i] = 0.0;
+    for (int i = threadIdx.x; i <= g.nrbins; i += blockDim.x) s_thr[i] = thresh[i];
+    for (int i = threadIdx.x; i < g.nz; i += blockDim.x) s_w1[i] = w1g[i];
+    __syncthreads();
+    for (long long m = blockIdx.x * (long long)blockDim.x + threadIdx.x; m < g.nmodes;
+         m += (long long)gridDim.x * blockDim.x) {
+        const long long r = m / g.nz;
+        ModeCursor c;
+        c.z = (int)(m - r * g.nz);
+        c.il = (int)(r / g.N);
+        c.j = (int)(r - (long long)c.il * g.N);
+        c.set_row(g, s_w1);
+        const int k2 = c.kxy2 + c.z * c.z;
+        if (k2 == 0) continue;
+        const float2 v = reinterpret_cast<const float2*>(grid)[m];
+        atomicAdd(&s_hist[bin_of(k2, g.c1, s_thr, g.nrbins)], (double)mode_power(v.x, v.y, c, s_w1, g.half));
+    }
+    if (blockIdx.x == 0 && threadIdx.x == 0 && g.slab0 == 0 && g.nmodes > 0) {
+        const float re = grid[0], im = grid[1];
+        *F0sq = (double)__fadd_rn(__fmul_rn(re, re), __fmul_rn(im, im));
+    }
+    __syncthreads();
+    for (int i = threadIdx.x; i < g.nrbins; i += blockDim.x)
+        if (s_hist[i] != 0.0) atomicAdd(bin_sum + i, s_hist[i]);
+}
+
+// ------------------------------------------------------------------ K3 helpers
+struct CorrSmem {
+    const int* thr; const int* cmap; const float* xf; const float* rn; const float* sn;
+};
+
+// 1 + norm*interp(log k) - 1 for a mode with integer k^2 (delta_pow.c:19-37 clamping)
+__device__ __forceinline__ float corr_delta(int k2, const GridArgs& g, const CorrSmem& t, unsigned& flags) {
+    const int b = bin_of(k2, g.c1, t.thr, g.nrbins);
+    const int c = t.cmap[b];
+    if (c < 0) { flags |= kStGsl; return 0.f; }
+    const float x = fmaf(0.5f, __logf((float)k2), g.lnscale);
+    const int nk = g.nk;
+    if (x < t.xf[c]) {
+        if (c == 0) {
+            if (x < t.xf[0] - 0.69314718f) flags |= kStKWarn;
+            return t.rn[0];
+        }
+        return fmaf(x - t.xf[c - 1], t.sn[c - 1], t.rn[c - 1]);
+    }
+    if (c >= nk - 1) return t.rn[nk - 1];
+    return fmaf(x - t.xf[c], t.sn[c], t.rn[c]);
+}
+
+// ------------------------------------------------------------------ K3 (TMA in/out)
+template <int ROWS, int STAGES>
+__global__ void __launch_bounds__(ROWS) k_correct_tma(const __grid_constant__ CUtensorMap tmap, GridArgs g,
+                                                      const int* __restrict__ thresh, const int* __restrict__ cmapg,
+                                                      CorrTable corr, float* grid, unsigned* status, int ntiles) {
+    extern __shared__ unsigned char sm_raw[];
+    __shared__ int s_abort;
+    __shared__ long long s_rowbase;
+    __shared__ int s_zbase;
+    const SmemPlan P = plan_smem(ROWS, STAGES, g.nrbins, 3 * g.nk + g.nrbins);
+    const uint32_t base_u = smem_addr(sm_raw);
+    unsigned char* stage0 = sm_raw + ((1024 - (base_u & 1023)) & 1023);
+    int* s_thr = reinterpret_cast<int*>(sm_raw + P.thr_off);
+    float* s_tab = reinterpret_cast<float*>(sm_raw + P.tab_off);
+    int* s_cmap = reinterpret_cast<int*>(s_tab + 3 * g.nk);
+    uint64_t* bars = reinterpret_cast<uint64_t*>(sm_raw + P.bar_off);
+    const int tid = threadIdx.x;
+    for (int i = tid; i <= g.nrbins; i += ROWS) s_thr[i] = thresh[i];
+    for (int i = tid; i < g.nrbins; i += ROWS) s_cmap[i] = cmapg[i];
+    for (int i = tid; i < g.nk; i += ROWS) {
+        s_tab[i] = corr.xf[i];
+        s_tab[g.nk + i] = corr.rn[i];
+        s_tab[2 * g.nk + i] = corr.sn[i];
+    }
+    if (tid == 0) {
+        s_abort = 0;
+        for (int s = 0; s < STAGES; s++) mbar_init_(&bars[s], 1);
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+    __syncthreads();
+    CorrSmem T{s_thr, s_cmap, s_tab, s_tab + g.nk, s_tab + 2 * g.nk};
+    const int my_n = blockIdx.x < ntiles ? (ntiles - 1 - blockIdx.x) / gridDim.x + 1 : 0;
+    if (tid == 0) {
+        for (int k = 0; k < STAGES - 1 && k < my_n; k++) {
+            const int tile = blockIdx.x + k * gridDim.x;
+            mbar_expect_tx_(&bars[k], ROWS * 128);
+            tma_load_2d(stage0 + (size_t)k * ROWS * 128, &tmap, &bars[k], 0, tile * ROWS);
+        }
+    }
+    unsigned flags = 0;
+    int k = 0;
+    for (; k < my_n; k++) {
+        const int s = k % STAGES;
+        const int tile = blockIdx.x + k * gridDim.x;
+        if (tid == 0) {
+            if (!mbar_wait_bounded_(&bars[s], (k / STAGES) & 1)) s_abort = 1;
+            const long long m = (long long)tile * ROWS * 16;
+            s_rowbase = m / g.nz;
+            s_zbase = (int)(m - s_rowbase * g.nz);
+        }
+        __syncthreads();
+        if (s_abort) break;
+        const long long row = (long long)tile * ROWS + tid;
+        if (row < g.nrows16) {
+            unsigned char* rp = stage0 + (size_t)s * ROWS * 128 + (size_t)tid * 128;
+            KCursor c;
+            c.init(g, s_rowbase, s_zbase, tid * 16);
+#pragma unroll
+            for (int u = 0; u < 8; u++) {
+                float4* vp = reinterpret_cast<float4*>(rp + ((u ^ (tid & 7)) << 4));
+                float4 v = *vp;
+                {
+                    const int k2 = c.kxy2 + c.z * c.z;
+                    if (k2 != 0) {
+                        const float d = corr_delta(k2, g, T, flags);
+                        v.x = fmaf(v.x, d, v.x);
+                        v.y = fmaf(v.y, d, v.y);
+                    }
+                    c.next(g);
+                }
+                {
+                    const int k2 = c.kxy2 + c.z * c.z;
+                    if (k2 != 0) {
+                        const float d = corr_delta(k2, g, T, flags);
+                        v.z = fmaf(v.z, d, v.z);
+                        v.w = fmaf(v.w, d, v.w);
+                    }
+                    c.next(g);
+                }
+                *vp = v;
+            }
+        }
+        fence_async_smem();
+        __syncthreads();
+        if (tid == 0) {
+            tma_store_2d(&tmap, stage0 + (size_t)s * ROWS * 128, 0, tile * ROWS);
+            bulk_commit();
+            if (k + STAGES - 1 < my_n) {
+                const int s2 = (k + STAGES - 1) % STAGES;
+                const int nt = blockIdx.x + (k + STAGES - 1) * gridDim.x;
+                bulk_wait_read_le1();  // the store issued from stage s2 one iteration ago has been read
+                mbar_expect_tx_(&bars[s2], ROWS * 128);
+                tma_load_2d(stage0 + (size_t)s2 * ROWS * 128, &tmap, &bars[s2], 0, nt * ROWS);
+            }
+        }
+    }
+    if (tid == 0) {
+        if (s_abort) {
+            atomicOr(status, kStTimeout);
+            for (int kk = k; kk < my_n && kk < k + STAGES - 1; kk++)
+                mbar_wait_bounded_(&bars[kk % STAGES], (kk / STAGES) & 1);
+        }
+        bulk_wait_all();
+    }
+    if (s_abort) return;
+    // trailing modes (fewer than 16) by CTA 0
+    if (blockIdx.x == 0 && tid == 0) {
+        for (long long m = g.nrows16 * 16; m < g.nmodes; m++) {
+            const long long r = m / g.nz;
+            const int z = (int)(m - r * g.nz);
+            const int il = (int)(r / g.N), j = (int)(r - (long long)il * g.N);
+            const int kx = kval(g.slab0 + il, g.N), ky = kval(j, g.N);
+            const int k2 = kx * kx + ky * ky + z * z;
+            if (k2 != 0) {
+                const float d = corr_delta(k2, g, T, flags);
+                grid[2 * m] = fmaf(grid[2 * m], d, grid[2 * m]);
+                grid[2 * m + 1] = fmaf(grid[2 * m + 1], d, grid[2 * m + 1]);
+            }
+        }
+    }
+    if (flags) atomicOr(status, flags);
+}
+
+// ------------------------------------------------------------------ K3 (plain loads)
+__global__ void k_correct_plain(GridArgs g, const int* __restrict__ thresh, const int* __restrict__ cmapg,
+                                CorrTable corr, float* grid, unsigned* status) {
+    extern __shared__ unsigned char sm_raw[];
+    int* s_thr = reinterpret_cast<int*>(sm_raw);
+    int* s_cmap = s_thr + g.nrbins + 1;
+    float* s_tab = reinterpret_cast<float*>(s_cmap + g.nrbins);
+    for (int i = threadIdx.x; i <= g.nrbins; i += blockDim.x) s_thr[i] = thresh[i];
+    for (int i = threadIdx.x; i < g.nrbins; i += blockDim.x) s_cmap[i] = cmapg[i];
+    for (int i = threadIdx.x; i < g.nk; i += blockDim.x) {
+        s_tab[i] = corr.xf[i];
+        s_tab[g.nk + i] = corr.rn[i];
+        s_tab[2 * g.nk + i] = corr.sn[i];
+    }
+    __syncthreads();
+    CorrSmem T{s_thr, s_cmap, s_tab, s_tab + g.nk, s_tab + 2 * g.nk};
+    unsigned flags = 0;
+    for (long long m = blockIdx.x * (long long)blockDim.x + threadIdx.x; m < g.nmodes;
+         m += (long long)gridDim.x * blockDim.x) {
+        const long long r = m / g.nz;
+        const int z = (int)(m - r * g.nz);
+        const int il = (int)(r / g.N), j = (int)(r - (long long)il * g.N);
+        const int kx = kval(g.slab0 + il, g.N), ky = kval(j, g.N);
+        const int k2 = kx * kx + ky * ky + z * z;
+        if (k2 == 0) continue;
+        const float d = corr_delta(k2, g, T, flags);
+        float2 v = reinterpret_cast<float2*>(grid)[m];
+        v.x = fmaf(v.x, d, v.x);
+        v.y = fmaf(v.y, d, v.y);
+        reinterpret_cast<float2*>(grid)[m] = v;
+    }
+    if (flags) atomicOr(status, flags);
+}
+
+// ------------------------------------------------------------------ geometry
+// weighted mode count per integer k^2 over the slab range (weights as powerspectrum.c:56-89)
+__global__ void k_k2_hist(int N, int slab0, int nslab, unsigned long long* hist) {
+    const long long rows = (long long)nslab * N;
+    for (long long r = blockIdx.x * (long long)blockDim.x + threadIdx.x; r < rows;
+         r += (long long)gridDim.x * blockDim.x) {
+        const int il = (int)(r / N), j = (int)(r - (long long)il * N);
+        const int kx = kval(slab0 + il, N), ky = kval(j, N);
+        const int kxy2 = kx * kx + ky * ky;
+        for (int z = 0; z <= N / 2; z++) {
+            const int k2 = kxy2 + z * z;
+            if (k2 == 0) continue;
+            atomicAdd(hist + k2, (unsigned long long)((z == 0 || z == N / 2) ? 1 : 2));
+        }
+    }
+}
+void launch_k2_histogram(int N, int slab0, int nslab, unsigned long long* hist, cudaStream_t st) {
+    const long long rows = (long long)nslab * N;
+    const int blocks = (int)((rows + 255) / 256 < 4096 ? (rows + 255) / 256 : 4096);
+    k_k2_hist<<<blocks > 0 ? blocks : 1, 256, 0, st>>>(N, slab0, nslab, hist);
+}
+
+// powerspectrum.c:98-115 + interface_gadget.c:96-100
+__global__ void k_finalize_power(const double* bin_sum, const double* F0sq, const long long* count,
+                                 const double* ksum, const int* compact_bins, int nk, double BoxSize,
+                                 double* power_out, double* keff_out, double* dcdm_out, double* keffphys_out) {
+    const int c = blockIdx.x * blockDim.x + threadIdx.x;
+    if (c >= nk) return;
+    const int b = compact_bins[c];
+    double p = bin_sum[b];
+    p /= *F0sq;
+    const double cnt = (double)count[b];
+    const double ke = ksum[b] / cnt;
+    p /= cnt;
+    if (power_out) power_out[c] = p;
+    if (keff_out) keff_out[c] = ke;
+    const double scale = pow(BoxSize, -3.0);
+    if (dcdm_out) dcdm_out[c] = sqrt(p / scale);
+    if (keffphys_out) keffphys_out[c] = ke * (2 * 3.14159265358979323846 / BoxSize);
+}
+void launch_finalize_power(const double* bin_sum, const double* F0sq, const long long* count, const double* ksum,
+                           const int* compact_bins, int nk, double BoxSize, double* power_out, double* keff_out,
+                           double* dcdm_out, double* keffphys_out, cudaStream_t st) {
+    k_finalize_power<<<(nk + 127) / 128, 128, 0, st>>>(bin_sum, F0sq, count, ksum, compact_bins, nk, BoxSize,
+                                                       power_out, keff_out, dcdm_out, keffphys_out);
+}
+
+// ------------------------------------------------------------------ host launchers
+typedef CUresult (*PFN_encodeTiled)(CUtensorMap*, CUtensorMapDataType, cuuint32_t, void*, const cuuint64_t*,
+                                     const cuuint64_t*, const cuuint32_t*, const cuuint32_t*, CUtensorMapInterleave,
+                                     CUtensorMapSwizzle, CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
+static PFN_encodeTiled get_encode() {
+    static PFN_encodeTiled fn = nullptr;
+    static bool tried = false;
+    if (!tried) {
+        tried = true;
+        void* p = nullptr;
+        cudaDriverEntryPointQueryResult q;
+        if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) ==
+                cudaSuccess &&
+            q == cudaDriverEntryPointSuccess)
+            fn = reinterpret_cast<PFN_encodeTiled>(p);
+    }
+    return fn;
+}
+
+static bool make_map(CUtensorMap* map, const void* grid, long long nrows16, int rows) {
+    PFN_encodeTiled enc = get_encode();
+    if (!enc || nrows16 <= 0) return false;
+    if ((reinterpret_cast<uintptr_t>(grid) & 15) != 0) return false;
+    cuuint64_t gdim[2] = {32, (cuuint64_t)nrows16};
+    cuuint64_t gstride[1] = {128};
+    cuuint32_t box[2] = {32, (cuuint32_t)rows};
+    cuuint32_t estr[2] = {1, 1};
+    return enc(map, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 2, const_cast<void*>(grid), gdim, gstride, box, estr,
+               CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+               CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
+}
+
+static GridArgs make_args(const GridGeom& g, int nk, float lnscale) {
+    GridArgs a;
+    a.N = g.N;
+    a.nz = g.N / 2 + 1;
+    a.half = g.N / 2;
+    a.slab0 = g.slab0;
+    a.nrbins = g.nrbins;
+    a.nk = nk;
+    a.nmodes = g.nmodes;
+    a.nrows16 = g.nmodes / 16;
+    a.c1 = g.bin_c1;
+    a.lnscale = lnscale;
+    a.fd_nz = make_fastdiv((uint32_t)a.nz);
+    a.fd_N = make_fastdiv((uint32_t)g.N);
+    return a;
+}
+
+static int sm_count() {
+    static int n = 0;
+    if (!n) {
+        int dev = 0;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev);
+        if (n <= 0) n = 1;
+    }
+    return n;
+}
+
+template <int ROWS, int STAGES>
+static int run_bin_tma(const GridGeom& g, const GridArgs& a, const float* grid, double* bin_sum, double* F0sq,
+                       unsigned* status, cudaStream_t st) {
+    CUtensorMap map;
+    if (!make_map(&map, grid, a.nrows16, ROWS)) return -1;
+    const SmemPlan P = plan_smem(ROWS, STAGES, g.nrbins, a.nz);
+    if (P.total > 220 * 1024) return -1;
+    auto kern = k_bin_power_tma<ROWS, STAGES>;
+    cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)P.total);
+    int per_sm = 1;
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, ROWS, P.total);
+    if (per_sm < 1) per_sm = 1;
+    const int ntiles = (int)((a.nrows16 + ROWS - 1) / ROWS);
+    int grid_n = sm_count() * per_sm;
+    if (grid_n > ntiles) grid_n = ntiles > 0 ? ntiles : 1;
+    kern<<<grid_n, ROWS, P.total, st>>>(map, a, g.thresh, g.w1, grid, bin_sum, F0sq, status, ntiles);
+    return cudaPeekAtLastError() == cudaSuccess ? 0 : -2;
+}
+
+int launch_bin_power(const GridGeom& g, const float* grid, double* bin_sum, double* F0sq, unsigned* status, int tma,
+                     int rows_per_cta, int stages, cudaStream_t st) {
+    const GridArgs a = make_args(g, 0, 0.f);
+    if (tma && a.nrows16 > 0) {
+        int r = -1;
+        if (rows_per_cta == 256 && stages == 3) r = run_bin_tma<256, 3>(g, a, grid, bin_sum, F0sq, status, st);
+        else if (rows_per_cta == 256 && stages == 4) r = run_bin_tma<256, 4>(g, a, grid, bin_sum, F0sq, status, st);
+        else if (rows_per_cta == 128 && stages == 6) r = run_bin_tma<128, 6>(g, a, grid, bin_sum, F0sq, status, st);
+        else r = run_bin_tma<128, 4>(g, a, grid, bin_sum, F0sq, status, st);
+        if (r == 0) return 0;
+        if (r == -2) return -2;
+    }
+    const size_t smem = sizeof(double) * g.nrbins + sizeof(int) * (g.nrbins + 1) + sizeof(float) * a.nz + 16;
+    cudaFuncSetAttribute(k_bin_power_plain, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    long long blocks = (g.nmodes + 255) / 256;
+    const long long cap = 8LL * sm_count();
+    if (blocks > cap) blocks = cap;
+    if (blocks < 1) blocks = 1;
+    k_bin_power_plain<<<(int)blocks, 256, smem, st>>>(a, g.thresh, g.w1, grid, bin_sum, F0sq);
+    return cudaPeekAtLastError() == cudaSuccess ? 1 : -2;
+}
+
+template <int ROWS, int STAGES>
+static int run_corr_tma(const GridGeom& g, const GridArgs& a, float* grid, CorrTable corr, unsigned* status,
+                        cudaStream_t st) {
+    CUtensorMap map;
+    if (!make_map(&map, grid, a.nrows16, ROWS)) return -1;
+    const SmemPlan P = plan_smem(ROWS, STAGES, g.nrbins, 3 * a.nk + g.nrbins);
+    if (P.total > 220 * 1024) return -1;
+    auto kern = k_correct_tma<ROWS, STAGES>;
+    cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)P.total);
+    int per_sm = 1;
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, ROWS, P.total);
+    if (per_sm < 1) per_sm = 1;
+    const int ntiles = (int)((a.nrows16 + ROWS - 1) / ROWS);
+    int grid_n = sm_count() * per_sm;
+    if (grid_n > ntiles) grid_n = ntiles > 0 ? ntiles : 1;
+    kern<<<grid_n, ROWS, P.total, st>>>(map, a, g.thresh, g.cmap, corr, grid, status, ntiles);
+    return cudaPeekAtLastError() == cudaSuccess ? 0 : -2;
+}
+
+int launch_apply_correction(const GridGeom& g, float* grid, CorrTable corr, float lnscale, unsigned* status, int tma,
+                            int rows_per_cta, int stages, cudaStream_t st) {
+    const GridArgs a = make_args(g, corr.nk, lnscale);
+    if (tma && a.nrows16 > 0) {
+        int r = -1;
+        if (rows_per_cta == 256 && stages == 3) r = run_corr_tma<256, 3>(g, a, grid, corr, status, st);
+        else if (rows_per_cta == 256 && stages == 4) r = run_corr_tma<256, 4>(g, a, grid, corr, status, st);
+        else if (rows_per_cta == 128 && stages == 6) r = run_corr_tma<128, 6>(g, a, grid, corr, status, st);
+        else r = run_corr_tma<128, 4>(g, a, grid, corr, status, st);
+        if (r == 0) return 0;
+        if (r == -2) return -2;
+    }
+    const size_t smem = sizeof(int) * (2 * g.nrbins + 1) + sizeof(float) * 3 * a.nk + 16;
+    cudaFuncSetAttribute(k_correct_plain, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    long long blocks = (g.nmodes + 255) / 256;
+    const long long cap = 8LL * sm_count();
+    if (blocks > cap) blocks = cap;
+    if (blocks < 1) blocks = 1;
+    k_correct_plain<<<(int)blocks, 256, smem, st>>>(a, g.thresh, g.cmap, corr, grid, status);
+    return cudaPeekAtLastError() == cudaSuccess ? 1 : -2;
+}
+
+}  // namespace ksp

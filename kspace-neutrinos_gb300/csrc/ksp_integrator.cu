@@ -1,0 +1,629 @@
+// ksp_integrator.cu -- the linear-response neutrino integrator on the GPU.
+//
+//   k_rho_points / k_spline1    Omega_nu(a) tables (omega_nu_single.c:117-153)
+//   k_nufrac_low                hybrid-neutrino fractions (omega_nu_single.c:214-240)
+//   k_update_row                update_delta_tot (delta_tot_table.c:177-191)
+//   k_delta_tot_init            delta_tot_init's per-bin part (delta_tot_table.c:94-129)
+//   k_scalars                   per-call scalars + factorised knot spline system
+//   k_fs_segments/k_fs_finish   the fslength table (delta_tot_table.c:574-591): a
+//                               cumulative fixed-order Gauss-Legendre sum over the 16*Na
+//                               uniform nodes replaces 16*Na adaptive integrals; spline
+//                               coefficients by the closed-form inverse of tridiag(1,4,1)
+//   k_dtot_coeffs               natural spline of every history row (shared knots)
+//   k_dnu_qag                   one warp per (species, bin): history row staged into
+//                               shared memory by a TMA bulk copy, then QAG/GK61 of the
+//                               delta_nu time integral (delta_tot_table.c:492-500,592-599)
+//   k_combine / k_finish        species sum, row commit, NaN check, clamp, ratio table
+#include <cuda_runtime.h>
+#include <stdio.h>
+#include "ksp_internal.h"
+
+namespace ksp {
+
+// ------------------------------------------------------------------ small PTX helpers
+__device__ __forceinline__ uint32_t smem_u32(const void* p) {
+    return static_cast<uint32_t>(__cvta_generic_to_shared(p));
+}
+__device__ __forceinline__ void mbar_init(uint64_t* bar, unsigned count) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(count) : "memory");
+}
+__device__ __forceinline__ void mbar_expect_tx(uint64_t* bar, unsigned bytes) {
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)), "r"(bytes)
+                 : "memory");
+}
+__device__ __forceinline__ bool mbar_try_wait(uint64_t* bar, unsigned phase) {
+    uint32_t ok;
+    asm volatile(
+        "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}\n"
+        : "=r"(ok)
+        : "r"(smem_u32(bar)), "r"(phase)
+        : "memory");
+    return ok != 0;
+}
+// Bounded wait: gives up after ~2^22 polls (each poll may suspend for a while).
+__device__ __forceinline__ bool mbar_wait_bounded(uint64_t* bar, unsigned phase) {
+    for (int it = 0; it < (1 << 22); it++)
+        if (mbar_try_wait(bar, phase)) return true;
+    return false;
+}
+__device__ __forceinline__ void bulk_g2s(void* dst, const void* src, unsigned bytes, uint64_t* bar) {
+    asm volatile(
+        "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+            smem_u32(dst)),
+        "l"(src), "r"(bytes), "r"(smem_u32(bar))
+        : "memory");
+}
+
+// ------------------------------------------------------------------ background tables
+struct RhoIntegrand {  // omega_nu_single.c:89-96
+    double amnu, kT;
+    __device__ double operator()(double q) const {
+        const double epsilon = sqrt(q * q + amnu * amnu);
+        const double f0 = 1. / (exp(q / kT) + 1);
+        return q * q * epsilon * f0;
+    }
+};
+
+// one warp per (species, table point): rhonu[i] = qag(...)/a^4 * conversion
+__global__ void k_rho_points(Background* B, unsigned* status) {
+    __shared__ Gk61Nodes N;
+    extern __shared__ unsigned char smraw[];
+    QagList* lists = reinterpret_cast<QagList*>(smraw);
+    gk61_fill(N, threadIdx.x, blockDim.x);
+    __syncthreads();
+    const int warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+    const int task = blockIdx.x * nw + warp;
+    const int s = task / kNRhoTab, i = task % kNRhoTab;
+    if (s >= kNuSpecies) return;
+    RhoTable& T = B->tab[s];
+    if (!B->deg[s] || !T.has_table) return;
+    RhoIntegrand f{T.mnu * exp(T.loga[i]), B->kBtnu};
+    QagResult r = qag_warp(f, N, lists[warp], 0.0, 500 * B->kBtnu, 0.0, 1e-9, kQagLimit);
+    if ((threadIdx.x & 31) == 0) {
+        const double ea = exp(T.loga[i]);
+        T.rhonu[i] = r.result / (ea * ea * ea * ea) * B->conv;
+        if (!r.ok) atomicOr(status, kStGsl);
+    }
+}
+
+__global__ void k_rho_splines(Background* B, double* scratch) {
+    const int s = threadIdx.x;
+    if (s >= kNuSpecies) return;
+    RhoTable& T = B->tab[s];
+    if (!B->deg[s] || !T.has_table) return;
+    natural_spline_coeffs(T.loga, T.rhonu, kNRhoTab, T.c, scratch + s * 2 * kNRhoTab);
+}
+
+void launch_background_tables(Background* dB, double a0, cudaStream_t st, unsigned* status) {
+    (void)a0;
+    const int warps = 4;
+    const int tasks = kNuSpecies * kNRhoTab;
+    k_rho_points<<<(tasks + warps - 1) / warps, 32 * warps, warps * sizeof(QagList), st>>>(dB, status);
+    double* scratch = nullptr;
+    cudaMallocAsync(&scratch, sizeof(double) * 2 * kNRhoTab * kNuSpecies, st);
+    k_rho_splines<<<1, 32, 0, st>>>(dB, scratch);
+    cudaFreeAsync(scratch, st);
+}
+
+__global__ void k_spline1(const double* x, const double* y, double* c, double* scratch, int n) {
+    if (threadIdx.x == 0 && blockIdx.x == 0) natural_spline_coeffs(x, y, n, c, scratch);
+}
+void launch_spline_coeffs_1thread(const double* x, const double* y, double* c, double* scratch, int n,
+                                  cudaStream_t st) {
+    k_spline1<<<1, 32, 0, st>>>(x, y, c, scratch, n);
+}
+
+struct FermiDirac {  // omega_nu_single.c:207-210
+    __device__ double operator()(double x) const { return x * x / (exp(x) + 1); }
+};
+
+// omega_nu_single.c:214-228 (qag limit 100) and :230-240
+__global__ void k_nufrac_low(Background* B, double light, double vcrit, unsigned* status) {
+    __shared__ Gk61Nodes N;
+    __shared__ QagList L[kNuSpecies];
+    gk61_fill(N, threadIdx.x, blockDim.x);
+    __syncthreads();
+    const int s = threadIdx.x >> 5;
+    if (s >= kNuSpecies) return;
+    const double qc = B->mnu[s] * vcrit / light / B->kBtnu;
+    QagResult r = qag_warp(FermiDirac{}, N, L[s], 0.0, qc, 0.0, 1e-6, 100);
+    if ((threadIdx.x & 31) == 0) {
+        B->nufrac_low[s] = r.result / (1.5 * kZeta3);
+        if (!r.ok) atomicOr(status, kStGsl);
+    }
+}
+void launch_nufrac_low(Background* dB, double light, double vcrit, cudaStream_t st, unsigned* status) {
+    k_nufrac_low<<<1, 32 * kNuSpecies, 0, st>>>(dB, light, vcrit, status);
+}
+
+// ------------------------------------------------------------------ history rows
+// delta_tot_table.c:177-191: row `row` = get_delta_tot(dnu, dcdm) at a
+__global__ void k_update_row(IntegratorDev I, int nk, int row, double a, double loga, const double* dcdm,
+                             const double* dnu) {
+    __shared__ double s3[3];
+    const Background& B = *I.B;
+    if (threadIdx.x == 0) {
+        s3[0] = omega_nu_nopart(B, a) * (a * a * a);
+        s3[1] = omega_nu(B, 1);
+        s3[2] = particle_nu_fraction(B, a, 0);
+        if (blockIdx.x == 0) I.scalefact[row] = loga;
+    }
+    __syncthreads();
+    const double Omeganonu = I.sc->Omeganonu;
+    for (int ik = blockIdx.x * blockDim.x + threadIdx.x; ik < nk; ik += gridDim.x * blockDim.x)
+        I.dtot[(size_t)ik * I.ld + row] = get_delta_tot(dnu[ik], dcdm[ik], s3[0], Omeganonu, s3[1], s3[2]);
+}
+void launch_update_row(const IntegratorDev& I, int nk, int row, double a, double loga, const double* dcdm,
+                       const double* dnu, cudaStream_t st) {
+    k_update_row<<<(nk + 255) / 256, 256, 0, st>>>(I, nk, row, a, loga, dcdm, dnu);
+}
+
+// delta_tot_table.c:94-129: transfer spline, first row (fresh start), delta_nu_init
+__global__ void k_delta_tot_init(IntegratorDev I, int nk, const double* wavenum, const double* dcdm, int fresh,
+                                 double TimeTransfer) {
+    __shared__ double s4[4];
+    const Background& B = *I.B;
+    if (threadIdx.x == 0) {
+        s4[0] = omega_nu_nopart(B, TimeTransfer) * (TimeTransfer * TimeTransfer * TimeTransfer);
+        s4[1] = omega_nu(B, 1);
+        s4[2] = particle_nu_fraction(B, TimeTransfer, 0);
+        s4[3] = I.sc->Omeganonu;
+        // k beyond the transfer table (delta_tot_table.c:113-114)
+        if (log(wavenum[nk - 1]) > I.t_logk[I.ntrans - 1]) atomicOr(I.status, kStKmax);
+    }
+    __syncthreads();
+    const double OmegaNua3 = s4[0], OmegaNu1 = s4[1], Omeganonu = s4[3];
+    const double OmegaMa = Omeganonu + OmegaNua3;
+    for (int ik = blockIdx.x * blockDim.x + threadIdx.x; ik < nk; ik += gridDim.x * blockDim.x) {
+        const double lk = log(wavenum[ik]);
+        double T;
+        if (lk < I.t_logk[0] || lk > I.t_logk[I.ntrans - 1]) {
+            atomicOr(I.status, kStGsl);  // GSL interpolation domain error -> 2001
+            T = 0;
+        } else {
+            const int i = seg_bsearch(I.t_logk, I.ntrans, lk);
+            T = cspline_seg(I.t_logk, I.t_T, I.t_c, i, lk);
+        }
+        double* row = I.dtot + (size_t)ik * I.ld;
+        if (fresh) row[0] = get_delta_tot(dcdm[ik] * T, dcdm[ik], OmegaNua3, Omeganonu, OmegaNu1, s4[2]);
+        I.nu_init[ik] = row[0] * OmegaMa / (OmegaMa - OmegaNua3 + T * OmegaNua3) * fabs(T);
+        I.wavenum[ik] = wavenum[ik];
+    }
+}
+void launch_delta_tot_init(const IntegratorDev& I, int nk, const double* wavenum, const double* dcdm, int fresh,
+                           double TimeTransfer, cudaStream_t st) {
+    k_delta_tot_init<<<(nk + 255) / 256, 256, 0, st>>>(I, nk, wavenum, dcdm, fresh, TimeTransfer);
+}
+
+// ------------------------------------------------------------------ per-call scalars
+// Scalars of the call and the factorised natural-spline system of the history knots
+// x = scalefact[0..Na-1] (shared by every row).  Rows below `start_row` were factorised
+// by an earlier call with the same leading knots and are kept.  Reciprocals are stored
+// so the per-row sweeps need no divisions.
+__global__ void k_scalars(IntegratorDev I, int Na, double a, double loga, double loga0, double TimeTransfer,
+                          int start_row) {
+    const double* xk = I.scalefact;
+    for (int i = threadIdx.x; i + 1 < Na; i += blockDim.x) I.knot_invh[i] = 1.0 / (xk[i + 1] - xk[i]);
+    if (threadIdx.x != 0) return;
+    const Background& B = *I.B;
+    StepScalars& S = *I.sc;
+    S.a = a;
+    S.loga = loga;
+    S.loga0 = loga0;
+    S.Na = Na;
+    S.OmegaNua3 = omega_nu_nopart(B, a) * (a * a * a);
+    S.OmegaNu1 = omega_nu(B, 1);
+    S.partnu = particle_nu_fraction(B, a, 0);
+    S.Omega_nu_tot = omega_nu_nopart(B, a);
+    for (int mi = 0; mi < kNuSpecies; mi++)
+        S.omeganu[mi] = B.deg[mi] > 0 ? B.deg[mi] * omega_nu_single(B, a, mi) : 0.0;
+    S.deriv_prefac = TimeTransfer * (hubble(B, TimeTransfer) / S.light) * TimeTransfer;
+    S.relerr = 1e-6;
+    S.partnu_now = particle_nu_fraction(B, a, 0);
+    S.skip_integral = 0;
+    if (S.partnu_now > 0) {
+        if (1 - S.partnu_now < 1e-3) S.skip_integral = 1;
+        S.relerr /= (1. + 1e-5 - S.partnu_now);
+    }
+    const double OmegaNu_nop = omega_nu_nopart(B, a);
+    const double omega_hybrid = omega_nu(B, a) - OmegaNu_nop;
+    S.kspace_prefac = OmegaNu_nop / (S.Omeganonu / (a * a * a) + omega_hybrid);
+    const double* x = I.scalefact;
+    if (Na > 2) {
+        const int m = Na - 2;
+        for (int i = start_row < 0 ? 0 : start_row; i < m; i++) {
+            const double h0 = x[i + 1] - x[i], h1 = x[i + 2] - x[i + 1];
+            double d = 2.0 * (h0 + h1);
+            if (i > 0) {
+                const double f = h0 * I.knot_invdiag[i - 1];
+                d -= f * h0;
+                I.knot_fac[i] = f;
+            }
+            I.knot_invdiag[i] = 1.0 / d;
+        }
+    }
+}
+
+// ------------------------------------------------------------------ fslength table
+struct GL8 { double x[4], w[4]; };
+
+struct FslIntegrand {  // delta_tot_table.c:378-383
+    const Background* B;
+    __device__ double operator()(double loga) const {
+        const double a = exp(loga);
+        return 1. / a / (a * hubble(*B, a));
+    }
+};
+
+// 8 lanes per segment: lane q evaluates node q of the 8-point Gauss-Legendre rule on
+// [x_i, x_{i+1}] (segment Nfs-1 is the rounding sliver [x_{Nfs-1}, log a]).
+__global__ void k_fs_segments(IntegratorDev I, int Nfs, double loga0, double loga, GL8 gl) {
+    const int gt = blockIdx.x * blockDim.x + threadIdx.x;
+    const int seg = gt >> 3, q = gt & 7;
+    const bool live = seg < Nfs;
+    double v = 0.0;
+    if (live) {
+        const double xa = loga0 + seg * (loga - loga0) / (Nfs - 1.);
+        double xb = loga0 + (seg + 1) * (loga - loga0) / (Nfs - 1.);
+        if (seg == Nfs - 1) xb = loga;
+        if (xb > xa) {
+            const double c = 0.5 * (xa + xb), h = 0.5 * (xb - xa);
+            const int j = q & 3;
+            const double x = (q < 4) ? c - h * gl.x[j] : c + h * gl.x[j];
+            v = gl.w[j] * h * FslIntegrand{I.B}(x);
+        }
+        if (q == 0) I.fs_x[seg] = xa;
+    }
+    // sum the 8 lanes of the segment (fixed order)
+    v += __shfl_down_sync(0xffffffffu, v, 4, 8);
+    v += __shfl_down_sync(0xffffffffu, v, 2, 8);
+    v += __shfl_down_sync(0xffffffffu, v, 1, 8);
+    if (live && q == 0) I.fs_seg[seg] = v;
+}
+
+// One block: suffix sums of the segment integrals -> fslength at every node.
+__global__ void k_fs_finish(IntegratorDev I, int Nfs) {
+    __shared__ double warp_tot[32];
+    const int t = threadIdx.x, nt = blockDim.x, lane = t & 31, w = t >> 5;
+    const int per = (Nfs + nt - 1) / nt;
+    const int i0 = t * per, i1 = min(Nfs, i0 + per);
+    double loc = 0;
+    for (int i = i1 - 1; i >= i0; i--) loc += I.fs_seg[i];
+    // inclusive suffix scan over the threads of a warp, then over warps
+    double v = loc;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        const double n = __shfl_down_sync(0xffffffffu, v, o);
+        if (lane + o < 32) v += n;
+    }
+    if (lane == 0) warp_tot[w] = v;
+    __syncthreads();
+    if (w == 0) {
+        const int nwarps = nt >> 5;
+        double u = lane < nwarps ? warp_tot[lane] : 0.0;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const double n = __shfl_down_sync(0xffffffffu, u, o);
+            if (lane + o < 32) u += n;
+        }
+        if (lane < nwarps) warp_tot[lane] = u;  // inclusive suffix over warps
+    }
+    __syncthreads();
+    const double later_warps = (w + 1 < (nt >> 5)) ? warp_tot[w + 1] : 0.0;
+    double run = v - loc + later_warps;  // exclusive suffix of this thread's chunk
+    const double light = I.sc->light;
+    for (int i = i1 - 1; i >= i0; i--) {
+        run += I.fs_seg[i];
+        I.fs_y[i] = light * run;  // fslength(x_i, log a)
+    }
+    __syncthreads();
+    if (t == 0) {
+        I.sc->fsl_A0a = I.fs_y[0];
+        I.sc->Nfs = Nfs;
+        I.fs_c[0] = 0.0;
+        I.fs_c[Nfs - 1] = 0.0;
+    }
+}
+
+// Natural-spline coefficients of the (uniformly spaced) fslength table, one thread per
+// unknown.  The system is tridiag(1,4,1) c = 3 D^2 y / h^2 with known inverse: for
+// mu = 2 - sqrt(3) and 1-based i <= j,
+//   (T^-1)_{ij} = (-1)^{i+j} mu^{j-i} (1-mu^{2i}) (1-mu^{2(m+1-j)}) / (2 sqrt3 (1-mu^{2(m+1)})).
+// Terms with |i-j| > 40 are below 1e-22 relative and dropped.
+__global__ void k_fs_coeffs(IntegratorDev I, int Nfs, double loga0, double loga) {
+    __shared__ double mupow[82];
+    if (threadIdx.x < 82) {
+        const double mu = 2.0 - sqrt(3.0);
+        double p = 1.0;
+        for (int k = 0; k < (int)threadIdx.x; k++) p *= mu;
+        mupow[threadIdx.x] = p;
+    }
+    __syncthreads();
+    const int m = Nfs - 2;
+    const int u = blockIdx.x * blockDim.x + threadIdx.x;
+    if (u >= m) return;
+    const double h = (loga - loga0) / (Nfs - 1.);
+    const double scale = 3.0 / (h * h) / (2.0 * sqrt(3.0));
+    const double D = (2 * (m + 1) < 82) ? 1.0 - mupow[2 * (m + 1)] : 1.0;
+    const double* y = I.fs_y;
+    double acc = 0;
+    const int vlo = max(0, u - 40), vhi = min(m - 1, u + 40);
+    for (int v = vlo; v <= vhi; v++) {
+        const int d = v > u ? v - u : u - v;
+        const int lo1 = min(u, v) + 1, hi1 = max(u, v) + 1;
+        const double A = (2 * lo1 < 82) ? 1.0 - mupow[2 * lo1] : 1.0;
+        const int e2 = 2 * (m + 1 - hi1);
+        const double Bf = (e2 < 82) ? 1.0 - mupow[e2] : 1.0;
+        const double r = __ldg(y + v + 2) - 2.0 * __ldg(y + v + 1) + __ldg(y + v);
+        acc += ((d & 1) ? -mupow[d] : mupow[d]) * A * Bf * r;
+    }
+    I.fs_c[u + 1] = acc * scale / D;
+}
+
+// ------------------------------------------------------------------ history splines
+// Forward/back substitution of every history row against the shared factorisation.
+__global__ void k_dtot_coeffs(IntegratorDev I, int nk, int Na) {
+    const int ik = blockIdx.x * blockDim.x + threadIdx.x;
+    if (ik >= nk || Na <= 2) return;
+    const double* y = I.dtot + (size_t)ik * I.ld;
+    double* c = I.coef + (size_t)ik * I.ld;
+    const double* ih = I.knot_invh;
+    const int m = Na - 2;
+    double prev = 0;
+    for (int i = 0; i < m; i++) {
+        double r = 3.0 * ((y[i + 2] - y[i + 1]) * ih[i + 1] - (y[i + 1] - y[i]) * ih[i]);
+        if (i > 0) r -= I.knot_fac[i] * prev;
+        prev = r;
+        c[i + 1] = r;
+    }
+    c[0] = 0.0;
+    c[Na - 1] = 0.0;
+    double next = c[m] * I.knot_invdiag[m - 1];
+    c[m] = next;
+    const double* x = I.scalefact;
+    for (int i = m - 1; i-- > 0;) {
+        const double off = x[i + 2] - x[i + 1];
+        next = (c[i + 1] - off * next) * I.knot_invdiag[i];
+        c[i + 1] = next;
+    }
+}
+
+// ------------------------------------------------------------------ delta_nu integral
+struct DnuIntegrand {  // delta_tot_table.c:492-500
+    const Background* B;
+    double k, mnubykT, qc, nufrac_low;
+    const double* fs_x; const double* fs_y; const double* fs_c; int nfs; double fs_x0, fs_inv;
+    const double* kx; const double* ky; const double* kc; int na;
+    __device__ double operator()(double logai) const {
+        // free-streaming spline (uniform knots: direct index, settled against stored knots)
+        int i = (int)((logai - fs_x0) * fs_inv);
+        i = i < 0 ? 0 : (i > nfs - 2 ? nfs - 2 : i);
+        while (i > 0 && logai < __ldg(fs_x + i)) i--;
+        while (i < nfs - 2 && logai >= __ldg(fs_x + i + 1)) i++;
+        double fsl;
+        {
+            const double x0 = __ldg(fs_x + i), x1 = __ldg(fs_x + i + 1);
+            const double y0 = __ldg(fs_y + i), y1 = __ldg(fs_y + i + 1);
+            const double c0 = __ldg(fs_c + i), c1 = __ldg(fs_c + i + 1);
+            const double h = x1 - x0, dx = logai - x0;
+            const double b = (y1 - y0) / h - h * (c1 + 2.0 * c0) / 3.0;
+            const double d = (c1 - c0) / (3.0 * h);
+            fsl = y0 + dx * (b + dx * (c0 + dx * d));
+        }
+        const int j = seg_bsearch(kx, na, logai);
+        const double dt = na > 2 ? cspline_seg(kx, ky, kc, j, logai) : linear_seg(kx, ky, j, logai);
+        const double specJ = specialJ(k * fsl / mnubykT, qc, nufrac_low);
+        const double ai = exp(logai);
+        return fsl / (ai * hubble(*B, ai)) * specJ * dt;
+    }
+};
+
+// Shared memory per CTA: Gk61Nodes | knots[ld] | per warp: QagList, row[ld], coef[ld] | mbarriers
+__global__ void __launch_bounds__(128) k_dnu_qag(IntegratorDev I, int nk, int Na, int nspec, int4 spec_ids) {
+    extern __shared__ __align__(16) unsigned char sm[];
+    Gk61Nodes& N = *reinterpret_cast<Gk61Nodes*>(sm);
+    size_t off = (sizeof(Gk61Nodes) + 15) & ~size_t(15);
+    double* knots = reinterpret_cast<double*>(sm + off);
+    off += sizeof(double) * I.ld;
+    const int nw = blockDim.x >> 5, warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const size_t per_warp = sizeof(QagList) + 2 * sizeof(double) * I.ld;
+    unsigned char* wbase = sm + off + warp * per_warp;
+    QagList& L = *reinterpret_cast<QagList*>(wbase);
+    double* row = reinterpret_cast<double*>(wbase + sizeof(QagList));
+    double* rc = row + I.ld;
+    uint64_t* bars = reinterpret_cast<uint64_t*>(sm + off + nw * per_warp);
+    uint64_t* mybar = bars + warp;
+
+    gk61_fill(N, threadIdx.x, blockDim.x);
+    for (int i = threadIdx.x; i < Na; i += blockDim.x) knots[i] = I.scalefact[i];
+    if (lane == 0) mbar_init(mybar, 1);
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    __syncthreads();
+
+    const Background* B = I.B;
+    const StepScalars& S = *I.sc;
+    const int ntask = nspec * nk;
+    const unsigned row_bytes = (unsigned)(((Na + 1) & ~1) * sizeof(double));
+    unsigned phase = 0;
+    int my_max = 0;
+    long long my_tot = 0;
+    for (int task = blockIdx.x * nw + warp; task < ntask; task += gridDim.x * nw) {
+        const int si = task / nk, ik = task % nk;
+        const int mi = si == 0 ? spec_ids.x : (si == 1 ? spec_ids.y : spec_ids.z);
+        const double mnu = B->mnu[mi];
+        const double mnubykT = mnu / B->kBtnu;
+        const double k = I.wavenum[ik];
+        // initial-condition piece (delta_tot_table.c:525-535); qc = 0 here
+        const double specJ0 = specialJ(k * S.fsl_A0a / (mnubykT > 0 ? mnubykT : 1), 0.0, B->nufrac_low[0]);
+        double val = specJ0 * I.nu_init[ik] * (1. + S.deriv_prefac * S.fsl_A0a);
+        const bool integrate = !S.skip_integral && Na > 1 && mnubykT > 0;
+        if (integrate) {
+            // stage the history row and its spline coefficients (TMA bulk copies)
+            __syncwarp();
+            if (lane == 0) {
+                // order this warp's earlier generic reads of the buffers before the async writes
+                asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+                mbar_expect_tx(mybar, Na > 2 ? 2 * row_bytes : row_bytes);
+                bulk_g2s(row, I.dtot + (size_t)ik * I.ld, row_bytes, mybar);
+                if (Na > 2) bulk_g2s(rc, I.coef + (size_t)ik * I.ld, row_bytes, mybar);
+            }
+            const bool got = mbar_wait_bounded(mybar, phase);
+            phase ^= 1;
+            if (!got) {
+                if (lane == 0) atomicOr(I.status, kStTimeout);
+                // wait (bounded) for the copy still in flight before leaving
+                mbar_wait_bounded(mybar, phase ^ 1);
+                return;
+            }
+            const double qc = S.partnu_now > 0 ? B->vcrit * mnubykT : 0.0;
+            DnuIntegrand f;
+            f.B = B; f.k = k; f.mnubykT = mnubykT; f.qc = qc; f.nufrac_low = B->nufrac_low[0];
+            f.fs_x = I.fs_x; f.fs_y = I.fs_y; f.fs_c = I.fs_c; f.nfs = S.Nfs; f.fs_x0 = S.loga0;
+            f.fs_inv = (S.Nfs - 1.) / (S.loga - S.loga0);
+            f.kx = knots; f.ky = row; f.kc = rc; f.na = Na;
+            QagResult r = qag_warp(f, N, L, S.loga0, S.loga, 0.0, S.relerr, kQagLimit);
+            val += S.prefac * r.result;
+            if (!r.ok && lane == 0) atomicOr(I.status, kStGsl);
+            my_max = max(my_max, r.nint);
+            my_tot += r.nint;
+        }
+        if (lane == 0) I.dnu_s[(size_t)mi * I.nk_alloc + ik] = val;
+    }
+    if (lane == 0 && my_tot) {
+        atomicMax(I.qag_max, my_max);
+        atomicAdd(reinterpret_cast<unsigned long long*>(I.qag_total), (unsigned long long)my_tot);
+    }
+}
+
+// delta_tot_table.c:155-170: combine the species
+__global__ void k_combine(IntegratorDev I, int nk) {
+    const int ik = blockIdx.x * blockDim.x + threadIdx.x;
+    if (ik >= nk) return;
+    const StepScalars& S = *I.sc;
+    double acc = 0;
+    for (int mi = 0; mi < kNuSpecies; mi++)
+        if (I.B->deg[mi] > 0) acc += I.dnu_s[(size_t)mi * I.nk_alloc + ik] * S.omeganu[mi] / S.Omega_nu_tot;
+    I.dnu[ik] = acc;
+}
+
+static GL8 gl8_host() {
+    GL8 g;
+    const int n = 8;
+    for (int i = 0; i < n / 2; i++) {
+        double x = cos(3.14159265358979323846 * (i + 0.75) / (n + 0.5)), dp = 0;
+        for (int it = 0; it < 100; it++) {
+            double p0 = 1, p1 = x;
+            for (int k = 2; k <= n; k++) {
+                const double p2 = ((2 * k - 1) * x * p1 - (k - 1) * p0) / k;
+                p0 = p1;
+                p1 = p2;
+            }
+            dp = n * (x * p1 - p0) / (x * x - 1);
+            const double dx = p1 / dp;
+            x -= dx;
+            if (fabs(dx) < 1e-16) break;
+        }
+        g.x[i] = x;
+        g.w[i] = 2 / ((1 - x * x) * dp * dp);
+    }
+    return g;
+}
+
+size_t dnu_qag_smem(int ld, int wpb) {
+    return ((sizeof(Gk61Nodes) + 15) & ~size_t(15)) + sizeof(double) * ld +
+           wpb * (sizeof(QagList) + 2 * sizeof(double) * ld) + wpb * sizeof(uint64_t);
+}
+
+void launch_delta_nu_combined(const IntegratorDev& I, int nk, int Na, double a, double loga, double loga0,
+                              double TimeTransfer, int start_row, int nspec, const int* spec_ids,
+                              int warps_per_block, cudaStream_t st) {
+    static const GL8 gl = gl8_host();
+    k_scalars<<<1, 256, 0, st>>>(I, Na, a, loga, loga0, TimeTransfer, start_row);
+    if (nk <= 0) return;  // scalars only
+    // the fslength table (always built: it also gives fslength(log a0, log a))
+    const int Nfs = 16 * (Na > 1 ? Na : 1);
+    if (loga > loga0) {
+        const long long threads = 8LL * Nfs;
+        k_fs_segments<<<(unsigned)((threads + 255) / 256), 256, 0, st>>>(I, Nfs, loga0, loga, gl);
+        k_fs_finish<<<1, 1024, 0, st>>>(I, Nfs);
+        if (Nfs > 2) k_fs_coeffs<<<(Nfs - 2 + 127) / 128, 128, 0, st>>>(I, Nfs, loga0, loga);
+    } else {
+        cudaMemsetAsync(&I.sc->fsl_A0a, 0, sizeof(double), st);
+        cudaMemsetAsync(&I.sc->Nfs, 0, sizeof(int), st);
+    }
+    if (Na > 2) k_dtot_coeffs<<<(nk + 127) / 128, 128, 0, st>>>(I, nk, Na);
+    const int wpb = warps_per_block < 1 ? 1 : (warps_per_block > 4 ? 4 : warps_per_block);
+    const size_t smem = dnu_qag_smem(I.ld, wpb);
+    static bool attr_set = false;
+    if (!attr_set) {
+        cudaFuncSetAttribute(k_dnu_qag, cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024);
+        attr_set = true;
+    }
+    const int ntask = nspec * nk;
+    if (ntask > 0) {
+        const int blocks = (ntask + wpb - 1) / wpb;
+        k_dnu_qag<<<blocks, 32 * wpb, smem, st>>>(I, nk, Na, nspec,
+                                                  make_int4(spec_ids[0], spec_ids[1], spec_ids[2], 0));
+    }
+    k_combine<<<(nk + 255) / 256, 256, 0, st>>>(I, nk);
+}
+
+// ------------------------------------------------------------------ end of an update
+// commit_row >= 0: overwrite that row with the final delta_tot (delta_tot_table.c:229-233);
+// -1: the provisional row is dropped; -2: delta_nu_last is returned as is (the
+// same-scale-factor path, delta_tot_table.c:209-213: no NaN check, no clamp).
+__global__ void k_finish(IntegratorDev I, int nk, int commit_row, double a, double loga, const double* keff,
+                         double* dnu_out, double* logk_out, double* ratio_out, CorrTable corr, double* norm_out) {
+    __shared__ double s3[3];
+    const StepScalars& S = *I.sc;
+    const bool pass = commit_row == -2;
+    if (threadIdx.x == 0) {
+        s3[0] = S.OmegaNua3; s3[1] = S.OmegaNu1; s3[2] = S.partnu;
+        if (commit_row >= 0) I.scalefact[commit_row] = loga;
+        if (norm_out) *norm_out = S.kspace_prefac;
+    }
+    __syncthreads();
+    const double norm = S.kspace_prefac;
+    for (int ik = threadIdx.x; ik < nk; ik += blockDim.x) {
+        const double v = I.dnu[ik];
+        double out = v;
+        if (!pass) {
+            I.nu_last[ik] = v;
+            if (commit_row >= 0)
+                I.dtot[(size_t)ik * I.ld + commit_row] =
+                    get_delta_tot(v, I.dcdm[ik], s3[0], S.Omeganonu, s3[1], s3[2]);
+            if (isnan(v)) atomicOr(I.status, kStDnuNaN);
+            out = v < 0 ? 0.0 : v;  // delta_tot_table.c:246-247
+        }
+        dnu_out[ik] = out;
+        if (keff) {
+            if (logk_out) logk_out[ik] = log(keff[ik]);
+            if (ratio_out) ratio_out[ik] = out / I.dcdm[ik];
+        }
+    }
+    __syncthreads();
+    if (keff && corr.xf) {
+        for (int j = threadIdx.x; j < nk; j += blockDim.x) {
+            const double lk = log(keff[j]);
+            const double r = dnu_out[j] / I.dcdm[j];
+            corr.xf[j] = (float)lk;
+            corr.rn[j] = (float)(norm * r);
+            double s = 0;
+            if (j + 1 < nk) {
+                const double lk1 = log(keff[j + 1]);
+                const double r1 = dnu_out[j + 1] / I.dcdm[j + 1];
+                s = norm * (r1 - r) / (lk1 - lk);
+            }
+            corr.sn[j] = (float)s;
+            if (!isfinite(norm * r) || !isfinite(s)) atomicOr(I.status, kStGridNaN);
+        }
+    }
+}
+
+void launch_finish_update(const IntegratorDev& I, int nk, int commit_row, double a, double loga,
+                          const double* keff, double* dnu_out, double* logk_out, double* ratio_out,
+                          CorrTable corr, double* norm_out, cudaStream_t st) {
+    k_finish<<<1, 1024, 0, st>>>(I, nk, commit_row, a, loga, keff, dnu_out, logk_out, ratio_out, corr, norm_out);
+}
+
+}  // namespace ksp

@@ -1,0 +1,114 @@
+// ksp_internal.h -- host-visible structures and kernel launchers shared by the
+// translation units of libkspace_gb300.so.  Not part of the public C ABI.
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+#include "ksp_device.cuh"
+
+namespace ksp {
+
+// Scalars of one integrator call at scale factor a (delta_tot_table.c:153-172,507-548,
+// interface_common.c:139-145), computed on the device by k_scalars.
+struct StepScalars {
+    double a, loga, loga0;           // inputs (logs taken on the host, as the reference does)
+    double light, prefac, Omeganonu; // delta_tot_table.c:52-57
+    double OmegaNua3, OmegaNu1, partnu;  // get_delta_tot coefficients at a (:179-181)
+    double Omega_nu_tot;             // get_omega_nu_nopart(a) (:155)
+    double omeganu[kNuSpecies];      // deg * omega_nu_single(a, mi) (:162)
+    double fsl_A0a;                  // fslength(log a0, log a) (:522)
+    double deriv_prefac;             // a0 * H(a0)/c * a0 (:524)
+    double relerr;                   // 1e-6, loosened for hybrid neutrinos (:547)
+    double partnu_now;               // particle_nu_fraction(a, 0) (:539)
+    double kspace_prefac;            // interface_common.c:139-145
+    int skip_integral;               // particles carry everything (:542-543)
+    int Na, Nfs;
+};
+
+// One integrator instance (the reference's delta_tot_table + omega_nu + transfer table).
+struct IntegratorDev {
+    Background* B;                   // device
+    int nk_alloc, namax, ld;         // ld: padded row length of the history table
+    double* scalefact;               // [namax]
+    double* dtot;                    // [nk_alloc][ld]
+    double* coef;                    // [nk_alloc][ld]  spline coefficients of each row
+    double* nu_init;                 // [nk_alloc]
+    double* nu_last;                 // [nk_alloc]
+    double* wavenum;                 // [nk_alloc]
+    double* dcdm;                    // [nk_alloc] sqrt(P_cdm) of the current call
+    double* dnu_s;                   // [kNuSpecies][nk_alloc] per-species delta_nu
+    double* dnu;                     // [nk_alloc] combined
+    double* knot_invdiag;            // [namax] factorised spline system of the knots
+    double* knot_fac;                // [namax]
+    double* knot_invh;               // [namax] 1/(x_{i+1}-x_i)
+    double* fs_x;                    // [fs_cap]
+    double* fs_y;                    // [fs_cap]
+    double* fs_c;                    // [fs_cap]
+    double* fs_seg;                  // [fs_cap]
+    int fs_cap;
+    double* t_logk;                  // transfer table [ntrans]
+    double* t_T;
+    double* t_c;
+    int ntrans;
+    StepScalars* sc;                 // device scalars
+    unsigned* status;                // device status bits
+    int* qag_max;                    // diagnostics: max intervals of any bin in the last call
+    long long* qag_total;
+};
+
+// Interpolation table for the grid correction (delta_pow.c:19-37), float, per
+// non-empty bin, plus the bin -> compact index map.
+struct CorrTable {
+    float* xf;   // log k of node j
+    float* rn;   // norm * ratio_j
+    float* sn;   // norm * (ratio_{j+1}-ratio_j)/(logk_{j+1}-logk_j)
+    int nk;
+};
+
+// ---- integrator launchers (ksp_integrator.cu)
+void launch_background_tables(Background* dB, double a0, cudaStream_t st, unsigned* status);
+void launch_spline_coeffs_1thread(const double* x, const double* y, double* c, double* scratch, int n,
+                                  cudaStream_t st);
+void launch_nufrac_low(Background* dB, double light, double vcrit, cudaStream_t st, unsigned* status);
+// update_delta_tot (delta_tot_table.c:177-191) for row `row` at scale factor a
+void launch_update_row(const IntegratorDev& I, int nk, int row, double a, double loga, const double* dcdm,
+                       const double* dnu, cudaStream_t st);
+// delta_tot_init part that needs the device (delta_tot_table.c:94-129)
+void launch_delta_tot_init(const IntegratorDev& I, int nk, const double* wavenum, const double* dcdm,
+                           int fresh, double TimeTransfer, cudaStream_t st);
+// get_delta_nu_combined (delta_tot_table.c:153-172) with Na rows: writes I.dnu
+// start_row: leading rows of the knot factorisation still valid from an earlier call
+void launch_delta_nu_combined(const IntegratorDev& I, int nk, int Na, double a, double loga, double loga0,
+                              double TimeTransfer, int start_row, int nspec, const int* spec_ids,
+                              int warps_per_block, cudaStream_t st);
+size_t dnu_qag_smem(int ld, int wpb);
+// end of get_delta_nu_update (delta_tot_table.c:226-248) + interface_common.c:134-146:
+// delta_nu_last, committed row, NaN check, clamp, ratio/log k/kspace_prefac, grid table
+void launch_finish_update(const IntegratorDev& I, int nk, int commit_row, double a, double loga,
+                          const double* keff, double* dnu_out, double* logk_out, double* ratio_out,
+                          CorrTable corr, double* norm_out, cudaStream_t st);
+
+// ---- grid launchers (ksp_grid.cu)
+struct GridGeom {
+    int N, nrbins, slab0, nslab;
+    long long nmodes;               // nslab * N * (N/2+1)
+    int* thresh;                    // device [nrbins+1]: min k^2 of each bin
+    float* w1;                      // device [N/2+1]: 1-D inverse CIC window (float)
+    int* cmap;                      // device [nrbins]: bin -> compact index (-1 empty)
+    float bin_c1;                   // binsperunit * ln2 / 2 (approximate bin estimate)
+};
+// histogram of weighted mode counts over integer k^2 for the slab range
+void launch_k2_histogram(int N, int slab0, int nslab, unsigned long long* hist, cudaStream_t st);
+// K1: per-bin sum of w |F|^2 W^4 (double), and |F(0)|^2 when slab0 == 0
+// returns 0 (TMA kernel), 1 (plain kernel) or -2 (launch error)
+int launch_bin_power(const GridGeom& g, const float* grid, double* bin_sum, double* F0sq, unsigned* status, int tma,
+                     int rows_per_cta, int stages, cudaStream_t st);
+// K3: grid *= 1 + norm * interp(log k)
+int launch_apply_correction(const GridGeom& g, float* grid, CorrTable corr, float lnscale, unsigned* status, int tma,
+                            int rows_per_cta, int stages, cudaStream_t st);
+// normalisation of K1's sums into P(k), delta_cdm, keff (powerspectrum.c:98-115,
+// interface_gadget.c:96-100)
+void launch_finalize_power(const double* bin_sum, const double* F0sq, const long long* count, const double* ksum,
+                           const int* compact_bins, int nk, double BoxSize, double* power_out, double* keff_out,
+                           double* dcdm_out, double* keffphys_out, cudaStream_t st);
+
+}  // namespace ksp
