@@ -98,7 +98,7 @@ int kspace_gpu_set_transfer(kspace_ctx *ctx, const double *logk, const double *T
 /* allocate_transfer_init_table (transfer_init.c:9-83): read a CAMB transfer file. */
 int kspace_gpu_read_transfer_file(kspace_ctx *ctx, double BoxSize, double UnitLength_in_cm,
                                   double InputSpectrum_UnitLength_in_cm, const char *path, int *nrows);
-/* set_nu_state (interface_common.c:166-180): flat delta_tot[nk][ia] */
+/* set_nu_state (interface_common.c:166-180): flat delta_tot[nk][ia] (host or device memory) */
 int kspace_gpu_set_nu_state(kspace_ctx *ctx, const double *scalefact, const double *delta_tot, size_t nk,
                             size_t ia);
 /* get_nu_state (interface_common.c:150-164).  Pass NULL arrays to query nk and ia. */
@@ -139,6 +139,26 @@ int kspace_gpu_apply_delta_pow(kspace_ctx *ctx, double BoxSize, void *grid, int 
 int kspace_gpu_compute_total_power_spectrum(kspace_ctx *ctx, double Time, double BoxSize, const void *grid,
                                             int pmgrid, int slabstart_y, int nslab_y);
 int kspace_gpu_save_total_power(kspace_ctx *ctx, double Time, int snapnum, const char *OutputDir);
+
+/* ---- differentiation (one step with the integrator state held fixed) ---- */
+/* Set delta_nu_init, delta_nu_last and wavenum (nk each) and mark the table initialised:
+ * restores a native snapshot (the reference keeps these in _delta_tot_table,
+ * delta_tot_table.h:40-46) and fixes the state a differentiable step starts from. */
+int kspace_gpu_set_vectors(kspace_ctx *ctx, const double *nu_init, const double *nu_last, const double *wavenum,
+                           int nk);
+/* The mass (eV) inside the free-streaming argument of J per mass state (the mnu
+ * argument of get_delta_nu, delta_tot_table.c:507); NULL restores the background's. */
+int kspace_gpu_set_jmass(kspace_ctx *ctx, const double MNu[3]);
+/* Forward of one step (interface_gadget.c:158-194 without updating the state):
+ * grid_out = grid_in * (1 + correction) and pnu_out[nk] = delta_nu^2.  Device pointers;
+ * grid_out may equal grid_in.  store_intervals keeps each QAG subdivision. */
+int kspace_gpu_diff_forward(kspace_ctx *ctx, double Time, double BoxSize, const void *grid_in, void *grid_out,
+                            int pmgrid, double *pnu_out, int store_intervals);
+/* Adjoint of the last diff_forward: from dL/dgrid_out and dL/dP_nu, produce dL/dgrid_in,
+ * dL/d(history)[nk][ia] (device) and dL/dm per mass state (host, 3).  recompute = 1
+ * re-runs each QAG instead of reading the stored subdivision. */
+int kspace_gpu_diff_backward(kspace_ctx *ctx, const void *gbar_out, const void *grid_in, const double *pnu_bar,
+                             void *gbar_in, double *Dbar, double *mbar, int recompute);
 
 /* ---- diagnostics ---- */
 /* last call: nk, log k, ratio and norm of the correction (arrays of nk_alloc) */

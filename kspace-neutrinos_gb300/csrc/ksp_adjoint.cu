@@ -1,0 +1,510 @@
+// ksp_adjoint.cu -- hand-written adjoint of one neutrino-correction step.
+//
+// The differentiated function is one step at scale factor a with the integrator state
+// (delta_nu_init, delta_nu_last) held fixed:
+//   P_b    = S_b(x) / (|x_0|^2 C_b)                          (binning, K1)
+//   dcdm_b = sqrt(P_b L^3)
+//   D_b,Na-1 = get_delta_tot(delta_nu_last_b, dcdm_b, ...)     (provisional row)
+//   dnu_b  = sum_s w_s [ J(k_b fsl0/m_s) nu_init_b (1+..) + prefac QAG_s,b(D_b, m_s) ]
+//   r_b    = max(dnu_b, 0) / dcdm_b,   P_nu,b = max(dnu_b,0)^2
+//   y_m    = x_m (1 + norm interp_r(log|k_m|))                (correction, K3)
+// Adjoint (subdivision of every QAG held fixed, background Omega_nu(a), H(a) fixed):
+//   B1  k_adj_reduce_plain   rbar_j = norm sum_m (gbar_m . x_m) dinterp/dr_j   (reads gbar, x)
+//   B2a k_adj_bins           dnubar_b from rbar and the P_nu cotangent
+//   B2  k_dnu_adj            warp per (species, bin): history row and spline
+//                            coefficients staged by TMA bulk copies; the GK61 nodes of the
+//                            stored (or recomputed) final QAG intervals give
+//                            d/d(row) through the spline (cubic basis + transposed
+//                            natural-spline solve) and d/dm through J's argument
+//   B2c k_adj_bins2          dcdm/P cotangents -> per-bin Q_b and the DC term
+//   B3  k_adj_grid_plain     xbar_m = gbar_m smth_m + Q_b w_m W_m^4 x_m   (reads gbar, x; writes xbar)
+#include <cuda_runtime.h>
+#include <stdint.h>
+#include "ksp_internal.h"
+#include "ksp_gridutil.cuh"
+
+namespace ksp {
+
+__device__ __forceinline__ uint32_t smem_u32a(const void* p) {
+    return static_cast<uint32_t>(__cvta_generic_to_shared(p));
+}
+__device__ __forceinline__ bool mbar_try_wait_a(uint64_t* bar, unsigned phase) {
+    uint32_t ok;
+    asm volatile(
+        "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}\n"
+        : "=r"(ok)
+        : "r"(smem_u32a(bar)), "r"(phase)
+        : "memory");
+    return ok != 0;
+}
+__device__ __forceinline__ bool mbar_wait_bounded_a(uint64_t* bar, unsigned phase) {
+    for (int it = 0; it < (1 << 22); it++)
+        if (mbar_try_wait_a(bar, phase)) return true;
+    return false;
+}
+
+// d specialJ_fit / dx (derivative of the rational fit of delta_tot_table.c:417-428)
+__device__ __forceinline__ double specialJ_fit_deriv(double x) {
+    if (x <= 0.) return 0.;
+    const double x2 = x * x, x4 = x2 * x2, x8 = x4 * x4;
+    const double p = exp(4.1811 * log(x));
+    const double N = 1. + 0.0168 * x2 + 0.0407 * x4;
+    const double D = 1. + 2.1734 * x2 + 1.6787 * p + 0.1467 * x8;
+    const double dN = 0.0336 * x + 0.1628 * x2 * x;
+    const double dD = 4.3468 * x + 1.6787 * 4.1811 * p / x + 1.1736 * x4 * x2 * x;
+    return (dN * D - N * dD) / (D * D);
+}
+
+// ------------------------------------------------------------------ B1
+// Interpolation weights of the correction for integer k^2 (same segment choice and
+// clamping as corr_delta): node j0 gets w0, node j0+1 gets w1.
+__device__ __forceinline__ void corr_weights(int k2, const GridArgs& g, const CorrSmem& t, int& j0, float& w0,
+                                             float& w1) {
+    const int b = bin_of(k2, g.c1, t.thr, g.nrbins);
+    const int c = t.cmap[b];
+    const float x = fmaf(0.5f, __logf((float)k2), g.lnscale);
+    const int nk = g.nk;
+    if (c < 0) { j0 = 0; w0 = 0.f; w1 = 0.f; return; }
+    if (x < t.xf[c]) {
+        if (c == 0) { j0 = 0; w0 = 1.f; w1 = 0.f; return; }
+        j0 = c - 1;
+    } else {
+        if (c >= nk - 1) { j0 = nk - 2; w0 = 0.f; w1 = 1.f; return; }
+        j0 = c;
+    }
+    const float tt = (x - t.xf[j0]) / (t.xf[j0 + 1] - t.xf[j0]);
+    w0 = 1.f - tt;
+    w1 = tt;
+}
+
+__global__ void k_adj_reduce_plain(GridArgs g, const int* __restrict__ thresh, const int* __restrict__ cmapg,
+                                   CorrTable corr, const float* __restrict__ gbar, const float* __restrict__ x,
+                                   double* node_sum) {
+    extern __shared__ __align__(16) unsigned char sm_raw[];
+    double* s_acc = reinterpret_cast<double*>(sm_raw);  // doubles first: 8-byte aligned
+    int* s_thr = reinterpret_cast<int*>(s_acc + g.nk);
+    int* s_cmap = s_thr + g.nrbins + 1;
+    float* s_tab = reinterpret_cast<float*>(s_cmap + g.nrbins);
+    for (int i = threadIdx.x; i <= g.nrbins; i += blockDim.x) s_thr[i] = thresh[i];
+    for (int i = threadIdx.x; i < g.nrbins; i += blockDim.x) s_cmap[i] = cmapg[i];
+    for (int i = threadIdx.x; i < g.nk; i += blockDim.x) {
+        s_tab[i] = corr.xf[i];
+        s_tab[g.nk + i] = corr.rn[i];
+        s_tab[2 * g.nk + i] = corr.sn[i];
+        s_acc[i] = 0.0;
+    }
+    __syncthreads();
+    CorrSmem T{s_thr, s_cmap, s_tab, s_tab + g.nk, s_tab + 2 * g.nk};
+    // runs keyed by the segment's first node, Kahan-summed in FP32 per node pair
+    int rj = -1;
+    float a0 = 0.f, c0 = 0.f, a1 = 0.f, c1 = 0.f;
+    auto flush = [&]() {
+        if (rj >= 0) {
+            atomicAdd(&s_acc[rj], (double)a0 - (double)c0);
+            if (rj + 1 < g.nk) atomicAdd(&s_acc[rj + 1], (double)a1 - (double)c1);
+        }
+    };
+    for (long long m = blockIdx.x * (long long)blockDim.x + threadIdx.x; m < g.nmodes;
+         m += (long long)gridDim.x * blockDim.x) {
+        const long long r = m / g.nz;
+        const int z = (int)(m - r * g.nz);
+        const int il = (int)(r / g.N), j = (int)(r - (long long)il * g.N);
+        const int kx = kval(g.slab0 + il, g.N), ky = kval(j, g.N);
+        const int k2 = kx * kx + ky * ky + z * z;
+        if (k2 == 0) continue;
+        const float2 gv = reinterpret_cast<const float2*>(gbar)[m];
+        const float2 xv = reinterpret_cast<const float2*>(x)[m];
+        const float v = fmaf(gv.x, xv.x, gv.y * xv.y);
+        int j0;
+        float w0, w1;
+        corr_weights(k2, g, T, j0, w0, w1);
+        if (j0 != rj) {
+            flush();
+            rj = j0; a0 = c0 = a1 = c1 = 0.f;
+        }
+        {
+            const float y = v * w0 - c0, t = a0 + y;
+            c0 = (t - a0) - y; a0 = t;
+        }
+        {
+            const float y = v * w1 - c1, t = a1 + y;
+            c1 = (t - a1) - y; a1 = t;
+        }
+    }
+    flush();
+    __syncthreads();
+    for (int i = threadIdx.x; i < g.nk; i += blockDim.x)
+        if (s_acc[i] != 0.0) atomicAdd(node_sum + i, s_acc[i]);
+}
+
+// ------------------------------------------------------------------ B2a / B2c
+struct AdjBins {
+    const double* node_sum;  // sum over modes of (gbar.x) dinterp/dr_j   [nk]
+    const double* pnu_bar;   // cotangent of P_nu                         [nk]
+    const double* dnu;       // combined delta_nu (unclamped)             [nk]
+    const double* dcdm;      // [nk]
+    const double* power;     // P_b normalised                           [nk]
+    const long long* count;  // mode count per bin (indexed by bin)
+    const int* compact;      // compact -> bin
+    const double* F0sq;
+    double* dnu_bar;         // out [nk]
+    const double* dprov_bar; // provisional-row cotangent (from k_dnu_adj), stride ld
+    double* rbar;            // out [nk]
+    double* Q;               // out: 2 Pbar_b / (F0 C_b), indexed by bin [nrbins]
+    double* dc_sum;          // out: sum_b Pbar_b P_b (DC term)
+    double norm, L3, fcdm;
+    int ld;
+};
+
+__global__ void k_adj_bins(AdjBins A, int nk) {
+    const int b = blockIdx.x * blockDim.x + threadIdx.x;
+    if (b >= nk) return;
+    const double rb = A.norm * A.node_sum[b];
+    A.rbar[b] = rb;
+    const double v = A.dnu[b];
+    const double out = v < 0 ? 0.0 : v;
+    A.dnu_bar[b] = v > 0 ? (2.0 * out * A.pnu_bar[b] + rb / A.dcdm[b]) : 0.0;
+}
+
+__global__ void k_adj_bins2(AdjBins A, int nk) {
+    __shared__ double red[256];
+    double acc = 0;
+    for (int b = threadIdx.x; b < nk; b += blockDim.x) {
+        const double v = A.dnu[b];
+        const double out = v < 0 ? 0.0 : v;
+        const double dc = A.dcdm[b];
+        const double dcbar = -A.rbar[b] * out / (dc * dc) + A.dprov_bar[(size_t)b * A.ld] * A.fcdm;
+        const double Pbar = dcbar * A.L3 / (2.0 * dc);
+        const int bin = A.compact[b];
+        A.Q[bin] = 2.0 * Pbar / (*A.F0sq * (double)A.count[bin]);
+        acc += Pbar * A.power[b];
+    }
+    red[threadIdx.x] = acc;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double s = 0;
+        for (int i = 0; i < (int)blockDim.x; i++) s += red[i];
+        *A.dc_sum = s;
+    }
+}
+
+// ------------------------------------------------------------------ B2
+struct DnuAdjArgs {
+    const double* dnu_bar;   // [nk]
+    double* Dbar;            // [nk][ld] history cotangent (columns < Na)
+    double* mbar;            // [kNuSpecies]
+    const double* ivals;     // stored intervals [kNuSpecies][nk][kQagLimit][2] or null
+    const int* nivals;       // [kNuSpecies][nk]
+    int recompute;
+};
+
+// Node quantities of the delta_nu integrand for one bin (delta_tot_table.c:492-500).
+struct DnuNode {
+    double g, J, Jd, S, xj;
+    int seg;
+    double dx, h;
+};
+
+__device__ __forceinline__ DnuNode dnu_node(const Background* B, double k, double mnubykT, double qc, double nfl,
+                                            const double* fs_x, const double* fs_y, const double* fs_c, int nfs,
+                                            double fs_x0, double fs_inv, const double* kx, const double* ky,
+                                            const double* kc, int na, double logai) {
+    DnuNode o;
+    int i = (int)((logai - fs_x0) * fs_inv);
+    i = i < 0 ? 0 : (i > nfs - 2 ? nfs - 2 : i);
+    while (i > 0 && logai < __ldg(fs_x + i)) i--;
+    while (i < nfs - 2 && logai >= __ldg(fs_x + i + 1)) i++;
+    double fsl;
+    {
+        const double x0 = __ldg(fs_x + i), x1 = __ldg(fs_x + i + 1);
+        const double y0 = __ldg(fs_y + i), y1 = __ldg(fs_y + i + 1);
+        const double c0 = __ldg(fs_c + i), c1 = __ldg(fs_c + i + 1);
+        const double h = x1 - x0, dx = logai - x0;
+        const double b = (y1 - y0) / h - h * (c1 + 2.0 * c0) / 3.0;
+        const double d = (c1 - c0) / (3.0 * h);
+        fsl = y0 + dx * (b + dx * (c0 + dx * d));
+    }
+    const int j = seg_bsearch(kx, na, logai);
+    o.seg = j;
+    o.h = kx[j + 1] - kx[j];
+    o.dx = logai - kx[j];
+    o.S = na > 2 ? cspline_seg(kx, ky, kc, j, logai) : linear_seg(kx, ky, j, logai);
+    o.xj = k * fsl / mnubykT;
+    o.J = specialJ(o.xj, qc, nfl);
+    o.Jd = qc > 0 ? 0.0 : specialJ_fit_deriv(o.xj);
+    const double ai = exp(logai);
+    o.g = fsl / (ai * hubble(*B, ai));
+    return o;
+}
+
+// Shared memory per CTA: Gk61Nodes | knots[ld] | per warp: QagList, row[ld], coef[ld], ybar[ld], cbar[ld] | bars
+__global__ void __launch_bounds__(128) k_dnu_adj(IntegratorDev I, DnuAdjArgs A, int nk, int Na, int nspec,
+                                                 int4 spec_ids) {
+    extern __shared__ __align__(16) unsigned char sm[];
+    Gk61Nodes& N = *reinterpret_cast<Gk61Nodes*>(sm);
+    size_t off = (sizeof(Gk61Nodes) + 15) & ~size_t(15);
+    double* knots = reinterpret_cast<double*>(sm + off);
+    off += sizeof(double) * I.ld;
+    const int nw = blockDim.x >> 5, warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const size_t per_warp = sizeof(QagList) + 4 * sizeof(double) * I.ld;
+    unsigned char* wbase = sm + off + warp * per_warp;
+    QagList& L = *reinterpret_cast<QagList*>(wbase);
+    double* row = reinterpret_cast<double*>(wbase + sizeof(QagList));
+    double* rc = row + I.ld;
+    double* ybar = rc + I.ld;
+    double* cbar = ybar + I.ld;
+    uint64_t* bars = reinterpret_cast<uint64_t*>(sm + off + nw * per_warp);
+    uint64_t* mybar = bars + warp;
+    gk61_fill(N, threadIdx.x, blockDim.x);
+    for (int i = threadIdx.x; i < Na; i += blockDim.x) knots[i] = I.scalefact[i];
+    if (lane == 0) asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_u32a(mybar)) : "memory");
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    __syncthreads();
+    const Background* B = I.B;
+    const StepScalars& S = *I.sc;
+    const unsigned row_bytes = (unsigned)(((Na + 1) & ~1) * sizeof(double));
+    unsigned phase = 0;
+    for (int task = blockIdx.x * nw + warp; task < nspec * nk; task += gridDim.x * nw) {
+        const int si = task / nk, ik = task % nk;
+        const int mi = si == 0 ? spec_ids.x : (si == 1 ? spec_ids.y : spec_ids.z);
+        const double mnu = B->mnu_J[mi];
+        const double mnubykT = mnu / B->kBtnu;
+        const double k = I.wavenum[ik];
+        const double sbar = A.dnu_bar[ik] * S.omeganu[mi] / S.Omega_nu_tot;
+        if (sbar == 0.0) continue;
+        double mder = 0.0;
+        // initial-condition piece (delta_tot_table.c:525-535)
+        if (lane == 0 && mnubykT > 0) {
+            const double x0 = k * S.fsl_A0a / mnubykT;
+            mder += sbar * specialJ_fit_deriv(x0) * (-x0 / mnu) * I.nu_init[ik] * (1. + S.deriv_prefac * S.fsl_A0a);
+        }
+        const bool integrate = !S.skip_integral && Na > 1 && mnubykT > 0;
+        if (integrate) {
+            __syncwarp();
+            if (lane == 0) {
+                asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+                asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32a(mybar)),
+                             "r"(Na > 2 ? 2 * row_bytes : row_bytes)
+                             : "memory");
+                asm volatile(
+                    "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+                        smem_u32a(row)),
+                    "l"(I.dtot + (size_t)ik * I.ld), "r"(row_bytes), "r"(smem_u32a(mybar))
+                    : "memory");
+                if (Na > 2)
+                    asm volatile(
+                        "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+                            smem_u32a(rc)),
+                        "l"(I.coef + (size_t)ik * I.ld), "r"(row_bytes), "r"(smem_u32a(mybar))
+                        : "memory");
+            }
+            for (int i = lane; i < Na; i += 32) { ybar[i] = 0.0; cbar[i] = 0.0; }
+            const bool got = mbar_wait_bounded_a(mybar, phase);
+            phase ^= 1;
+            if (!got) {
+                if (lane == 0) atomicOr(I.status, kStTimeout);
+                mbar_wait_bounded_a(mybar, phase ^ 1);
+                return;
+            }
+            const double qc = S.partnu_now > 0 ? B->vcrit * mnubykT : 0.0;
+            const double fs_inv = (S.Nfs - 1.) / (S.loga - S.loga0);
+            // the final subdivision of the forward QAG: stored, or recomputed (same decisions)
+            int nint;
+            const double* iv = nullptr;
+            if (!A.recompute && A.ivals) {
+                nint = A.nivals[(size_t)mi * I.nk_alloc + ik];
+                iv = A.ivals + ((size_t)mi * I.nk_alloc + ik) * kQagLimit * 2;
+            } else {
+                struct F {
+                    const Background* B; double k, m, qc, nfl; const double *fx, *fy, *fc; int nfs; double x0, inv;
+                    const double *kx, *ky, *kc; int na;
+                    __device__ double operator()(double x) const {
+                        DnuNode o = dnu_node(B, k, m, qc, nfl, fx, fy, fc, nfs, x0, inv, kx, ky, kc, na, x);
+                        return o.g * o.J * o.S;
+                    }
+                } f{B, k, mnubykT, qc, B->nufrac_low[0], I.fs_x, I.fs_y, I.fs_c, S.Nfs, S.loga0, fs_inv, knots, row, rc,
+                    Na};
+                QagResult r = qag_warp(f, N, L, S.loga0, S.loga, 0.0, S.relerr, kQagLimit);
+                nint = r.nint;
+            }
+            for (int q = 0; q < nint; q++) {
+                const double a_i = iv ? iv[2 * q] : L.a[q];
+                const double b_i = iv ? iv[2 * q + 1] : L.b[q];
+                const double c = __dmul_rn(0.5, __dadd_rn(a_i, b_i));
+                const double h = __dmul_rn(0.5, __dsub_rn(b_i, a_i));
+                for (int jn = lane; jn < 61; jn += 32) {
+                    const double xn = __dadd_rn(c, __dmul_rn(h, N.x[jn]));
+                    const DnuNode o = dnu_node(B, k, mnubykT, qc, B->nufrac_low[0], I.fs_x, I.fs_y, I.fs_c, S.Nfs,
+                                               S.loga0, fs_inv, knots, row, rc, Na, xn);
+                    const double wt = N.wk[jn] * h;
+                    const double u = wt * o.g * o.J;
+                    const double t = o.dx / o.h;
+                    atomicAdd(&ybar[o.seg], u * (1 - t));
+                    atomicAdd(&ybar[o.seg + 1], u * t);
+                    if (Na > 2) {
+                        const double dx = o.dx, hh = o.h;
+                        atomicAdd(&cbar[o.seg], u * (dx * (-2 * hh / 3) + dx * dx - dx * dx * dx / (3 * hh)));
+                        atomicAdd(&cbar[o.seg + 1], u * (dx * (-hh / 3) + dx * dx * dx / (3 * hh)));
+                    }
+                    mder += S.prefac * sbar * wt * o.g * o.Jd * (-o.xj / mnu) * o.S;
+                }
+            }
+            __syncwarp();
+            if (lane == 0 && Na > 2) {
+                // z = A^-1 cbar_int with the shared factorisation; ybar += rhs^T z
+                const int m = Na - 2;
+                double prev = 0;
+                for (int u = 0; u < m; u++) {
+                    double r = cbar[u + 1];
+                    if (u > 0) r -= I.knot_fac[u] * prev;
+                    prev = r;
+                    cbar[u + 1] = r;
+                }
+                double next = cbar[m] * I.knot_invdiag[m - 1];
+                cbar[m] = next;
+                for (int u = m - 1; u-- > 0;) {
+                    next = (cbar[u + 1] - (knots[u + 2] - knots[u + 1]) * next) * I.knot_invdiag[u];
+                    cbar[u + 1] = next;
+                }
+                for (int u = 0; u < m; u++) {
+                    const double z = cbar[u + 1];
+                    const double ih0 = I.knot_invh[u], ih1 = I.knot_invh[u + 1];
+                    ybar[u] += 3 * z * ih0;
+                    ybar[u + 1] -= 3 * z * (ih0 + ih1);
+                    ybar[u + 2] += 3 * z * ih1;
+                }
+            }
+            __syncwarp();
+            for (int j = lane; j < Na; j += 32)  // column Na-1: the provisional row
+                atomicAdd(&A.Dbar[(size_t)ik * I.ld + j], S.prefac * sbar * ybar[j]);
+        }
+        mder = warp_sum_to0(mder);
+        if (lane == 0 && mder != 0.0) atomicAdd(&A.mbar[mi], mder);
+    }
+}
+
+// ------------------------------------------------------------------ B3
+__global__ void k_adj_grid_plain(GridArgs g, const int* __restrict__ thresh, const int* __restrict__ cmapg,
+                                 const float* __restrict__ w1g, CorrTable corr, const float* __restrict__ gbar,
+                                 const float* __restrict__ x, float* xbar, const double* __restrict__ Q,
+                                 const double* dc_sum, const double* F0sq) {
+    extern __shared__ unsigned char sm_raw[];
+    int* s_thr = reinterpret_cast<int*>(sm_raw);
+    int* s_cmap = s_thr + g.nrbins + 1;
+    float* s_tab = reinterpret_cast<float*>(s_cmap + g.nrbins);
+    float* s_w1 = s_tab + 3 * g.nk;
+    float* s_Q = s_w1 + g.nz;
+    for (int i = threadIdx.x; i <= g.nrbins; i += blockDim.x) s_thr[i] = thresh[i];
+    for (int i = threadIdx.x; i < g.nrbins; i += blockDim.x) {
+        s_cmap[i] = cmapg[i];
+        s_Q[i] = (float)Q[i];
+    }
+    for (int i = threadIdx.x; i < g.nk; i += blockDim.x) {
+        s_tab[i] = corr.xf[i];
+        s_tab[g.nk + i] = corr.rn[i];
+        s_tab[2 * g.nk + i] = corr.sn[i];
+    }
+    for (int i = threadIdx.x; i < g.nz; i += blockDim.x) s_w1[i] = w1g[i];
+    __syncthreads();
+    CorrSmem T{s_thr, s_cmap, s_tab, s_tab + g.nk, s_tab + 2 * g.nk};
+    unsigned flags = 0;
+    for (long long m = blockIdx.x * (long long)blockDim.x + threadIdx.x; m < g.nmodes;
+         m += (long long)gridDim.x * blockDim.x) {
+        const long long r = m / g.nz;
+        ModeCursor c;
+        c.z = (int)(m - r * g.nz);
+        c.il = (int)(r / g.N);
+        c.j = (int)(r - (long long)c.il * g.N);
+        c.set_row(g, s_w1);
+        const int k2 = c.kxy2 + c.z * c.z;
+        const float2 gv = reinterpret_cast<const float2*>(gbar)[m];
+        const float2 xv = reinterpret_cast<const float2*>(x)[m];
+        float2 o;
+        if (k2 == 0) {
+            // DC: y_0 = x_0, and |x_0|^2 normalises every P_b
+            const double f = -2.0 * (*dc_sum) / (*F0sq);
+            o.x = (float)(gv.x + f * xv.x);
+            o.y = (float)(gv.y + f * xv.y);
+        } else {
+            const float d = corr_delta(k2, g, T, flags);
+            const float t = __fmul_rn(c.iwxy, s_w1[c.z]);
+            const float inv = __fmul_rn(t, t);
+            float wW = __fmul_rn(inv, inv);
+            if (c.z != 0 && c.z != g.half) wW = wW + wW;
+            const float q = s_Q[bin_of(k2, g.c1, s_thr, g.nrbins)] * wW;
+            o.x = fmaf(gv.x, d, gv.x) + q * xv.x;
+            o.y = fmaf(gv.y, d, gv.y) + q * xv.y;
+        }
+        reinterpret_cast<float2*>(xbar)[m] = o;
+    }
+}
+
+// ------------------------------------------------------------------ launchers
+size_t dnu_adj_smem(int ld, int wpb) {
+    return ((sizeof(Gk61Nodes) + 15) & ~size_t(15)) + sizeof(double) * ld +
+           wpb * (sizeof(QagList) + 4 * sizeof(double) * ld) + wpb * sizeof(uint64_t);
+}
+
+static int sm_count_a() {
+    static int n = 0;
+    if (!n) {
+        int dev = 0;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev);
+        if (n <= 0) n = 1;
+    }
+    return n;
+}
+
+void launch_adj_reduce(const GridGeom& gg, CorrTable corr, float lnscale, const float* gbar, const float* x,
+                       double* node_sum, cudaStream_t st) {
+    GridArgs a = make_grid_args(gg, corr.nk, lnscale);
+    const size_t smem = sizeof(double) * corr.nk + sizeof(int) * (2 * gg.nrbins + 1) + sizeof(float) * 3 * corr.nk + 64;
+    cudaFuncSetAttribute(k_adj_reduce_plain, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    long long blocks = (gg.nmodes + 255) / 256;
+    if (blocks > 4LL * sm_count_a()) blocks = 4LL * sm_count_a();
+    k_adj_reduce_plain<<<(int)(blocks > 0 ? blocks : 1), 256, smem, st>>>(a, gg.thresh, gg.cmap, corr, gbar, x,
+                                                                          node_sum);
+}
+
+void launch_adj_bins(const AdjBinsHost& h, cudaStream_t st) {
+    AdjBins A{h.node_sum, h.pnu_bar, h.dnu, h.dcdm, h.power, h.count, h.compact, h.F0sq, h.dnu_bar, h.dprov_bar,
+              h.rbar, h.Q, h.dc_sum, h.norm, h.L3, h.fcdm, h.ld};
+    k_adj_bins<<<(h.nk + 127) / 128, 128, 0, st>>>(A, h.nk);
+}
+
+void launch_adj_bins2(const AdjBinsHost& h, cudaStream_t st) {
+    AdjBins A{h.node_sum, h.pnu_bar, h.dnu, h.dcdm, h.power, h.count, h.compact, h.F0sq, h.dnu_bar, h.dprov_bar,
+              h.rbar, h.Q, h.dc_sum, h.norm, h.L3, h.fcdm, h.ld};
+    k_adj_bins2<<<1, 256, 0, st>>>(A, h.nk);
+}
+
+void launch_dnu_adj(const IntegratorDev& I, const double* dnu_bar, double* Dbar, double* mbar, const double* ivals,
+                    const int* nivals, int recompute, int nk, int Na, int nspec, const int* spec_ids, int wpb,
+                    cudaStream_t st) {
+    DnuAdjArgs A{dnu_bar, Dbar, mbar, ivals, nivals, recompute};
+    wpb = wpb < 1 ? 1 : (wpb > 4 ? 4 : wpb);
+    const size_t smem = dnu_adj_smem(I.ld, wpb);
+    static bool attr = false;
+    if (!attr) {
+        cudaFuncSetAttribute(k_dnu_adj, cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024);
+        attr = true;
+    }
+    const int ntask = nspec * nk;
+    if (ntask <= 0) return;
+    k_dnu_adj<<<(ntask + wpb - 1) / wpb, 32 * wpb, smem, st>>>(I, A, nk, Na, nspec,
+                                                               make_int4(spec_ids[0], spec_ids[1], spec_ids[2], 0));
+}
+
+void launch_adj_grid(const GridGeom& gg, CorrTable corr, float lnscale, const float* gbar, const float* x, float* xbar,
+                     const double* Q, const double* dc_sum, const double* F0sq, cudaStream_t st) {
+    GridArgs a = make_grid_args(gg, corr.nk, lnscale);
+    const size_t smem = sizeof(int) * (2 * gg.nrbins + 1) + sizeof(float) * (3 * corr.nk + a.nz + gg.nrbins) + 64;
+    cudaFuncSetAttribute(k_adj_grid_plain, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    long long blocks = (gg.nmodes + 255) / 256;
+    if (blocks > 8LL * sm_count_a()) blocks = 8LL * sm_count_a();
+    k_adj_grid_plain<<<(int)(blocks > 0 ? blocks : 1), 256, smem, st>>>(a, gg.thresh, gg.cmap, gg.w1, corr, gbar, x,
+                                                                        xbar, Q, dc_sum, F0sq);
+}
+
+}  // namespace ksp

@@ -71,6 +71,16 @@ struct kspace_ctx {
     // staging for host grids
     void* stage_d = nullptr;
     size_t stage_bytes = 0;
+    // differentiable step
+    double Omeganonu = 0;
+    double *ivals_d = nullptr, *adj_node_d = nullptr, *adj_Dbar_d = nullptr, *adj_mbar_d = nullptr;
+    double *adj_Q_d = nullptr, *adj_dcsum_d = nullptr, *adj_dnubar_d = nullptr, *adj_rbar_d = nullptr;
+    int* nivals_d = nullptr;
+    int adj_cap_nb = 0;
+    bool diff_ready = false;
+    int diff_ia = 0, diff_Na = 0, diff_nk = 0, diff_store = 0;
+    double diff_time = 0, diff_box = 0;
+    int diff_pmgrid = 0;
     // profiling
     bool prof = false;
     cudaEvent_t ev[5] = {nullptr, nullptr, nullptr, nullptr, nullptr};
@@ -164,6 +174,15 @@ static void free_table(kspace_ctx* c) {
     c->corr = CorrTable{};
     if (c->ar_h) cudaFreeHost(c->ar_h);
     c->ar_h = nullptr;
+    void* adj[] = {c->ivals_d, c->adj_node_d, c->adj_Dbar_d, c->adj_mbar_d, c->adj_Q_d, c->adj_dcsum_d,
+                   c->adj_dnubar_d, c->adj_rbar_d, c->nivals_d};
+    for (void* p : adj)
+        if (p) cudaFree(p);
+    c->ivals_d = c->adj_node_d = c->adj_Dbar_d = c->adj_mbar_d = c->adj_Q_d = c->adj_dcsum_d = nullptr;
+    c->adj_dnubar_d = c->adj_rbar_d = nullptr;
+    c->nivals_d = nullptr;
+    c->adj_cap_nb = 0;
+    c->diff_ready = false;
     c->table_ready = false;
 }
 
@@ -278,6 +297,7 @@ extern "C" int kspace_gpu_init_omega_nu(kspace_ctx* c, const double MNu[3], doub
     for (int mi = 0; mi < kNuSpecies; mi++) {
         c->MNu[mi] = MNu[mi];
         B.mnu[mi] = MNu[mi];
+        B.mnu_J[mi] = MNu[mi];
         RhoTable& T = B.tab[mi];
         T.mnu = MNu[mi];
         T.has_table = 0;
@@ -414,6 +434,7 @@ extern "C" int kspace_gpu_alloc_table(kspace_ctx* c, int nk_alloc, double TimeTr
     S.light = kLightCgs * UnitTime_in_s / UnitLength_in_cm;                   // :52
     S.prefac = 1.5 * Omega0 * kHubble * kHubble * pow(UnitTime_in_s, 2) / S.light;  // :53
     S.Omeganonu = Omega0 - omega_nu(c->hB, 1);                                 // :55
+    c->Omeganonu = S.Omeganonu;
     CK(cudaMemcpy(I.sc, &S, sizeof(S), cudaMemcpyHostToDevice));
     // step buffers
     c->buf_nb = nk_alloc;
@@ -505,9 +526,9 @@ extern "C" int kspace_gpu_set_nu_state(kspace_ctx* c, const double* scalefact, c
     c->ia = (int)ia;
     for (size_t i = 0; i < ia; i++) c->h_scalefact[i] = scalefact[i];
     CK(cudaMemcpyAsync(I.scalefact, scalefact, sizeof(double) * ia, cudaMemcpyHostToDevice, c->stream));
-    if (ia > 0 && nk > 0)
+    if (ia > 0 && nk > 0)  // delta_tot may be host or device memory
         CK(cudaMemcpy2DAsync(I.dtot, sizeof(double) * I.ld, delta_tot, sizeof(double) * ia, sizeof(double) * ia, nk,
-                             cudaMemcpyHostToDevice, c->stream));
+                             cudaMemcpyDefault, c->stream));
     CK(cudaStreamSynchronize(c->stream));
     c->fact_valid = 0;
     return KSPACE_OK;
@@ -1119,4 +1140,179 @@ extern "C" int kspace_gpu_qag_stats(kspace_ctx* c, int* mx, long long* tot) {
     if (mx) *mx = m;
     if (tot) *tot = t;
     return KSPACE_OK;
+}
+
+// ------------------------------------------------------------------ differentiable step
+extern "C" int kspace_gpu_set_vectors(kspace_ctx* c, const double* nu_init, const double* nu_last,
+                                      const double* wavenum, int nk) {
+    NEED(c && nu_init && nu_last && wavenum, KSPACE_ERR_ARG);
+    NEED(c->table_ready, KSPACE_ERR_ORDER);
+    NEED(nk <= c->I.nk_alloc && nk > 0, KSPACE_ERR_NK_ALLOC);
+    CK(cudaMemcpyAsync(c->I.nu_init, nu_init, sizeof(double) * nk, cudaMemcpyHostToDevice, c->stream));
+    CK(cudaMemcpyAsync(c->I.nu_last, nu_last, sizeof(double) * nk, cudaMemcpyHostToDevice, c->stream));
+    CK(cudaMemcpyAsync(c->I.wavenum, wavenum, sizeof(double) * nk, cudaMemcpyHostToDevice, c->stream));
+    CK(cudaStreamSynchronize(c->stream));
+    c->nk = nk;
+    c->init_done = 1;
+    return KSPACE_OK;
+}
+
+extern "C" int kspace_gpu_set_jmass(kspace_ctx* c, const double* MNu) {
+    NEED(c, KSPACE_ERR_ARG);
+    NEED(c->bg_ready, KSPACE_ERR_ORDER);
+    for (int i = 0; i < kNuSpecies; i++) c->hB.mnu_J[i] = MNu ? MNu[i] : c->hB.mnu[i];
+    CK(cudaMemcpyAsync(&c->dB->mnu_J[0], &c->hB.mnu_J[0], sizeof(double) * kNuSpecies, cudaMemcpyHostToDevice,
+                       c->stream));
+    CK(cudaStreamSynchronize(c->stream));
+    return KSPACE_OK;
+}
+
+__global__ void k_square(const double* v, double* out, int n) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) out[i] = v[i] * v[i];
+}
+
+static int ensure_adj_buffers(kspace_ctx* c, int nrbins) {
+    const size_t nk = c->I.nk_alloc, ld = c->I.ld;
+    if (!c->ivals_d) {
+        CK(dalloc(&c->ivals_d, (size_t)kNuSpecies * nk * kQagLimit * 2));
+        CK(dalloc(&c->nivals_d, (size_t)kNuSpecies * nk));
+        CK(dalloc(&c->adj_node_d, nk));
+        CK(dalloc(&c->adj_Dbar_d, nk * ld));
+        CK(dalloc(&c->adj_mbar_d, kNuSpecies));
+        CK(dalloc(&c->adj_dcsum_d, 1));
+        CK(dalloc(&c->adj_dnubar_d, nk));
+        CK(dalloc(&c->adj_rbar_d, nk));
+    }
+    if (c->adj_cap_nb < nrbins) {
+        if (c->adj_Q_d) cudaFree(c->adj_Q_d);
+        CK(dalloc(&c->adj_Q_d, nrbins));
+        c->adj_cap_nb = nrbins;
+    }
+    return KSPACE_OK;
+}
+
+// One step at `Time` with the integrator state held fixed (interface_gadget.c:158-194
+// without the state update): grid_out = grid_in * (1 + correction); pnu_out = delta_nu^2.
+// Device pointers only.  store_intervals keeps every QAG subdivision for the adjoint.
+extern "C" int kspace_gpu_diff_forward(kspace_ctx* c, double Time, double BoxSize, const void* grid_in,
+                                       void* grid_out, int pmgrid, double* pnu_out, int store_intervals) {
+    NEED(c && grid_in && grid_out && pnu_out, KSPACE_ERR_ARG);
+    NEED(c->table_ready && c->hubble_ready && c->init_done, KSPACE_ERR_ORDER);
+    NEED(is_device_ptr(grid_in) && is_device_ptr(grid_out) && is_device_ptr(pnu_out), KSPACE_ERR_ARG);
+    Geo* G = nullptr;
+    int st = get_geo(c, pmgrid, c->I.nk_alloc, &G);
+    if (st) return st;
+    st = ensure_adj_buffers(c, G->g.nrbins);
+    if (st) return st;
+    st = bin_grid(c, G, reinterpret_cast<const float*>(grid_in), pmgrid, 0, pmgrid, BoxSize);
+    if (st) return st;
+    if (G->nk != c->nk) return KSPACE_ERR_NK_MISMATCH;
+    if (c->ia >= c->I.namax) return KSPACE_ERR_NAMAX;
+    IntegratorDev& I = c->I;
+    const double loga = log(Time);
+    launch_update_row(I, c->nk, c->ia, Time, loga, I.dcdm, I.nu_last, c->stream);
+    const int Na = c->ia + 1;
+    int start = c->fact_valid < Na - 3 ? c->fact_valid : Na - 3;
+    if (start < 0) start = 0;
+    IntegratorDev Is = I;
+    if (store_intervals) {
+        Is.ivals = c->ivals_d;
+        Is.nivals = c->nivals_d;
+    }
+    CK(cudaMemsetAsync(I.qag_max, 0, sizeof(int), c->stream));
+    CK(cudaMemsetAsync(I.qag_total, 0, sizeof(long long), c->stream));
+    launch_delta_nu_combined(Is, c->nk, Na, Time, loga, c->loga0, c->TimeTransfer, start, c->nspec, c->spec_ids,
+                             c->qag_warps, c->stream);
+    c->fact_valid = start;
+    launch_finish_update(I, c->nk, -3, Time, loga, c->keff_d, c->dnu_out_d, c->logk_d, c->ratio_d, c->corr,
+                         c->norm_d, c->stream);
+    k_square<<<(c->nk + 127) / 128, 128, 0, c->stream>>>(c->dnu_out_d, pnu_out, c->nk);
+    g_launches += 10;
+    const size_t bytes = sizeof(float) * 2 * (size_t)pmgrid * pmgrid * (pmgrid / 2 + 1);
+    if (grid_out != grid_in) CK(cudaMemcpyAsync(grid_out, grid_in, bytes, cudaMemcpyDeviceToDevice, c->stream));
+    st = correct_grid(c, G, reinterpret_cast<float*>(grid_out), BoxSize, c->nk);
+    if (st) return st;
+    st = sync_status(c);
+    if (st) return st;
+    c->diff_ready = true;
+    c->diff_ia = c->ia;
+    c->diff_Na = Na;
+    c->diff_nk = c->nk;
+    c->diff_time = Time;
+    c->diff_box = BoxSize;
+    c->diff_store = store_intervals;
+    c->diff_pmgrid = pmgrid;
+    c->last_nk = c->nk;
+    c->last_BoxSize = BoxSize;
+    return KSPACE_OK;
+}
+
+// Adjoint of the last kspace_gpu_diff_forward (no other call in between).
+//   gbar_out: dL/d grid_out (device c64), grid_in: the forward's input (device),
+//   pnu_bar: dL/dP_nu (device, nk), gbar_in: out dL/d grid_in (device c64),
+//   Dbar: out dL/d history (device, [nk][ia] of the current table), mbar: out
+//   dL/dm per mass state (host, 3; through the free-streaming argument of J),
+//   recompute: 1 = re-run every QAG instead of reading the stored subdivisions.
+extern "C" int kspace_gpu_diff_backward(kspace_ctx* c, const void* gbar_out, const void* grid_in,
+                                        const double* pnu_bar, void* gbar_in, double* Dbar, double* mbar,
+                                        int recompute) {
+    NEED(c && gbar_out && grid_in && pnu_bar && gbar_in, KSPACE_ERR_ARG);
+    NEED(c->diff_ready, KSPACE_ERR_ORDER);
+    NEED(recompute || c->diff_store, KSPACE_ERR_ORDER);
+    Geo* G = nullptr;
+    int st = get_geo(c, c->diff_pmgrid, c->I.nk_alloc, &G);
+    if (st) return st;
+    IntegratorDev& I = c->I;
+    const int nk = c->diff_nk, Na = c->diff_Na;
+    const double a = c->diff_time, L = c->diff_box;
+    CK(cudaMemsetAsync(c->adj_node_d, 0, sizeof(double) * nk, c->stream));
+    CK(cudaMemsetAsync(c->adj_Dbar_d, 0, sizeof(double) * (size_t)I.nk_alloc * I.ld, c->stream));
+    CK(cudaMemsetAsync(c->adj_mbar_d, 0, sizeof(double) * kNuSpecies, c->stream));
+    CK(cudaMemsetAsync(c->adj_Q_d, 0, sizeof(double) * G->g.nrbins, c->stream));
+    CorrTable corr = c->corr;
+    corr.nk = nk;
+    const float lnscale = (float)log(2 * kPi / L);
+    G->g.slab0 = 0;
+    G->g.nslab = c->diff_pmgrid;
+    G->g.nmodes = (long long)c->diff_pmgrid * c->diff_pmgrid * (c->diff_pmgrid / 2 + 1);
+    launch_adj_reduce(G->g, corr, lnscale, reinterpret_cast<const float*>(gbar_out),
+                      reinterpret_cast<const float*>(grid_in), c->adj_node_d, c->stream);
+    const Background& B = c->hB;
+    const double OmegaNua3 = omega_nu_nopart(B, a) * (a * a * a);
+    const double OmegaNu1 = omega_nu(B, 1);
+    const double OmegaNu_nop = omega_nu_nopart(B, a);
+    const double norm = OmegaNu_nop / (c->Omeganonu / (a * a * a) + (omega_nu(B, a) - OmegaNu_nop));
+    AdjBinsHost h;
+    h.node_sum = c->adj_node_d;
+    h.pnu_bar = pnu_bar;
+    h.dnu = I.dnu;
+    h.dcdm = I.dcdm;
+    h.power = c->power_d;
+    h.count = G->count_d;
+    h.compact = G->compact_d;
+    h.F0sq = c->F0sq_d;
+    h.dnu_bar = c->adj_dnubar_d;
+    h.dprov_bar = c->adj_Dbar_d + (Na - 1);  // provisional column, stride ld
+    h.rbar = c->adj_rbar_d;
+    h.Q = c->adj_Q_d;
+    h.dc_sum = c->adj_dcsum_d;
+    h.norm = norm;
+    h.L3 = L * L * L;
+    h.fcdm = 1 - OmegaNua3 / (c->Omeganonu + OmegaNu1);
+    h.nk = nk;
+    h.ld = I.ld;
+    launch_adj_bins(h, c->stream);
+    launch_dnu_adj(I, c->adj_dnubar_d, c->adj_Dbar_d, c->adj_mbar_d, c->ivals_d, c->nivals_d, recompute, nk, Na,
+                   c->nspec, c->spec_ids, c->qag_warps, c->stream);
+    launch_adj_bins2(h, c->stream);
+    launch_adj_grid(G->g, corr, lnscale, reinterpret_cast<const float*>(gbar_out),
+                    reinterpret_cast<const float*>(grid_in), reinterpret_cast<float*>(gbar_in), c->adj_Q_d,
+                    c->adj_dcsum_d, c->F0sq_d, c->stream);
+    g_launches += 5;
+    if (Dbar && Na > 1)
+        CK(cudaMemcpy2DAsync(Dbar, sizeof(double) * (Na - 1), c->adj_Dbar_d, sizeof(double) * I.ld,
+                             sizeof(double) * (Na - 1), nk, cudaMemcpyDeviceToDevice, c->stream));
+    if (mbar) CK(cudaMemcpyAsync(mbar, c->adj_mbar_d, sizeof(double) * kNuSpecies, cudaMemcpyDeviceToHost, c->stream));
+    return sync_status(c);
 }

@@ -53,6 +53,7 @@ struct Background {
     double rhocrit, kBtnu, tcmb0, conv, omegag0;
     int deg[kNuSpecies];
     double mnu[kNuSpecies];
+    double mnu_J[kNuSpecies];  // mass inside J's argument (get_delta_nu's mnu, delta_tot_table.c:507)
     int hyb_enabled;
     double nufrac_low[kNuSpecies], nu_crit_time, vcrit;
     double Omega_nonu_H, OmegaLambda, OmegaK, hubble;

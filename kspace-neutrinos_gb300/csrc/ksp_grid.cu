@@ -15,6 +15,7 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 #include "ksp_internal.h"
+#include "ksp_gridutil.cuh"
 
 namespace ksp {
 
@@ -60,131 +61,6 @@ __device__ __forceinline__ void bulk_commit() { asm volatile("cp.async.bulk.comm
 __device__ __forceinline__ void bulk_wait_read_le1() { asm volatile("cp.async.bulk.wait_group.read 1;" ::: "memory"); }
 __device__ __forceinline__ void bulk_wait_all() { asm volatile("cp.async.bulk.wait_group 0;" ::: "memory"); }
 __device__ __forceinline__ void fence_async_smem() { asm volatile("fence.proxy.async.shared::cta;" ::: "memory"); }
-
-// n / d for n < 2^31: m = floor(2^s/d)+1 with s = 31 + ceil(log2 d)
-struct FastDiv {
-    uint32_t d, m;
-    int s;
-};
-static FastDiv make_fastdiv(uint32_t d) {
-    FastDiv f;
-    f.d = d;
-    int l = 0;
-    while ((1u << l) < d) l++;
-    f.s = 31 + l;
-    f.m = (uint32_t)((((unsigned __int128)1) << f.s) / d + 1);
-    return f;
-}
-__device__ __forceinline__ uint32_t fdiv(uint32_t n, const FastDiv& f) {
-    return (uint32_t)(((uint64_t)n * f.m) >> f.s);
-}
-
-struct GridArgs {
-    int N, nz, half, slab0, nrbins, nk;
-    long long nmodes, nrows16;
-    float c1;       // binsperunit * ln2 / 2: bin ~ c1 * log2(k^2)
-    float lnscale;  // log(2 pi / BoxSize) (K3)
-    FastDiv fd_nz, fd_N;
-};
-
-__device__ __forceinline__ int kval(int n, int N) { return n <= N / 2 ? n : n - N; }
-
-// reference bin of integer k^2 >= 1: max b with thresh[b] <= k2
-__device__ __forceinline__ int bin_of(int k2, float c1, const int* thr, int nb) {
-    int b = __float2int_rd(c1 * __log2f((float)k2));
-    b = b < 0 ? 0 : (b > nb - 1 ? nb - 1 : b);
-    while (b > 0 && k2 < thr[b]) b--;
-    while (b < nb - 1 && k2 >= thr[b + 1]) b++;
-    return b;
-}
-
-// Mode coordinates that advance through a row of the slab.
-struct ModeCursor {
-    int il, j, z;       // local slab, second index, z
-    int kxy2;
-    float iwxy;
-    __device__ __forceinline__ void set_row(const GridArgs& g, const float* w1) {
-        const int kx = kval(g.slab0 + il, g.N), ky = kval(j, g.N);
-        kxy2 = kx * kx + ky * ky;
-        iwxy = __fmul_rn(w1[kx < 0 ? -kx : kx], w1[ky < 0 ? -ky : ky]);
-    }
-    __device__ __forceinline__ void init(const GridArgs& g, const float* w1, long long row_base, int z_base, int add) {
-        // row_base/z_base: decoded flat mode index of the tile start; add: modes from there
-        const uint32_t o = (uint32_t)(z_base + add);
-        const uint32_t dr = fdiv(o, g.fd_nz);
-        z = (int)(o - dr * (uint32_t)g.nz);
-        const uint32_t r = (uint32_t)(row_base + dr);
-        const uint32_t i = fdiv(r, g.fd_N);
-        il = (int)i;
-        j = (int)(r - i * (uint32_t)g.N);
-        set_row(g, w1);
-    }
-    __device__ __forceinline__ void next(const GridArgs& g, const float* w1) {
-        if (++z == g.nz) {
-            z = 0;
-            if (++j == g.N) { j = 0; il++; }
-            set_row(g, w1);
-        }
-    }
-};
-
-// Coordinates for K3, which needs only k^2.
-struct KCursor {
-    int il, j, z, kxy2;
-    __device__ __forceinline__ void set_row(const GridArgs& g) {
-        const int kx = kval(g.slab0 + il, g.N), ky = kval(j, g.N);
-        kxy2 = kx * kx + ky * ky;
-    }
-    __device__ __forceinline__ void init(const GridArgs& g, long long row_base, int z_base, int add) {
-        const uint32_t o = (uint32_t)(z_base + add);
-        const uint32_t dr = fdiv(o, g.fd_nz);
-        z = (int)(o - dr * (uint32_t)g.nz);
-        const uint32_t r = (uint32_t)(row_base + dr);
-        const uint32_t i = fdiv(r, g.fd_N);
-        il = (int)i;
-        j = (int)(r - i * (uint32_t)g.N);
-        set_row(g);
-    }
-    __device__ __forceinline__ void next(const GridArgs& g) {
-        if (++z == g.nz) {
-            z = 0;
-            if (++j == g.N) { j = 0; il++; }
-            set_row(g);
-        }
-    }
-};
-
-// K1 contribution of one mode: w |F|^2 W^4, W = product of 1-D inverse windows, with
-// the reference's float arithmetic (powerspectrum.c:16-24,68,76,84).
-__device__ __forceinline__ float mode_power(float re, float im, const ModeCursor& c, const float* w1, int half) {
-    const float t = __fmul_rn(c.iwxy, w1[c.z]);
-    const float inv = __fmul_rn(t, t);
-    const float f = __fmul_rn(inv, inv);
-    const float F2 = __fadd_rn(__fmul_rn(re, re), __fmul_rn(im, im));
-    float p = __fmul_rn(F2, f);
-    if (c.z != 0 && c.z != half) p = p + p;
-    return p;
-}
-
-struct RunAcc {  // Kahan sum of a run of modes in one bin
-    int b = -1;
-    float s = 0.f, cc = 0.f;
-    __device__ __forceinline__ void add(int bin, float p, double* hist) {
-        if (bin == b) {
-            const float y = __fsub_rn(p, cc);
-            const float t = __fadd_rn(s, y);
-            cc = __fsub_rn(__fsub_rn(t, s), y);
-            s = t;
-        } else {
-            flush(hist);
-            b = bin; s = p; cc = 0.f;
-        }
-    }
-    __device__ __forceinline__ void flush(double* hist) {
-        if (b >= 0) atomicAdd(hist + b, (double)s - (double)cc);
-        b = -1;
-    }
-};
 
 // ------------------------------------------------------------------ shared-memory layout
 struct SmemPlan {
@@ -266,12 +142,12 @@ __global__ void __launch_bounds__(ROWS) k_bin_power_tma(const __grid_constant__ 
                 const float4 v = *reinterpret_cast<const float4*>(rp + ((u ^ (tid & 7)) << 4));
                 {
                     const int k2 = c.kxy2 + c.z * c.z;
-                    if (k2 != 0) run.add(bin_of(k2, g.c1, s_thr, g.nrbins), mode_power(v.x, v.y, c, s_w1, g.half), s_hist);
+                    if (k2 != 0) run.add(bin_of(k2, g.c1, s_thr, g.nrbins), mode_power2(v.x, v.y, c, s_w1, g.half), s_hist);
                     c.next(g, s_w1);
                 }
                 {
                     const int k2 = c.kxy2 + c.z * c.z;
-                    if (k2 != 0) run.add(bin_of(k2, g.c1, s_thr, g.nrbins), mode_power(v.z, v.w, c, s_w1, g.half), s_hist);
+                    if (k2 != 0) run.add(bin_of(k2, g.c1, s_thr, g.nrbins), mode_power2(v.z, v.w, c, s_w1, g.half), s_hist);
                     c.next(g, s_w1);
                 }
             }
@@ -305,7 +181,7 @@ __global__ void __launch_bounds__(ROWS) k_bin_power_tma(const __grid_constant__ 
             const int k2 = c.kxy2 + c.z * c.z;
             if (k2 != 0) {
                 const float re = grid[2 * m], im = grid[2 * m + 1];
-                atomicAdd(&s_hist[bin_of(k2, g.c1, s_thr, g.nrbins)], (double)mode_power(re, im, c, s_w1, g.half));
+                atomicAdd(&s_hist[bin_of(k2, g.c1, s_thr, g.nrbins)], mode_power_d(re, im, c, s_w1, g.half));
             }
         }
     }
@@ -340,7 +216,7 @@ __global__ void k_bin_power_plain(GridArgs g, const int* __restrict__ thresh, co
         const int k2 = c.kxy2 + c.z * c.z;
         if (k2 == 0) continue;
         const float2 v = reinterpret_cast<const float2*>(grid)[m];
-        atomicAdd(&s_hist[bin_of(k2, g.c1, s_thr, g.nrbins)], (double)mode_power(v.x, v.y, c, s_w1, g.half));
+        atomicAdd(&s_hist[bin_of(k2, g.c1, s_thr, g.nrbins)], mode_power_d(v.x, v.y, c, s_w1, g.half));
     }
     if (blockIdx.x == 0 && threadIdx.x == 0 && g.slab0 == 0 && g.nmodes > 0) {
         const float re = grid[0], im = grid[1];
@@ -349,29 +225,6 @@ __global__ void k_bin_power_plain(GridArgs g, const int* __restrict__ thresh, co
     __syncthreads();
     for (int i = threadIdx.x; i < g.nrbins; i += blockDim.x)
         if (s_hist[i] != 0.0) atomicAdd(bin_sum + i, s_hist[i]);
-}
-
-// ------------------------------------------------------------------ K3 helpers
-struct CorrSmem {
-    const int* thr; const int* cmap; const float* xf; const float* rn; const float* sn;
-};
-
-// 1 + norm*interp(log k) - 1 for a mode with integer k^2 (delta_pow.c:19-37 clamping)
-__device__ __forceinline__ float corr_delta(int k2, const GridArgs& g, const CorrSmem& t, unsigned& flags) {
-    const int b = bin_of(k2, g.c1, t.thr, g.nrbins);
-    const int c = t.cmap[b];
-    if (c < 0) { flags |= kStGsl; return 0.f; }
-    const float x = fmaf(0.5f, __logf((float)k2), g.lnscale);
-    const int nk = g.nk;
-    if (x < t.xf[c]) {
-        if (c == 0) {
-            if (x < t.xf[0] - 0.69314718f) flags |= kStKWarn;
-            return t.rn[0];
-        }
-        return fmaf(x - t.xf[c - 1], t.sn[c - 1], t.rn[c - 1]);
-    }
-    if (c >= nk - 1) return t.rn[nk - 1];
-    return fmaf(x - t.xf[c], t.sn[c], t.rn[c]);
 }
 
 // ------------------------------------------------------------------ K3 (TMA in/out)
@@ -610,23 +463,6 @@ static bool make_map(CUtensorMap* map, const void* grid, long long nrows16, int 
                CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
 }
 
-static GridArgs make_args(const GridGeom& g, int nk, float lnscale) {
-    GridArgs a;
-    a.N = g.N;
-    a.nz = g.N / 2 + 1;
-    a.half = g.N / 2;
-    a.slab0 = g.slab0;
-    a.nrbins = g.nrbins;
-    a.nk = nk;
-    a.nmodes = g.nmodes;
-    a.nrows16 = g.nmodes / 16;
-    a.c1 = g.bin_c1;
-    a.lnscale = lnscale;
-    a.fd_nz = make_fastdiv((uint32_t)a.nz);
-    a.fd_N = make_fastdiv((uint32_t)g.N);
-    return a;
-}
-
 static int sm_count() {
     static int n = 0;
     if (!n) {
@@ -659,7 +495,7 @@ static int run_bin_tma(const GridGeom& g, const GridArgs& a, const float* grid, 
 
 int launch_bin_power(const GridGeom& g, const float* grid, double* bin_sum, double* F0sq, unsigned* status, int tma,
                      int rows_per_cta, int stages, cudaStream_t st) {
-    const GridArgs a = make_args(g, 0, 0.f);
+    const GridArgs a = make_grid_args(g, 0, 0.f);
     if (tma && a.nrows16 > 0) {
         int r = -1;
         if (rows_per_cta == 256 && stages == 3) r = run_bin_tma<256, 3>(g, a, grid, bin_sum, F0sq, status, st);
@@ -700,7 +536,7 @@ static int run_corr_tma(const GridGeom& g, const GridArgs& a, float* grid, CorrT
 
 int launch_apply_correction(const GridGeom& g, float* grid, CorrTable corr, float lnscale, unsigned* status, int tma,
                             int rows_per_cta, int stages, cudaStream_t st) {
-    const GridArgs a = make_args(g, corr.nk, lnscale);
+    const GridArgs a = make_grid_args(g, corr.nk, lnscale);
     if (tma && a.nrows16 > 0) {
         int r = -1;
         if (rows_per_cta == 256 && stages == 3) r = run_corr_tma<256, 3>(g, a, grid, corr, status, st);

@@ -450,7 +450,7 @@ __global__ void __launch_bounds__(128) k_dnu_qag(IntegratorDev I, int nk, int Na
     for (int task = blockIdx.x * nw + warp; task < ntask; task += gridDim.x * nw) {
         const int si = task / nk, ik = task % nk;
         const int mi = si == 0 ? spec_ids.x : (si == 1 ? spec_ids.y : spec_ids.z);
-        const double mnu = B->mnu[mi];
+        const double mnu = B->mnu_J[mi];
         const double mnubykT = mnu / B->kBtnu;
         const double k = I.wavenum[ik];
         // initial-condition piece (delta_tot_table.c:525-535); qc = 0 here
@@ -483,6 +483,14 @@ __global__ void __launch_bounds__(128) k_dnu_qag(IntegratorDev I, int nk, int Na
             f.kx = knots; f.ky = row; f.kc = rc; f.na = Na;
             QagResult r = qag_warp(f, N, L, S.loga0, S.loga, 0.0, S.relerr, kQagLimit);
             val += S.prefac * r.result;
+            if (I.ivals) {  // keep the final subdivision for the adjoint
+                double* dst = I.ivals + ((size_t)mi * I.nk_alloc + ik) * kQagLimit * 2;
+                for (int q = lane; q < r.nint; q += 32) {
+                    dst[2 * q] = L.a[q];
+                    dst[2 * q + 1] = L.b[q];
+                }
+                if (lane == 0) I.nivals[(size_t)mi * I.nk_alloc + ik] = r.nint;
+            }
             if (!r.ok && lane == 0) atomicOr(I.status, kStGsl);
             my_max = max(my_max, r.nint);
             my_tot += r.nint;
@@ -571,7 +579,8 @@ void launch_delta_nu_combined(const IntegratorDev& I, int nk, int Na, double a, 
 // ------------------------------------------------------------------ end of an update
 // commit_row >= 0: overwrite that row with the final delta_tot (delta_tot_table.c:229-233);
 // -1: the provisional row is dropped; -2: delta_nu_last is returned as is (the
-// same-scale-factor path, delta_tot_table.c:209-213: no NaN check, no clamp).
+// same-scale-factor path, delta_tot_table.c:209-213: no NaN check, no clamp);
+// -3: a differentiable step: like -1 but delta_nu_last is left unchanged.
 __global__ void k_finish(IntegratorDev I, int nk, int commit_row, double a, double loga, const double* keff,
                          double* dnu_out, double* logk_out, double* ratio_out, CorrTable corr, double* norm_out) {
     __shared__ double s3[3];
@@ -588,7 +597,7 @@ __global__ void k_finish(IntegratorDev I, int nk, int commit_row, double a, doub
         const double v = I.dnu[ik];
         double out = v;
         if (!pass) {
-            I.nu_last[ik] = v;
+            if (commit_row != -3) I.nu_last[ik] = v;
             if (commit_row >= 0)
                 I.dtot[(size_t)ik * I.ld + commit_row] =
                     get_delta_tot(v, I.dcdm[ik], s3[0], S.Omeganonu, s3[1], s3[2]);

@@ -53,6 +53,8 @@ struct IntegratorDev {
     unsigned* status;                // device status bits
     int* qag_max;                    // diagnostics: max intervals of any bin in the last call
     long long* qag_total;
+    double* ivals;                   // optional: final QAG intervals [kNuSpecies][nk_alloc][kQagLimit][2]
+    int* nivals;                     // [kNuSpecies][nk_alloc]
 };
 
 // Interpolation table for the grid correction (delta_pow.c:19-37), float, per
@@ -87,6 +89,16 @@ void launch_finish_update(const IntegratorDev& I, int nk, int commit_row, double
                           const double* keff, double* dnu_out, double* logk_out, double* ratio_out,
                           CorrTable corr, double* norm_out, cudaStream_t st);
 
+// ---- adjoint (ksp_adjoint.cu)
+struct AdjBinsHost {
+    const double* node_sum; const double* pnu_bar; const double* dnu; const double* dcdm; const double* power;
+    const long long* count; const int* compact; const double* F0sq;
+    double* dnu_bar; double* dprov_bar; double* rbar; double* Q; double* dc_sum;
+    double norm, L3, fcdm;
+    int nk, ld;  // dprov_bar has stride ld
+};
+size_t dnu_adj_smem(int ld, int wpb);
+
 // ---- grid launchers (ksp_grid.cu)
 struct GridGeom {
     int N, nrbins, slab0, nslab;
@@ -110,5 +122,16 @@ int launch_apply_correction(const GridGeom& g, float* grid, CorrTable corr, floa
 void launch_finalize_power(const double* bin_sum, const double* F0sq, const long long* count, const double* ksum,
                            const int* compact_bins, int nk, double BoxSize, double* power_out, double* keff_out,
                            double* dcdm_out, double* keffphys_out, cudaStream_t st);
+
+struct GridGeom;
+void launch_adj_reduce(const GridGeom& gg, CorrTable corr, float lnscale, const float* gbar, const float* x,
+                       double* node_sum, cudaStream_t st);
+void launch_adj_bins(const AdjBinsHost& h, cudaStream_t st);
+void launch_adj_bins2(const AdjBinsHost& h, cudaStream_t st);
+void launch_dnu_adj(const IntegratorDev& I, const double* dnu_bar, double* Dbar, double* mbar, const double* ivals,
+                    const int* nivals, int recompute, int nk, int Na, int nspec, const int* spec_ids, int wpb,
+                    cudaStream_t st);
+void launch_adj_grid(const GridGeom& gg, CorrTable corr, float lnscale, const float* gbar, const float* x, float* xbar,
+                     const double* Q, const double* dc_sum, const double* F0sq, cudaStream_t st);
 
 }  // namespace ksp

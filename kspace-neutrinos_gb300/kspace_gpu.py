@@ -64,6 +64,10 @@ _SIGS = {
     "kspace_gpu_stage_times": (_i, [_vp, C.POINTER(C.c_float)]),
     "kspace_gpu_qag_stats": (_i, [_vp, _PI, _PLL]),
     "kspace_gpu_launch_count": (C.c_longlong, [_vp]),
+    "kspace_gpu_set_vectors": (_i, [_vp, _PD, _PD, _PD, _i]),
+    "kspace_gpu_set_jmass": (_i, [_vp, _PD]),
+    "kspace_gpu_diff_forward": (_i, [_vp, _d, _d, _vp, _vp, _i, _vp, _i]),
+    "kspace_gpu_diff_backward": (_i, [_vp, _vp, _vp, _vp, _vp, _vp, _PD, _i]),
 }
 
 _lib = None
@@ -335,6 +339,29 @@ class KspaceNeutrinos:
 
     def save_total_power(self, Time, snapnum, OutputDir):
         return self.L.kspace_gpu_save_total_power(self.h, Time, snapnum, OutputDir.encode())
+
+    # ---- differentiation
+    def set_vectors(self, nu_init, nu_last, wavenum):
+        a, b, c = _f64(nu_init), _f64(nu_last), _f64(wavenum)
+        _check(self.L.kspace_gpu_set_vectors(self.h, _pd(a), _pd(b), _pd(c), len(a)), "set_vectors")
+
+    def set_jmass(self, MNu=None):
+        if MNu is None:
+            _check(self.L.kspace_gpu_set_jmass(self.h, None), "set_jmass")
+        else:
+            m = _f64(MNu)
+            _check(self.L.kspace_gpu_set_jmass(self.h, _pd(m)), "set_jmass")
+
+    def diff_forward(self, Time, BoxSize, grid_in, grid_out, pmgrid, pnu_out, store_intervals=True):
+        _check(self.L.kspace_gpu_diff_forward(self.h, Time, BoxSize, grid_in.data_ptr(), grid_out.data_ptr(),
+                                              pmgrid, pnu_out.data_ptr(), int(store_intervals)), "diff_forward")
+
+    def diff_backward(self, gbar_out, grid_in, pnu_bar, gbar_in, Dbar, recompute=False):
+        mbar = np.zeros(3)
+        _check(self.L.kspace_gpu_diff_backward(self.h, gbar_out.data_ptr(), grid_in.data_ptr(), pnu_bar.data_ptr(),
+                                               gbar_in.data_ptr(), Dbar.data_ptr() if Dbar is not None else None,
+                                               _pd(mbar), int(recompute)), "diff_backward")
+        return mbar
 
     # ---- diagnostics
     def last_correction(self):

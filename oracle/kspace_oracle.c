@@ -345,7 +345,8 @@ static double fslength_int(double loga, void *params)
     return 1. / a / (a * ko_hubble(bg, a));
 }
 
-static double qag_run(gsl_function *F, double a, double b, double epsrel, int *status)
+static double qag_run_keep(gsl_function *F, double a, double b, double epsrel, int *status,
+                           gsl_integration_workspace **keep)
 {
     gsl_integration_workspace *w = gsl_integration_workspace_alloc(GSL_VAL);
     double r = 0, e;
@@ -353,8 +354,15 @@ static double qag_run(gsl_function *F, double a, double b, double epsrel, int *s
     gsl_integration_qag(F, a, b, 0, epsrel, GSL_VAL, 6, w, &r, &e);
     if (g_gsl_err && status && !*status)
         *status = 2001;
-    gsl_integration_workspace_free(w);
+    if (keep)
+        *keep = w;
+    else
+        gsl_integration_workspace_free(w);
     return r;
+}
+static double qag_run(gsl_function *F, double a, double b, double epsrel, int *status)
+{
+    return qag_run_keep(F, a, b, epsrel, status, NULL);
 }
 
 /* delta_tot_table.c:394-407 */
@@ -413,6 +421,15 @@ struct ko_state {
     long long last_total_intervals;
     int last_nfs;
     double *last_fs_scales, *last_fs_lengths;
+    /* differentiation support (test infrastructure): mass used inside J per species,
+     * and the adjoint accumulators filled when adj_dnu_bar is set */
+    int mJ_set;
+    double mJ[NUSPECIES];
+    const double *adj_dnu_bar;
+    double *adj_Dbar;       /* [nk][Na] */
+    double adj_mbar[NUSPECIES];
+    double adj_weight;      /* omega_s / Omega_nu_tot of the species being integrated */
+    int adj_species;
 };
 
 /* delta_tot_table.c:25-60 */
@@ -610,6 +627,95 @@ static void fs_table(ko_state *s, double a, int Nfs, double *fsscales, double *f
     }
 }
 
+/* d specialJ_fit / dx (derivative of the rational fit of delta_tot_table.c:417-428) */
+static double specialJ_fit_deriv(double x)
+{
+    if (x <= 0.)
+        return 0.;
+    const double x2 = x * x, x4 = x2 * x2, x8 = x4 * x4;
+    const double p = exp(4.1811 * log(x));
+    const double N = 1. + 0.0168 * x2 + 0.0407 * x4;
+    const double D = 1. + 2.1734 * x2 + 1.6787 * p + 0.1467 * x8;
+    const double dN = 0.0336 * x + 0.1628 * x2 * x;
+    const double dD = 4.3468 * x + 1.6787 * 4.1811 * p / x + 1.1736 * x4 * x2 * x;
+    return (dN * D - N * dD) / (D * D);
+}
+
+/* Adjoint of one bin's time integral over the final QAG subdivision in w: the
+ * derivative of the computed Kronrod sums with the subdivision held fixed.  Adds
+ * prefac*sbar*d(integral)/d(row values) to Dbar_row[Na] and returns
+ * d(integral)/d(mass) (J argument only). */
+static double adj_bin(const ko_state *s, const dnu_params *p, const gsl_integration_workspace *w, int Na,
+                      double *Dbar_row, double sbar)
+{
+    static const double XK[31] = KSP_GK61_XK_INIT;
+    static const double WK[31] = KSP_GK61_WK_INIT;
+    double *ybar = (double *)calloc(2 * (size_t)Na, sizeof(double));
+    double *cbar = ybar + Na;
+    const double *x = p->scale, *y = p->delta_tot;
+    const double *cc = Na > 2 ? p->spline->c : NULL;
+    double mder = 0;
+    for (size_t iv = 0; iv < w->size; iv++) {
+        const double c = 0.5 * (w->alist[iv] + w->blist[iv]), h = 0.5 * (w->blist[iv] - w->alist[iv]);
+        for (int jn = 0; jn < 61; jn++) {
+            const double xn = jn < 30 ? c - h * XK[jn] : (jn < 60 ? c + h * XK[jn - 30] : c);
+            const double wt = (jn < 60 ? WK[jn % 30] : WK[30]) * h;
+            const double fsl = gsl_interp_eval(p->fs_spline, p->fsscales, p->fslengths, xn, NULL);
+            size_t lo = 0, hi = (size_t)Na - 1;
+            while (hi > lo + 1) {
+                const size_t mid = (lo + hi) / 2;
+                if (x[mid] > xn) hi = mid; else lo = mid;
+            }
+            const size_t i = lo;
+            const double hh = x[i + 1] - x[i], dx = xn - x[i];
+            const double S = gsl_interp_eval(p->spline, p->scale, p->delta_tot, xn, NULL);
+            const double xj = p->k * fsl / p->mnubykT;
+            const double J = ko_specialJ(xj, p->qc, p->nufrac_low);
+            const double ai = exp(xn);
+            const double g = fsl / (ai * ko_hubble(p->bg, ai));
+            const double u = wt * g * J;
+            ybar[i] += u * (1 - dx / hh);
+            ybar[i + 1] += u * (dx / hh);
+            if (cc) {
+                cbar[i] += u * (dx * (-2 * hh / 3) + dx * dx - dx * dx * dx / (3 * hh));
+                cbar[i + 1] += u * (dx * (-hh / 3) + dx * dx * dx / (3 * hh));
+            }
+            if (p->qc <= 0)
+                mder += wt * g * specialJ_fit_deriv(xj) * (-xj / (p->mnubykT * s->bg->kBtnu)) * S;
+        }
+    }
+    if (cc && Na > 2) {
+        /* c (interior) = A^-1 rhs(y); z = A^-1 cbar (A symmetric), ybar += rhs^T z */
+        const int m = Na - 2;
+        double *diag = (double *)malloc(2 * (size_t)m * sizeof(double));
+        double *z = diag + m;
+        for (int u = 0; u < m; u++) {
+            diag[u] = 2.0 * ((x[u + 1] - x[u]) + (x[u + 2] - x[u + 1]));
+            z[u] = cbar[u + 1];
+        }
+        for (int u = 1; u < m; u++) {
+            const double off = x[u + 1] - x[u];
+            const double f = off / diag[u - 1];
+            diag[u] -= f * off;
+            z[u] -= f * z[u - 1];
+        }
+        z[m - 1] /= diag[m - 1];
+        for (int u = m - 1; u-- > 0;)
+            z[u] = (z[u] - (x[u + 2] - x[u + 1]) * z[u + 1]) / diag[u];
+        for (int u = 0; u < m; u++) {
+            const double ih0 = 1.0 / (x[u + 1] - x[u]), ih1 = 1.0 / (x[u + 2] - x[u + 1]);
+            ybar[u] += 3 * z[u] * ih0;
+            ybar[u + 1] -= 3 * z[u] * (ih0 + ih1);
+            ybar[u + 2] += 3 * z[u] * ih1;
+        }
+        free(diag);
+    }
+    for (int j = 0; j < Na; j++)
+        Dbar_row[j] += s->prefac * sbar * ybar[j];
+    free(ybar);
+    return mder;
+}
+
 /* delta_tot_table.c:507-611 */
 int ko_get_delta_nu(ko_state *s, double a, const double *wavenum, double *dnu, double mnu)
 {
@@ -628,6 +734,11 @@ int ko_get_delta_nu(ko_state *s, double a, const double *wavenum, double *dnu, d
     for (int ik = 0; ik < s->nk; ik++) {
         const double specJ = ko_specialJ(wavenum[ik] * fsl_A0a / (mnubykT > 0 ? mnubykT : 1), qc, bg->nufrac_low[0]);
         dnu[ik] = specJ * s->nu_init[ik] * (1. + deriv_prefac * fsl_A0a);
+        if (s->adj_dnu_bar && mnubykT > 0) {
+            const double x0 = wavenum[ik] * fsl_A0a / mnubykT;
+            s->adj_mbar[s->adj_species] += s->adj_dnu_bar[ik] * s->adj_weight * specialJ_fit_deriv(x0) * (-x0 / mnu) *
+                                           s->nu_init[ik] * (1. + deriv_prefac * fsl_A0a);
+        }
     }
     const double partnu = ko_particle_nu_fraction(bg, a, 0);
     if (partnu > 0) {
@@ -667,7 +778,14 @@ int ko_get_delta_nu(ko_state *s, double a, const double *wavenum, double *dnu, d
             gsl_interp_init(p.spline, p.scale, p.delta_tot, Na);
             double d_nu_tmp = 0;
             if (!s->exact) {
-                d_nu_tmp = qag_run(&F, log(s->TimeTransfer), log(a), relerr, &status);
+                gsl_integration_workspace *wk = NULL;
+                d_nu_tmp = qag_run_keep(&F, log(s->TimeTransfer), log(a), relerr, &status, &wk);
+                if (s->adj_dnu_bar) {
+                    const double sbar = s->adj_dnu_bar[ik] * s->adj_weight;
+                    s->adj_mbar[s->adj_species] +=
+                        s->prefac * sbar * adj_bin(s, &p, wk, Na, s->adj_Dbar + (size_t)ik * Na, sbar);
+                }
+                gsl_integration_workspace_free(wk);
                 const int ni = gslsub_last_qag_intervals();
                 if (ni > s->last_max_intervals)
                     s->last_max_intervals = ni;
@@ -720,7 +838,9 @@ int ko_get_delta_nu_combined(ko_state *s, double a, const double *wavenum, doubl
     for (int mi = 0; mi < NUSPECIES; mi++) {
         if (bg->deg[mi] > 0) {
             const double omeganu = bg->deg[mi] * ko_omega_nu_single(bg, a, mi);
-            int st = ko_get_delta_nu(s, a, wavenum, single, bg->tab[mi].mnu);
+            s->adj_weight = omeganu / Omega_nu_tot;
+            s->adj_species = mi;
+            int st = ko_get_delta_nu(s, a, wavenum, single, s->mJ_set ? s->mJ[mi] : bg->tab[mi].mnu);
             if (st && !status)
                 status = st;
             for (int ik = 0; ik < s->nk; ik++)
@@ -1157,5 +1277,59 @@ int ko_add_nu_power_to_rhogrid(ko_state *s, double Time, double BoxSize, float *
     free(keff);
     free(dnu);
     free(count);
+    return st;
+}
+
+/* ================================================================== differentiation (test infrastructure) */
+int ko_state_set_vectors(ko_state *s, const double *nu_init, const double *nu_last, const double *wavenum, int nk)
+{
+    if (nk > s->nk_alloc)
+        return 2011;
+    s->nk = nk;
+    memcpy(s->nu_init, nu_init, nk * sizeof(double));
+    memcpy(s->nu_last, nu_last, nk * sizeof(double));
+    memcpy(s->wavenum, wavenum, nk * sizeof(double));
+    s->init_done = 1;
+    return 0;
+}
+
+void ko_state_set_jmass(ko_state *s, const double *mJ)
+{
+    if (!mJ) {
+        s->mJ_set = 0;
+        return;
+    }
+    s->mJ_set = 1;
+    for (int i = 0; i < NUSPECIES; i++)
+        s->mJ[i] = mJ[i];
+}
+
+/* One integrator call at a that leaves the state unchanged: provisional row from dcdm
+ * and delta_nu_last (delta_tot_table.c:222), delta_nu (unclamped), row dropped.  With
+ * dnu_bar: D_bar[nk][Na] (Na = ia+1; column Na-1 is the provisional row) and the
+ * derivative with respect to the mass inside J, per species. */
+int ko_dnu_diff(ko_state *s, double a, const double *wavenum, const double *dcdm, double *dnu, const double *dnu_bar,
+                double *D_bar, double *mJ_bar)
+{
+    if (!s->init_done)
+        return 10003;
+    int st = update_delta_tot(s, a, dcdm, s->nu_last, 0);
+    if (st)
+        return st;
+    const int Na = s->ia;
+    if (dnu_bar) {
+        s->adj_dnu_bar = dnu_bar;
+        s->adj_Dbar = D_bar;
+        memset(D_bar, 0, (size_t)s->nk * Na * sizeof(double));
+        memset(s->adj_mbar, 0, sizeof(s->adj_mbar));
+    }
+    st = ko_get_delta_nu_combined(s, a, wavenum, dnu);
+    if (dnu_bar) {
+        for (int i = 0; i < NUSPECIES; i++)
+            mJ_bar[i] = s->adj_mbar[i];
+        s->adj_dnu_bar = NULL;
+        s->adj_Dbar = NULL;
+    }
+    s->ia--;
     return st;
 }

@@ -102,6 +102,15 @@ int ko_add_nu_power_to_rhogrid(ko_state *s, double Time, double BoxSize, float *
                                int nslab, int nthreads, int *nk_out, double *keff, double *dcdm, double *dnu,
                                double *logk, double *ratio, double *norm, double *t_stages);
 
+/* ---- differentiation support ---- */
+/* set delta_nu_init, delta_nu_last, wavenum and mark the table initialised */
+int ko_state_set_vectors(ko_state *s, const double *nu_init, const double *nu_last, const double *wavenum, int nk);
+/* mass (eV) used inside J per species (NULL: the background's masses) */
+void ko_state_set_jmass(ko_state *s, const double *mJ);
+/* integrator call that leaves the state unchanged; optional FP64 adjoint */
+int ko_dnu_diff(ko_state *s, double a, const double *wavenum, const double *dcdm, double *dnu, const double *dnu_bar,
+                double *D_bar, double *mJ_bar);
+
 #ifdef __cplusplus
 }
 #endif

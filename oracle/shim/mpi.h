@@ -17,6 +17,7 @@ typedef int MPI_Op;
 #define MPI_BYTE 4
 #define MPI_LONG 5
 #define MPI_SUM 1
+#define MPI_SUCCESS 0
 #define MPI_IN_PLACE ((void *)1)
 #ifdef __cplusplus
 extern "C" {
@@ -51,6 +52,7 @@ static inline int MPI_Bcast(void *buf, int count, MPI_Datatype dt, int root, MPI
 static inline int MPI_Barrier(MPI_Comm comm) { (void)comm; return 0; }
 static inline int MPI_Abort(MPI_Comm comm, int code) { (void)comm; exit(code); return 0; }
 static inline int MPI_Comm_rank(MPI_Comm comm, int *rank) { (void)comm; *rank = 0; return 0; }
+static inline int MPI_Comm_size(MPI_Comm comm, int *size) { (void)comm; *size = 1; return 0; }
 static inline int MPI_Init(int *argc, char ***argv) { (void)argc; (void)argv; return 0; }
 static inline int MPI_Finalize(void) { return 0; }
 #endif
