@@ -160,6 +160,49 @@ int kspace_gpu_diff_forward(kspace_ctx *ctx, double Time, double BoxSize, const 
 int kspace_gpu_diff_backward(kspace_ctx *ctx, const void *gbar_out, const void *grid_in, const double *pnu_bar,
                              void *gbar_in, double *Dbar, double *mbar, int recompute);
 
+/* ---- batches of independent instances ----
+ * No counterpart in the reference, which holds one integrator per process.  A batch
+ * advances many contexts (each a complete integrator: its own cosmology, masses,
+ * transfer table, history length and k bins) with one captured sequence of kernels;
+ * each instance's delta_nu is the one kspace_gpu_get_delta_nu_update would return.
+ * Every context must be on the batch's device with its table, transfer function and
+ * H(a) set; while it belongs to a batch it is driven only through the batch.
+ * Per-instance bin arrays are concatenated ("pools"): instance i owns entries
+ * [offset[i], offset[i+1]). */
+typedef struct kspace_batch kspace_batch;
+int kspace_gpu_batch_create(kspace_batch **batch, kspace_ctx *const *ctxs, int M);
+int kspace_gpu_batch_destroy(kspace_batch *batch);
+/* Bind instance `inst` to a device grid (complex64, pmgrid x pmgrid x (pmgrid/2+1),
+ * fixed address): every step bins it into the instance's delta_cdm (nrbins = the
+ * context's nk_alloc, as add_nu_power_to_rhogrid) and corrects it in place afterwards.
+ * Must precede kspace_gpu_batch_init. */
+int kspace_gpu_batch_bind_grid(kspace_batch *batch, int inst, void *grid, int pmgrid, double BoxSize);
+/* First call of every instance (delta_tot_init, delta_tot_table.c:79-149) at a[i]:
+ * nk[i] bins with keff (physical k) and sqrt(P_cdm) in host pools laid out by nk.
+ * Bound instances take nk, keff and delta_cdm from their grid (their entries are
+ * ignored; pass nk[i] = 0).  Fixes the layout (kspace_gpu_batch_layout). */
+int kspace_gpu_batch_init(kspace_batch *batch, const double *a, const int *nk, const double *keff,
+                          const double *dcdm);
+/* nk[M] and offset[M+1] of the pools */
+int kspace_gpu_batch_layout(kspace_batch *batch, int *nk, int *offset);
+/* One step of every instance at a[i] (get_delta_nu_update, delta_tot_table.c:193-250):
+ * dcdm = sqrt(P_cdm) pool (host or device; NULL when every instance is bound to a
+ * grid), dnu = delta_nu pool out (host or device; NULL to keep it on the device).
+ * Returns the first instance's non-zero status (kspace_gpu_batch_status has all). */
+int kspace_gpu_batch_step(kspace_batch *batch, const double *a, const double *dcdm, double *dnu);
+/* per-instance status of the last step */
+int kspace_gpu_batch_status(kspace_batch *batch, int *status);
+/* warps per block (1..4) and resident blocks per SM of the integral kernel; use_graph
+ * = 0 launches the kernels one by one instead of replaying the captured graph */
+int kspace_gpu_batch_set_tuning(kspace_batch *batch, int warps_per_block, int blocks_per_sm, int use_graph);
+/* Time each (warps per block, blocks per SM) candidate on `reps` dry steps at a[i]
+ * (nothing committed, no state changed) and keep the fastest.  best[2] and its time
+ * (ms) are returned. */
+int kspace_gpu_batch_autotune(kspace_batch *batch, const double *a, const double *dcdm, int reps, int *best,
+                              float *best_ms);
+/* device time (ms) of the last step's kernels */
+int kspace_gpu_batch_last_ms(kspace_batch *batch, float *ms);
+
 /* ---- diagnostics ---- */
 /* last call: nk, log k, ratio and norm of the correction (arrays of nk_alloc) */
 int kspace_gpu_last_correction(kspace_ctx *ctx, int *nk, double *logk, double *ratio, double *norm, double *dcdm,

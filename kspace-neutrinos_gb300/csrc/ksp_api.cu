@@ -15,77 +15,13 @@
 #include <map>
 #include <string>
 #include <vector>
-#include "ksp_internal.h"
-#include "../../include/kspace_gpu.h"
+#include "ksp_ctx.h"
 
 using namespace ksp;
 
 namespace ksp {
 std::atomic<long long> g_launches{0};
 }
-
-struct Geo {
-    GridGeom g;                      // device tables + slab parameters (slab fields set per call)
-    std::vector<long long> count;    // full-grid mode count per bin
-    std::vector<double> ksum;        // full-grid sum |k| per bin (grid units)
-    std::vector<int> compact;        // non-empty bins in order
-    long long* count_d = nullptr;
-    double* ksum_d = nullptr;
-    int* compact_d = nullptr;
-    int nk = 0;
-};
-
-struct kspace_ctx {
-    int device = 0;
-    cudaStream_t stream = nullptr, own_stream = nullptr;
-    kspace_allreduce_fn ar_fn = nullptr;
-    void* ar_user = nullptr;
-    int tma = 1, rows = 128, stages = 4, qag_warps = 4;
-    // background
-    bool bg_ready = false, hubble_ready = false;
-    Background hB;
-    Background* dB = nullptr;
-    double MNu[3] = {0, 0, 0};
-    double bg_a0 = 0.01;
-    int nspec = 0, spec_ids[3] = {0, 0, 0};
-    // integrator table
-    bool table_ready = false;
-    IntegratorDev I{};
-    double TimeTransfer = 0, loga0 = 0;
-    int nk = 0, ia = 0, init_done = 0, fact_valid = 0;
-    std::vector<double> h_scalefact;
-    std::vector<double> t_logk, t_T;
-    bool transfer_ready = false;
-    // step buffers
-    double *bin_sum_d = nullptr, *F0sq_d = nullptr, *power_d = nullptr, *keffg_d = nullptr, *keff_d = nullptr;
-    double *logk_d = nullptr, *ratio_d = nullptr, *norm_d = nullptr, *dnu_out_d = nullptr, *io_d = nullptr;
-    int buf_nb = 0;
-    CorrTable corr{};
-    unsigned* status_d = nullptr;
-    unsigned* status_h = nullptr;
-    double* ar_h = nullptr;
-    int last_nk = 0;
-    double last_BoxSize = 0;
-    // geometry cache keyed by (N, nrbins)
-    std::map<std::pair<int, int>, Geo> geos;
-    // staging for host grids
-    void* stage_d = nullptr;
-    size_t stage_bytes = 0;
-    // differentiable step
-    double Omeganonu = 0;
-    double *ivals_d = nullptr, *adj_node_d = nullptr, *adj_Dbar_d = nullptr, *adj_mbar_d = nullptr;
-    double *adj_Q_d = nullptr, *adj_dcsum_d = nullptr, *adj_dnubar_d = nullptr, *adj_rbar_d = nullptr;
-    int* nivals_d = nullptr;
-    int adj_cap_nb = 0;
-    bool diff_ready = false;
-    int diff_ia = 0, diff_Na = 0, diff_nk = 0, diff_store = 0;
-    double diff_time = 0, diff_box = 0;
-    int diff_pmgrid = 0;
-    // profiling
-    bool prof = false;
-    cudaEvent_t ev[5] = {nullptr, nullptr, nullptr, nullptr, nullptr};
-    float stage_ms[4] = {0, 0, 0, 0};
-};
 
 // ------------------------------------------------------------------ helpers
 #define CK(x)                                                                                         \
@@ -107,7 +43,7 @@ static cudaError_t dalloc(T** p, size_t n) {
     return cudaMalloc(reinterpret_cast<void**>(p), sizeof(T) * (n ? n : 1));
 }
 
-static int map_status(unsigned s) {
+int ksp::map_status(unsigned s) {
     if (s & kStTimeout) return KSPACE_ERR_TIMEOUT;
     if (s & kStKmax) return KSPACE_ERR_KMAX;
     if (s & kStDnuNaN) return KSPACE_ERR_DNU_NAN;
@@ -127,7 +63,7 @@ static int sync_status(kspace_ctx* c) {
     return map_status(s);
 }
 
-static bool is_device_ptr(const void* p) {
+bool ksp::is_device_ptr(const void* p) {
     cudaPointerAttributes at;
     if (cudaPointerGetAttributes(&at, p) != cudaSuccess) {
         cudaGetLastError();
@@ -1316,3 +1252,13 @@ extern "C" int kspace_gpu_diff_backward(kspace_ctx* c, const void* gbar_out, con
     if (mbar) CK(cudaMemcpyAsync(mbar, c->adj_mbar_d, sizeof(double) * kNuSpecies, cudaMemcpyDeviceToHost, c->stream));
     return sync_status(c);
 }
+
+// ------------------------------------------------------------------ shared with the batch ABI
+int ksp::ctx_delta_tot_init(kspace_ctx* c, int nk_in, const double* keff_d, const double* dcdm_d, double Time) {
+    return delta_tot_init(c, nk_in, keff_d, dcdm_d, Time);
+}
+int ksp::ctx_get_geo(kspace_ctx* c, int N, int nrbins, Geo** out) { return get_geo(c, N, nrbins, out); }
+int ksp::ctx_bin_grid(kspace_ctx* c, Geo* G, const float* gd, int pmgrid, int slab0, int nslab, double BoxSize) {
+    return bin_grid(c, G, gd, pmgrid, slab0, nslab, BoxSize);
+}
+int ksp::ctx_sync_status(kspace_ctx* c) { return sync_status(c); }

@@ -1,0 +1,487 @@
+// ksp_batch.cu -- many independent integrator instances advanced by one launch sequence.
+//
+// Every instance is a complete integrator (its own cosmology and masses, transfer table,
+// history of its own length, its own k bins).  One batched call performs, for every
+// instance, the same arithmetic as the single-instance kernels of ksp_integrator.cu --
+// which follow get_delta_nu_update, delta_tot_table.c:193-250 -- so each instance's
+// delta_nu is the one a single-instance call returns:
+//   kb_prologue     block per instance: provisional history row (:222), call scalars,
+//                   knot factorisation of the history spline
+//   kb_fs_segments  every instance's fslength segments (4-point Gauss-Legendre)
+//   kb_fs_finish    block per instance: suffix sums of the segments -> fslength table
+//   kb_fs_coeffs    thread per (instance, unknown): natural spline of the table
+//   kb_dtot_coeffs  thread per (instance, bin): history-row spline coefficients
+//   kb_dnu_qag      persistent warps that pull (instance, species, bin) tasks from an
+//                   atomic queue; knots, row and coefficients staged into shared memory
+//                   by TMA bulk copies; QAG with the 61-point Gauss-Kronrod rule
+//   kb_finish       thread per (instance, bin): species sum, commit, NaN check, clamp
+//   kb_corr         block per bound grid: correction table (interface_common.c:134-146)
+// All kernels run on fixed launch shapes and read the call's totals from device memory,
+// so one captured CUDA graph serves every call.
+#include <cuda_runtime.h>
+#include <float.h>
+#include <stdint.h>
+#include "ksp_batch.h"
+#include "ksp_ptx.cuh"
+
+namespace ksp {
+
+// largest i in [0, n) with off[i] <= v (off ascending, off[0] = 0)
+__device__ __forceinline__ int owner_of(const int* off, int n, int v) {
+    int lo = 0, hi = n;
+    while (hi > lo + 1) {
+        const int mid = (lo + hi) >> 1;
+        if (__ldg(off + mid) <= v) lo = mid; else hi = mid;
+    }
+    return lo;
+}
+
+constexpr int kBatchSmallBlocks = 4 * 152;
+
+// ------------------------------------------------------------------ prologue
+// update_delta_tot's provisional row (as k_update_row), then the call scalars and the
+// knot factorisation (as k_scalars).
+__global__ void kb_prologue(BatchDev b) {
+    if (blockIdx.x == 0 && threadIdx.x == 0) b.hdr->counter = 0;
+    __shared__ double s3[3];
+    for (int i = blockIdx.x; i < b.M; i += gridDim.x) {
+        const BatchCall& P = b.calls[i];
+        __syncthreads();  // s3 reuse across instances
+        if (!P.active) continue;
+        const IntegratorDev& I = b.insts[i];
+        const Background& B = *I.B;
+        StepScalars& S = *I.sc;
+        const double a = P.a;
+        const int Na = P.Na;
+        const bool integrate = P.commit_row != -2;
+        if (threadIdx.x == 0) {
+            s3[0] = omega_nu_nopart(B, a) * (a * a * a);
+            s3[1] = omega_nu(B, 1);
+            s3[2] = particle_nu_fraction(B, a, 0);
+            if (integrate) I.scalefact[Na - 1] = P.loga;
+        }
+        __syncthreads();
+        if (integrate) {
+            const double Omeganonu = S.Omeganonu;
+            for (int ik = threadIdx.x; ik < P.nk; ik += blockDim.x)
+                I.dtot[(size_t)ik * I.ld + Na - 1] =
+                    get_delta_tot(I.nu_last[ik], I.dcdm[ik], s3[0], Omeganonu, s3[1], s3[2]);
+            const double* xk = I.scalefact;
+            for (int j = threadIdx.x; j + 1 < Na; j += blockDim.x) I.knot_invh[j] = 1.0 / (xk[j + 1] - xk[j]);
+        }
+        if (threadIdx.x != 0) continue;
+        S.a = a;
+        S.loga = P.loga;
+        S.loga0 = P.loga0;
+        S.Na = integrate ? Na : 1;
+        S.OmegaNua3 = omega_nu_nopart(B, a) * (a * a * a);
+        S.OmegaNu1 = omega_nu(B, 1);
+        S.partnu = particle_nu_fraction(B, a, 0);
+        S.Omega_nu_tot = omega_nu_nopart(B, a);
+        for (int mi = 0; mi < kNuSpecies; mi++)
+            S.omeganu[mi] = B.deg[mi] > 0 ? B.deg[mi] * omega_nu_single(B, a, mi) : 0.0;
+        const double TT = P.TimeTransfer;
+        S.deriv_prefac = TT * (hubble(B, TT) / S.light) * TT;
+        S.relerr = 1e-6;
+        S.partnu_now = particle_nu_fraction(B, a, 0);
+        S.skip_integral = 0;
+        if (S.partnu_now > 0) {
+            if (1 - S.partnu_now < 1e-3) S.skip_integral = 1;
+            S.relerr /= (1. + 1e-5 - S.partnu_now);
+        }
+        const double OmegaNu_nop = omega_nu_nopart(B, a);
+        const double omega_hybrid = omega_nu(B, a) - OmegaNu_nop;
+        S.kspace_prefac = OmegaNu_nop / (S.Omeganonu / (a * a * a) + omega_hybrid);
+        if (!integrate) continue;
+        if (P.nfs == 0) {
+            S.fsl_A0a = 0.0;
+            S.Nfs = 0;
+        }
+        const double* x = I.scalefact;
+        if (Na > 2) {
+            const int m = Na - 2;
+            for (int r = P.start_row < 0 ? 0 : P.start_row; r < m; r++) {
+                const double h0 = x[r + 1] - x[r], h1 = x[r + 2] - x[r + 1];
+                double d = 2.0 * (h0 + h1);
+                if (r > 0) {
+                    const double f = h0 * I.knot_invdiag[r - 1];
+                    d -= f * h0;
+                    I.knot_fac[r] = f;
+                }
+                I.knot_invdiag[r] = 1.0 / d;
+            }
+        }
+    }
+}
+
+// ------------------------------------------------------------------ fslength table
+struct GL4b { double x[2], w[2]; };
+
+// 4 lanes per segment, as k_fs_segments
+__global__ void kb_fs_segments(BatchDev b, GL4b gl) {
+    const int total = b.hdr->total_segs;
+    const long long stride = (long long)gridDim.x * blockDim.x;  // a multiple of 4
+    const long long end = 4LL * total;
+    for (long long base = (long long)blockIdx.x * blockDim.x; base < end; base += stride) {
+        const long long gt = base + threadIdx.x;
+        const int gseg = (int)(gt >> 2), q = (int)(gt & 3);
+        double v = 0.0;
+        const bool live = gt < end;
+        int i = 0, seg = 0;
+        if (live) {
+            i = owner_of(b.fs_off, b.M, gseg);
+            seg = gseg - __ldg(b.fs_off + i);
+            const BatchCall& P = b.calls[i];
+            const int Nfs = P.nfs;
+            const double loga0 = P.loga0, loga = P.loga;
+            const double xa = loga0 + seg * (loga - loga0) / (Nfs - 1.);
+            double xb = loga0 + (seg + 1) * (loga - loga0) / (Nfs - 1.);
+            if (seg == Nfs - 1) xb = loga;
+            if (xb > xa) {
+                const double c = 0.5 * (xa + xb), h = 0.5 * (xb - xa);
+                const int j = q & 1;
+                const double x = (q < 2) ? c - h * gl.x[j] : c + h * gl.x[j];
+                const double ax = exp(x);
+                v = gl.w[j] * h * (1. / ax / (ax * hubble(*b.insts[i].B, ax)));
+            }
+            if (q == 0) b.insts[i].fs_x[seg] = xa;
+        }
+        v += __shfl_down_sync(0xffffffffu, v, 2, 4);
+        v += __shfl_down_sync(0xffffffffu, v, 1, 4);
+        if (live && q == 0) b.insts[i].fs_seg[seg] = v;
+    }
+}
+
+// block of 1024 threads per instance: the partition and summation order of k_fs_finish
+// (which also runs with 1024 threads)
+__global__ void __launch_bounds__(1024) kb_fs_finish(BatchDev b) {
+    __shared__ double warp_tot[32];
+    const int t = threadIdx.x, nt = blockDim.x, lane = t & 31, w = t >> 5;
+    for (int i = blockIdx.x; i < b.M; i += gridDim.x) {
+        const BatchCall& P = b.calls[i];
+        const int Nfs = P.nfs;
+        if (!P.active || P.commit_row == -2 || Nfs <= 0) continue;  // uniform over the block
+        const IntegratorDev& I = b.insts[i];
+        const int per = (Nfs + nt - 1) / nt;
+        const int i0 = t * per, i1 = min(Nfs, i0 + per);
+        double loc = 0;
+        for (int k = i1 - 1; k >= i0; k--) loc += I.fs_seg[k];
+        double v = loc;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const double n = __shfl_down_sync(0xffffffffu, v, o);
+            if (lane + o < 32) v += n;
+        }
+        __syncthreads();  // warp_tot reuse across instances
+        if (lane == 0) warp_tot[w] = v;
+        __syncthreads();
+        if (w == 0) {
+            const int nw = nt >> 5;
+            double u = lane < nw ? warp_tot[lane] : 0.0;
+#pragma unroll
+            for (int o = 1; o < 32; o <<= 1) {
+                const double n = __shfl_down_sync(0xffffffffu, u, o);
+                if (lane + o < 32) u += n;
+            }
+            if (lane < nw) warp_tot[lane] = u;
+        }
+        __syncthreads();
+        const double later = (w + 1 < (nt >> 5)) ? warp_tot[w + 1] : 0.0;
+        double run = v - loc + later;
+        const double light = I.sc->light;
+        for (int k = i1 - 1; k >= i0; k--) {
+            run += I.fs_seg[k];
+            I.fs_y[k] = light * run;
+        }
+        __syncthreads();
+        if (t == 0) {
+            I.sc->fsl_A0a = I.fs_y[0];
+            I.sc->Nfs = Nfs;
+            I.fs_c[0] = 0.0;
+            I.fs_c[Nfs - 1] = 0.0;
+        }
+    }
+}
+
+// thread per (instance, unknown): closed-form inverse of tridiag(1,4,1), as k_fs_coeffs
+__global__ void kb_fs_coeffs(BatchDev b) {
+    __shared__ double mupow[82];
+    if (threadIdx.x < 82) {
+        const double mu = 2.0 - sqrt(3.0);
+        double p = 1.0;
+        for (int k = 0; k < (int)threadIdx.x; k++) p *= mu;
+        mupow[threadIdx.x] = p;
+    }
+    __syncthreads();
+    const int total = b.hdr->total_fsc;
+    for (int g = blockIdx.x * blockDim.x + threadIdx.x; g < total; g += gridDim.x * blockDim.x) {
+        const int i = owner_of(b.fsc_off, b.M, g);
+        const int u = g - __ldg(b.fsc_off + i);
+        const BatchCall& P = b.calls[i];
+        const IntegratorDev& I = b.insts[i];
+        const int Nfs = P.nfs, m = Nfs - 2;
+        const double h = (P.loga - P.loga0) / (Nfs - 1.);
+        const double scale = 3.0 / (h * h) / (2.0 * sqrt(3.0));
+        const double D = (2 * (m + 1) < 82) ? 1.0 - mupow[2 * (m + 1)] : 1.0;
+        const double* y = I.fs_y;
+        double acc = 0;
+        const int vlo = max(0, u - 40), vhi = min(m - 1, u + 40);
+        for (int v = vlo; v <= vhi; v++) {
+            const int d = v > u ? v - u : u - v;
+            const int lo1 = min(u, v) + 1, hi1 = max(u, v) + 1;
+            const double A = (2 * lo1 < 82) ? 1.0 - mupow[2 * lo1] : 1.0;
+            const int e2 = 2 * (m + 1 - hi1);
+            const double Bf = (e2 < 82) ? 1.0 - mupow[e2] : 1.0;
+            const double r = y[v + 2] - 2.0 * y[v + 1] + y[v];
+            acc += ((d & 1) ? -mupow[d] : mupow[d]) * A * Bf * r;
+        }
+        I.fs_c[u + 1] = acc * scale / D;
+    }
+}
+
+// ------------------------------------------------------------------ history splines
+__global__ void kb_dtot_coeffs(BatchDev b) {
+    const int total = b.hdr->total_bins;
+    for (int g = blockIdx.x * blockDim.x + threadIdx.x; g < total; g += gridDim.x * blockDim.x) {
+        const int i = owner_of(b.bin_off, b.M, g);
+        const int ik = g - __ldg(b.bin_off + i);
+        const BatchCall& P = b.calls[i];
+        const int Na = P.Na;
+        if (!P.active || P.commit_row == -2 || Na <= 2) continue;
+        const IntegratorDev& I = b.insts[i];
+        const double* y = I.dtot + (size_t)ik * I.ld;
+        double* c = I.coef + (size_t)ik * I.ld;
+        const double* ih = I.knot_invh;
+        const int m = Na - 2;
+        double prev = 0;
+        for (int k = 0; k < m; k++) {
+            double r = 3.0 * ((y[k + 2] - y[k + 1]) * ih[k + 1] - (y[k + 1] - y[k]) * ih[k]);
+            if (k > 0) r -= I.knot_fac[k] * prev;
+            prev = r;
+            c[k + 1] = r;
+        }
+        c[0] = 0.0;
+        c[Na - 1] = 0.0;
+        double next = c[m] * I.knot_invdiag[m - 1];
+        c[m] = next;
+        const double* x = I.scalefact;
+        for (int k = m - 1; k-- > 0;) {
+            const double off = x[k + 2] - x[k + 1];
+            next = (c[k + 1] - off * next) * I.knot_invdiag[k];
+            c[k + 1] = next;
+        }
+    }
+}
+
+// ------------------------------------------------------------------ delta_nu integrals
+struct DnuIntegrandB {  // delta_tot_table.c:492-500 (as DnuIntegrand)
+    const Background* B;
+    double k, mnubykT, qc, nufrac_low;
+    const double* fs_x; const double* fs_y; const double* fs_c; int nfs; double fs_x0, fs_inv;
+    const double* kx; const double* ky; const double* kc; int na;
+    __device__ double operator()(double logai) const {
+        int i = (int)((logai - fs_x0) * fs_inv);
+        i = i < 0 ? 0 : (i > nfs - 2 ? nfs - 2 : i);
+        while (i > 0 && logai < __ldg(fs_x + i)) i--;
+        while (i < nfs - 2 && logai >= __ldg(fs_x + i + 1)) i++;
+        double fsl;
+        {
+            const double x0 = __ldg(fs_x + i), x1 = __ldg(fs_x + i + 1);
+            const double y0 = __ldg(fs_y + i), y1 = __ldg(fs_y + i + 1);
+            const double c0 = __ldg(fs_c + i), c1 = __ldg(fs_c + i + 1);
+            const double h = x1 - x0, dx = logai - x0;
+            const double bq = (y1 - y0) / h - h * (c1 + 2.0 * c0) / 3.0;
+            const double d = (c1 - c0) / (3.0 * h);
+            fsl = y0 + dx * (bq + dx * (c0 + dx * d));
+        }
+        const int j = seg_bsearch(kx, na, logai);
+        const double dt = na > 2 ? cspline_seg(kx, ky, kc, j, logai) : linear_seg(kx, ky, j, logai);
+        const double specJ = specialJ(k * fsl / mnubykT, qc, nufrac_low);
+        const double ai = exp(logai);
+        return fsl / (ai * hubble(*B, ai)) * specJ * dt;
+    }
+};
+
+size_t batch_qag_smem(int ldmax, int wpb) {
+    return ((sizeof(Gk61Nodes) + 15) & ~size_t(15)) + wpb * (sizeof(QagList) + 3 * sizeof(double) * ldmax) +
+           wpb * sizeof(uint64_t);
+}
+
+// Shared memory: Gk61Nodes | per warp: QagList, knots[ldmax], row[ldmax], coef[ldmax] | mbarriers
+__global__ void __launch_bounds__(128) kb_dnu_qag(BatchDev b) {
+    extern __shared__ __align__(16) unsigned char sm[];
+    Gk61Nodes& N = *reinterpret_cast<Gk61Nodes*>(sm);
+    const size_t off = (sizeof(Gk61Nodes) + 15) & ~size_t(15);
+    const int nw = blockDim.x >> 5, warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const size_t per_warp = sizeof(QagList) + 3 * sizeof(double) * b.ldmax;
+    unsigned char* wbase = sm + off + warp * per_warp;
+    QagList& L = *reinterpret_cast<QagList*>(wbase);
+    double* knots = reinterpret_cast<double*>(wbase + sizeof(QagList));
+    double* row = knots + b.ldmax;
+    double* rc = row + b.ldmax;
+    uint64_t* mybar = reinterpret_cast<uint64_t*>(sm + off + nw * per_warp) + warp;
+    gk61_fill(N, threadIdx.x, blockDim.x);
+    if (lane == 0) ptx::mbar_init(mybar, 1);
+    ptx::mbar_init_fence();
+    __syncthreads();
+    const int total = b.hdr->total_tasks;
+    unsigned phase = 0;
+    for (;;) {
+        int task = 0;
+        if (lane == 0) task = atomicAdd(&b.hdr->counter, 1);
+        task = __shfl_sync(0xffffffffu, task, 0);
+        if (task >= total) break;
+        const int i = owner_of(b.task_off, b.M, task);
+        const int loc = task - __ldg(b.task_off + i);
+        const BatchCall& P = b.calls[i];
+        const IntegratorDev& I = b.insts[i];
+        const int nk = P.nk;
+        const int si = loc / nk, ik = loc - si * nk;
+        const int mi = P.spec[si];
+        const Background* B = I.B;
+        const StepScalars& S = *I.sc;
+        const int Na = P.Na;
+        const double mnubykT = B->mnu_J[mi] / B->kBtnu;
+        const double k = I.wavenum[ik];
+        // initial-condition piece (delta_tot_table.c:525-535); qc = 0 here
+        const double specJ0 = specialJ(k * S.fsl_A0a / (mnubykT > 0 ? mnubykT : 1), 0.0, B->nufrac_low[0]);
+        double val = specJ0 * I.nu_init[ik] * (1. + S.deriv_prefac * S.fsl_A0a);
+        if (!S.skip_integral && Na > 1 && mnubykT > 0) {
+            const unsigned bytes = (unsigned)(((Na + 1) & ~1) * sizeof(double));
+            __syncwarp();
+            if (lane == 0) {
+                ptx::fence_async_smem();
+                ptx::mbar_expect_tx(mybar, Na > 2 ? 3 * bytes : 2 * bytes);
+                ptx::bulk_g2s(knots, I.scalefact, bytes, mybar);
+                ptx::bulk_g2s(row, I.dtot + (size_t)ik * I.ld, bytes, mybar);
+                if (Na > 2) ptx::bulk_g2s(rc, I.coef + (size_t)ik * I.ld, bytes, mybar);
+            }
+            const bool got = ptx::mbar_wait_bounded(mybar, phase);
+            phase ^= 1;
+            if (!got) {
+                if (lane == 0) atomicOr(I.status, kStTimeout);
+                ptx::mbar_wait_bounded(mybar, phase ^ 1);  // the copies still in flight
+                return;
+            }
+            DnuIntegrandB f;
+            f.B = B; f.k = k; f.mnubykT = mnubykT; f.qc = S.partnu_now > 0 ? B->vcrit * mnubykT : 0.0;
+            f.nufrac_low = B->nufrac_low[0];
+            f.fs_x = I.fs_x; f.fs_y = I.fs_y; f.fs_c = I.fs_c; f.nfs = S.Nfs; f.fs_x0 = S.loga0;
+            f.fs_inv = (S.Nfs - 1.) / (S.loga - S.loga0);
+            f.kx = knots; f.ky = row; f.kc = rc; f.na = Na;
+            const QagResult r = qag_warp(f, N, L, S.loga0, S.loga, 0.0, S.relerr, kQagLimit);
+            val += S.prefac * r.result;
+            if (!r.ok && lane == 0) atomicOr(I.status, kStGsl);
+        }
+        if (lane == 0) I.dnu_s[(size_t)mi * I.nk_alloc + ik] = val;
+    }
+}
+
+// ------------------------------------------------------------------ finish
+// k_combine + k_finish for every bin of every instance
+__global__ void kb_finish(BatchDev b) {
+    const int total = b.hdr->total_bins;
+    for (int g = blockIdx.x * blockDim.x + threadIdx.x; g < total; g += gridDim.x * blockDim.x) {
+        const int i = owner_of(b.bin_off, b.M, g);
+        const int ik = g - __ldg(b.bin_off + i);
+        const BatchCall& P = b.calls[i];
+        if (!P.active) continue;
+        const IntegratorDev& I = b.insts[i];
+        const StepScalars& S = *I.sc;
+        double out;
+        if (P.commit_row == -2) {
+            out = I.nu_last[ik];  // same scale factor: delta_nu_last as it is
+            I.dnu[ik] = out;
+        } else {
+            double v = 0;
+            for (int mi = 0; mi < kNuSpecies; mi++)
+                if (I.B->deg[mi] > 0) v += I.dnu_s[(size_t)mi * I.nk_alloc + ik] * S.omeganu[mi] / S.Omega_nu_tot;
+            I.dnu[ik] = v;
+            if (!P.dry) I.nu_last[ik] = v;
+            if (P.commit_row >= 0 && !P.dry) {
+                if (ik == 0) I.scalefact[P.commit_row] = P.loga;
+                I.dtot[(size_t)ik * I.ld + P.commit_row] =
+                    get_delta_tot(v, I.dcdm[ik], S.OmegaNua3, S.Omeganonu, S.OmegaNu1, S.partnu);
+            }
+            if (isnan(v)) atomicOr(I.status, kStDnuNaN);
+            out = v < 0 ? 0.0 : v;
+        }
+        b.dnu_pool[__ldg(b.bin_off + i) + ik] = out;
+    }
+}
+
+// correction tables of the bound grids (the table part of k_finish)
+__global__ void kb_corr(BatchDev b, const BatchGridCorr* grids, int ngrid) {
+    for (int gi = blockIdx.x; gi < ngrid; gi += gridDim.x) {
+        const BatchGridCorr G = grids[gi];
+        const BatchCall& P = b.calls[G.inst];
+        if (!P.active) continue;
+        const IntegratorDev& I = b.insts[G.inst];
+        const double norm = I.sc->kspace_prefac;
+        const double* dnu_out = b.dnu_pool + b.bin_off[G.inst];
+        const int nk = P.nk;
+        if (threadIdx.x == 0 && G.norm_out) *G.norm_out = norm;
+        for (int j = threadIdx.x; j < nk; j += blockDim.x) {
+            const double lk = log(G.keff[j]);
+            const double r = dnu_out[j] / I.dcdm[j];
+            G.corr.xf[j] = (float)lk;
+            G.corr.rn[j] = (float)(norm * r);
+            double s = 0;
+            if (j + 1 < nk) {
+                const double lk1 = log(G.keff[j + 1]);
+                const double r1 = dnu_out[j + 1] / I.dcdm[j + 1];
+                s = norm * (r1 - r) / (lk1 - lk);
+            }
+            G.corr.sn[j] = (float)s;
+            if (!isfinite(norm * r) || !isfinite(s)) atomicOr(I.status, kStGridNaN);
+        }
+    }
+}
+
+// ------------------------------------------------------------------ launchers
+static void gl_nodes_b(int n, double* X, double* Wt) {  // Newton on P_n, positive half
+    for (int i = 0; i < n / 2; i++) {
+        double x = cos(3.14159265358979323846 * (i + 0.75) / (n + 0.5)), dp = 0;
+        for (int it = 0; it < 100; it++) {
+            double p0 = 1, p1 = x;
+            for (int k = 2; k <= n; k++) {
+                const double p2 = ((2 * k - 1) * x * p1 - (k - 1) * p0) / k;
+                p0 = p1;
+                p1 = p2;
+            }
+            dp = n * (x * p1 - p0) / (x * x - 1);
+            const double dx = p1 / dp;
+            x -= dx;
+            if (fabs(dx) < 1e-16) break;
+        }
+        X[i] = x;
+        Wt[i] = 2 / ((1 - x * x) * dp * dp);
+    }
+}
+
+void batch_set_attributes() {
+    cudaFuncSetAttribute(kb_dnu_qag, cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024);
+}
+
+void launch_batch_update(const BatchDev& b, cudaStream_t st) {
+    static GL4b gl;
+    static bool init = false;
+    if (!init) {
+        gl_nodes_b(4, gl.x, gl.w);
+        init = true;
+    }
+    const int nb = kBatchSmallBlocks;
+    kb_prologue<<<b.M < nb ? b.M : nb, 128, 0, st>>>(b);
+    kb_fs_segments<<<nb, 256, 0, st>>>(b, gl);
+    kb_fs_finish<<<b.M < 2 * 152 ? b.M : 2 * 152, 1024, 0, st>>>(b);
+    kb_fs_coeffs<<<nb, 128, 0, st>>>(b);
+    kb_dtot_coeffs<<<nb, 128, 0, st>>>(b);
+    kb_dnu_qag<<<b.qag_blocks, 32 * b.wpb, batch_qag_smem(b.ldmax, b.wpb), st>>>(b);
+    kb_finish<<<nb, 256, 0, st>>>(b);
+}
+
+void launch_batch_corr(const BatchDev& b, const BatchGridCorr* g, int ngrid, cudaStream_t st) {
+    if (ngrid > 0) kb_corr<<<ngrid, 256, 0, st>>>(b, g, ngrid);
+}
+
+}  // namespace ksp

@@ -68,6 +68,16 @@ _SIGS = {
     "kspace_gpu_set_jmass": (_i, [_vp, _PD]),
     "kspace_gpu_diff_forward": (_i, [_vp, _d, _d, _vp, _vp, _i, _vp, _i]),
     "kspace_gpu_diff_backward": (_i, [_vp, _vp, _vp, _vp, _vp, _vp, _PD, _i]),
+    "kspace_gpu_batch_create": (_i, [C.POINTER(_vp), C.POINTER(_vp), _i]),
+    "kspace_gpu_batch_destroy": (_i, [_vp]),
+    "kspace_gpu_batch_bind_grid": (_i, [_vp, _i, _vp, _i, _d]),
+    "kspace_gpu_batch_init": (_i, [_vp, _PD, _PI, _PD, _PD]),
+    "kspace_gpu_batch_layout": (_i, [_vp, _PI, _PI]),
+    "kspace_gpu_batch_step": (_i, [_vp, _PD, _vp, _vp]),
+    "kspace_gpu_batch_status": (_i, [_vp, _PI]),
+    "kspace_gpu_batch_set_tuning": (_i, [_vp, _i, _i, _i]),
+    "kspace_gpu_batch_autotune": (_i, [_vp, _PD, _vp, _i, _PI, C.POINTER(C.c_float)]),
+    "kspace_gpu_batch_last_ms": (_i, [_vp, C.POINTER(C.c_float)]),
 }
 
 _lib = None
@@ -243,7 +253,19 @@ class KspaceNeutrinos:
         return n.value
 
     def set_nu_state(self, scalefact, delta_tot):
+        """scalefact: host array [ia]; delta_tot: [nk][ia] float64, numpy or a torch tensor
+        (host or CUDA)."""
         sf = _f64(scalefact)
+        try:
+            import torch
+            if isinstance(delta_tot, torch.Tensor):
+                t = delta_tot.detach().to(torch.float64).contiguous()
+                nk, ia = t.shape
+                _check(self.L.kspace_gpu_set_nu_state(self.h, _pd(sf), C.cast(t.data_ptr(), _PD), nk, ia),
+                       "set_nu_state")
+                return
+        except ImportError:
+            pass
         dt = _f64(delta_tot)
         nk, ia = dt.shape
         _check(self.L.kspace_gpu_set_nu_state(self.h, _pd(sf), _pd(dt), nk, ia), "set_nu_state")
@@ -390,6 +412,105 @@ class KspaceNeutrinos:
 
     def launch_count(self):
         return int(self.L.kspace_gpu_launch_count(self.h))
+
+
+def _buf_ptr(x):
+    """(pointer, keepalive) of a float64 array: numpy (host) or torch tensor (host or CUDA)."""
+    if x is None:
+        return None, None
+    try:
+        import torch
+        if isinstance(x, torch.Tensor):
+            if x.dtype != torch.float64 or not x.is_contiguous():
+                raise TypeError("expected a contiguous float64 tensor")
+            return x.data_ptr(), x
+    except ImportError:
+        pass
+    if not isinstance(x, np.ndarray) or x.dtype != np.float64 or not x.flags.c_contiguous:
+        raise TypeError("expected a contiguous float64 array")
+    return x.ctypes.data, x
+
+
+class KspaceBatch:
+    """Many independent instances advanced by one captured CUDA graph (no counterpart
+    in the reference, which holds one integrator per process).  Instance i's bins are
+    entries offsets[i]:offsets[i+1] of the concatenated ("pool") arrays."""
+
+    def __init__(self, instances):
+        self.L = load_library()
+        self.instances = list(instances)
+        arr = (_vp * len(self.instances))(*[k.h for k in self.instances])
+        h = _vp()
+        _check(self.L.kspace_gpu_batch_create(C.byref(h), arr, len(self.instances)), "batch_create")
+        self.h = h
+        self.M = len(self.instances)
+        self._grids = []
+        self.nk = None
+        self.offsets = None
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.L.kspace_gpu_batch_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def bind_grid(self, inst, grid, pmgrid, BoxSize):
+        """Bin this CUDA complex64 grid into instance inst's delta_cdm every step and
+        correct it in place afterwards."""
+        ptr, keep = _grid_ptr(grid)
+        self._grids.append(keep)
+        _check(self.L.kspace_gpu_batch_bind_grid(self.h, inst, ptr, pmgrid, BoxSize), "batch_bind_grid")
+
+    def init(self, a, nk, keff, dcdm):
+        a = _f64(a)
+        nk = np.ascontiguousarray(nk, dtype=np.int32)
+        keff = _f64(keff)
+        dcdm = _f64(dcdm)
+        _check(self.L.kspace_gpu_batch_init(self.h, _pd(a), nk.ctypes.data_as(_PI), _pd(keff), _pd(dcdm)),
+               "batch_init")
+        self.nk = np.zeros(self.M, dtype=np.int32)
+        self.offsets = np.zeros(self.M + 1, dtype=np.int32)
+        _check(self.L.kspace_gpu_batch_layout(self.h, self.nk.ctypes.data_as(_PI), self.offsets.ctypes.data_as(_PI)),
+               "batch_layout")
+
+    def step(self, a, dcdm=None, dnu=None):
+        """One step of every instance at a[i].  dcdm / dnu: pools (numpy or torch,
+        host or CUDA); dnu=None returns a new numpy pool."""
+        a = _f64(a)
+        out = dnu
+        if out is None:
+            out = np.zeros(int(self.offsets[-1]), dtype=np.float64)
+        dp, keep1 = _buf_ptr(dcdm if dcdm is None or not isinstance(dcdm, np.ndarray) else _f64(dcdm))
+        op, keep2 = _buf_ptr(out)
+        _check(self.L.kspace_gpu_batch_step(self.h, _pd(a), dp, op), "batch_step")
+        return out
+
+    def status(self):
+        st = np.zeros(self.M, dtype=np.int32)
+        _check(self.L.kspace_gpu_batch_status(self.h, st.ctypes.data_as(_PI)), "batch_status")
+        return st
+
+    def set_tuning(self, warps_per_block=4, blocks_per_sm=2, use_graph=True):
+        _check(self.L.kspace_gpu_batch_set_tuning(self.h, warps_per_block, blocks_per_sm, int(use_graph)),
+               "batch_set_tuning")
+
+    def autotune(self, a, dcdm=None, reps=3):
+        a = _f64(a)
+        dp, keep = _buf_ptr(dcdm if dcdm is None or not isinstance(dcdm, np.ndarray) else _f64(dcdm))
+        best = (C.c_int * 2)()
+        ms = C.c_float()
+        _check(self.L.kspace_gpu_batch_autotune(self.h, _pd(a), dp, reps, best, C.byref(ms)), "batch_autotune")
+        return (best[0], best[1]), ms.value
+
+    def last_ms(self):
+        ms = C.c_float()
+        _check(self.L.kspace_gpu_batch_last_ms(self.h, C.byref(ms)), "batch_last_ms")
+        return ms.value
 
 
 def make_instance(MNu, TimeTransfer, HubbleParam, Omega0, nk_alloc, TimeMax, logk, T_nu, UnitLength_in_cm=3.085678e24,

@@ -154,3 +154,28 @@ CONFIGS = {
     # profiling case: grid larger than L2 (227 MB) but small enough for multi-pass captures
     "prof_n384": dict(N=384, nbins=192, Na=64, a_end=1.0, MNu=(0.1, 0.1, 0.1), L=512.0),
 }
+
+# Batched integration: independent instances with their own cosmology, masses, history
+# length and k bins, plus grids bound to some of them.
+BATCH = dict(M=4096, grids=16, grid_N=(64, 96, 128, 192, 256), nbins_grid=128, a_end=1.0, L=512.0)
+
+
+def batch_instances(M, seed=0, a_end=1.0, Na_range=(16, 512), nk_range=(64, 512)):
+    """Per-instance parameters: sum M_nu ~ U(0.03, 0.6) eV as 3 degenerate states,
+    Omega0 ~ U(0.25, 0.35), h ~ U(0.6, 0.75), history length Na ~ U{16..512} log-spaced
+    rows from a = 0.01 to a_end, nk ~ U{64..512} bins log-spaced over 0.005-5 h/Mpc."""
+    rng = np.random.default_rng(seed)
+    out = []
+    for _ in range(M):
+        s = float(rng.uniform(0.03, 0.6))
+        Na = int(rng.integers(Na_range[0], Na_range[1] + 1))
+        nk = int(rng.integers(nk_range[0], nk_range[1] + 1))
+        out.append(dict(MNu=(s / 3, s / 3, s / 3), Omega0=float(rng.uniform(0.25, 0.35)),
+                        h=float(rng.uniform(0.6, 0.75)), Na=Na, nk=nk, a_end=a_end,
+                        k=np.exp(np.linspace(math.log(0.005), math.log(5.0), nk))))
+    return out
+
+
+def batch_grid_sizes(G, seed=0, choices=(64, 96, 128, 192, 256)):
+    rng = np.random.default_rng(seed + 7)
+    return [int(x) for x in rng.choice(choices, size=G)]

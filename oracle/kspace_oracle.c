@@ -553,15 +553,10 @@ static double get_delta_nu_int(double logai, void *params)
     return fsl_aia / (ai * ko_hubble(p->bg, ai)) * specJ * delta_tot_at_a;
 }
 
-/* Gauss-Legendre 8-point nodes/weights on [-1,1] (positive half), computed once by
- * Newton iteration on P_8 so no table is transcribed. */
-static double GL8_X[4], GL8_W[4];
-static int gl8_ready = 0;
-static void gl8_init(void)
+/* Gauss-Legendre n-point nodes/weights on [-1,1] (positive half), computed by Newton
+ * iteration on P_n so no table is transcribed. */
+static void gl_nodes(int n, double *X, double *Wt)
 {
-    if (gl8_ready)
-        return;
-    const int n = 8;
     for (int i = 0; i < n / 2; i++) {
         double x = cos(M_PI * (i + 0.75) / (n + 0.5)), dp = 0;
         for (int it = 0; it < 100; it++) {
@@ -577,10 +572,19 @@ static void gl8_init(void)
             if (fabs(dx) < 1e-16)
                 break;
         }
-        GL8_X[i] = x;
-        GL8_W[i] = 2 / ((1 - x * x) * dp * dp);
+        X[i] = x;
+        Wt[i] = 2 / ((1 - x * x) * dp * dp);
     }
-    gl8_ready = 1;
+}
+static double GL8_X[4], GL8_W[4], GL4_X[2], GL4_W[2];
+static int gl_ready = 0;
+static void gl8_init(void)
+{
+    if (gl_ready)
+        return;
+    gl_nodes(8, GL8_X, GL8_W);
+    gl_nodes(4, GL4_X, GL4_W);
+    gl_ready = 1;
 }
 
 /* fslength table: mode 0 = one QAG per node (delta_tot_table.c:574-584);
@@ -609,19 +613,22 @@ static void fs_table(ko_state *s, double a, int Nfs, double *fsscales, double *f
         return;
     }
     gl8_init();
+    /* fs_mode 1: 8-point rule per segment; fs_mode 2: 4-point rule */
+    const int np = s->fs_mode == 2 ? 2 : 4;
+    const double *GX = s->fs_mode == 2 ? GL4_X : GL8_X, *GW = s->fs_mode == 2 ? GL4_W : GL8_W;
     double acc = 0;
     /* tail beyond the last node (non-zero only through rounding of the node formula) */
     if (fsscales[Nfs - 1] < la) {
         const double c = 0.5 * (fsscales[Nfs - 1] + la), h = 0.5 * (la - fsscales[Nfs - 1]);
-        for (int j = 0; j < 4; j++)
-            acc += GL8_W[j] * h * (fslength_int(c - h * GL8_X[j], s->bg) + fslength_int(c + h * GL8_X[j], s->bg));
+        for (int j = 0; j < np; j++)
+            acc += GW[j] * h * (fslength_int(c - h * GX[j], s->bg) + fslength_int(c + h * GX[j], s->bg));
     }
     fslengths[Nfs - 1] = fsscales[Nfs - 1] >= la ? 0 : s->light * acc;
     for (int ik = Nfs - 2; ik >= 0; ik--) {
         const double c = 0.5 * (fsscales[ik] + fsscales[ik + 1]), h = 0.5 * (fsscales[ik + 1] - fsscales[ik]);
         double seg = 0;
-        for (int j = 0; j < 4; j++)
-            seg += GL8_W[j] * (fslength_int(c - h * GL8_X[j], s->bg) + fslength_int(c + h * GL8_X[j], s->bg));
+        for (int j = 0; j < np; j++)
+            seg += GW[j] * (fslength_int(c - h * GX[j], s->bg) + fslength_int(c + h * GX[j], s->bg));
         acc += h * seg;
         fslengths[ik] = s->light * acc;
     }

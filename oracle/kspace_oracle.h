@@ -53,8 +53,8 @@ void ko_state_set_ia(ko_state *s, int ia);
 
 /* Integration options (not reference behaviour; used to measure the discretisation):
  *  fs_mode 0: fslength table by one QAG per node (the reference, delta_tot_table.c:574-584)
- *  fs_mode 1: fslength table by a cumulative composite Gauss-Legendre sum over the
- *             uniform nodes (what the GPU does)
+ *  fs_mode 1: fslength table by a cumulative 8-point Gauss-Legendre sum over the
+ *             uniform nodes; fs_mode 2: the same with a 4-point rule (what the GPU does)
  *  exact    : if nonzero, the delta_nu time integral and fslength are integrated to
  *             ~1e-13 relative (QAG at epsrel 1e-13 on each knot segment): the all-FP64
  *             reference of the same splines.                                          */

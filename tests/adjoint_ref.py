@@ -83,8 +83,13 @@ class StepRef:
         self.norm = bg_om / (O.scalars(s)["Omeganonu"] / a ** 3 + (om - bg_om))
 
     # ---- pieces
-    def power(self, x):
-        a2 = (x.real ** 2 + x.imag ** 2).ravel()
+    def power(self, x, f32=False):
+        if f32:  # |F|^2 formed in float, as the reference does (powerspectrum.c:66,74,82)
+            xr = x.real.astype(np.float32)
+            xi = x.imag.astype(np.float32)
+            a2 = (xr * xr + xi * xi).astype(np.float64).ravel()
+        else:
+            a2 = (x.real ** 2 + x.imag ** 2).ravel()
         m = self.cb >= 0
         S = np.bincount(self.cb[m], weights=(self.wt * a2 * self.W4)[m], minlength=self.nk)
         F0 = float(a2[0])
@@ -114,8 +119,8 @@ class StepRef:
         return s
 
     # ---- forward
-    def forward(self, x, D, mJ, wb):
-        P, F0 = self.power(x)
+    def forward(self, x, D, mJ, wb, f32=False):
+        P, F0 = self.power(x, f32)
         dc = np.sqrt(P * self.L ** 3)
         dnu = self.dnu(dc, D, mJ)
         out = np.maximum(dnu, 0)

@@ -241,11 +241,11 @@ def test_e2e_golden_oracle(oracle):
 
 
 def test_fs_table_fixed_order_vs_qag(oracle):
-    """The cumulative fixed-order fslength table (what the GPU computes) changes
-    delta_nu by far less than the 1e-10 bar, on the benchmark-like history."""
+    """The cumulative fixed-order (4-point Gauss-Legendre per segment) fslength table, as the
+    GPU computes it, changes delta_nu by far less than the 1e-10 bar."""
     c = cases.make_case(64, 48, 40, 1.0, (0.02, 0.03, 0.06), grid=False)
     res = []
-    for mode in (0, 1):
+    for mode in (0, 2):
         bg, s = cases.oracle_state(oracle, c, fs_mode=mode)
         st, d = oracle.get_delta_nu_update(s, 1.01, c["kphys"], np.sqrt(W.spectrum(c["kphys"])))
         assert st == 0
