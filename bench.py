@@ -312,18 +312,167 @@ def run_reference(args, cfg):
             "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
 
 
+def make_batch_sets(kg, M, G, seed, nsets, nbins_grid, L, extra_rows):
+    """nsets identical sets of M free instances + G grid-bound instances."""
+    import torch
+    ps = W.batch_instances(M, seed=seed)
+    Ns = W.batch_grid_sizes(G, seed=seed)
+    gps = W.batch_instances(G, seed=seed + 1)
+    sets = []
+    for _ in range(nsets):
+        insts, kph = [], []
+        for p in ps:
+            logk, T = W.transfer_table(float(sum(p["MNu"])))
+            k = kg.make_instance(p["MNu"], 0.01, p["h"], p["Omega0"], p["nk"], 0.01 + (p["Na"] + extra_rows) / 100.0,
+                                 logk, T, UnitLength_in_cm=W.UNIT_LENGTH_MPC)
+            sf, dt = W.history(p["k"], p["Na"], p["a_end"])
+            k.set_nu_state(sf, dt)
+            insts.append(k)
+            kph.append(p["k"])
+        grids = []
+        for j, (p, N) in enumerate(zip(gps, Ns)):
+            count, keff = W.geometry(N, nbins_grid)
+            kp = keff[count > 0] * 2 * math.pi / L
+            logk, T = W.transfer_table(float(sum(p["MNu"])))
+            k = kg.make_instance(p["MNu"], 0.01, p["h"], p["Omega0"], nbins_grid,
+                                 0.01 + (p["Na"] + extra_rows) / 100.0, logk, T, UnitLength_in_cm=W.UNIT_LENGTH_MPC)
+            sf, dt = W.history(kp, p["Na"], p["a_end"])
+            k.set_nu_state(sf, dt)
+            insts.append(k)
+            kph.append(kp)
+            grids.append(W.make_grid_torch(N, L, seed=100 + j))
+        torch.cuda.synchronize()
+        sets.append(dict(insts=insts, kph=kph, grids=grids, Ns=Ns))
+    return sets, ps
+
+
+def run_batch(args, cfg):
+    """Batched integration: M independent instances + G grids advanced per call by one
+    CUDA graph, against the same instances driven one call per instance."""
+    import torch
+    import kspace_gpu as kg
+    torch.cuda.set_device(0)
+    M, G, L, nbg = args.batch_m, cfg["grids"], cfg["L"], cfg["nbins_grid"]
+    nsteps = args.warmup + args.steps
+    t_setup = time.perf_counter()
+    sets, ps = make_batch_sets(kg, M, G, 0, 2, nbg, L, nsteps + 8)
+    t_setup = time.perf_counter() - t_setup
+    A, T = sets
+    MT = M + G
+    B = kg.KspaceBatch(A["insts"])
+    for j in range(G):
+        B.bind_grid(M + j, A["grids"][j], A["Ns"][j], L)
+    nk = np.array([len(A["kph"][i]) for i in range(M)] + [0] * G, dtype=np.int32)
+    keff = np.concatenate(A["kph"][:M])
+    dc0 = np.sqrt(W.spectrum(keff))
+    a_end = cfg["a_end"]
+    a_list = [a_end + 0.01 + 0.001 * i for i in range(nsteps)]
+    # first call at the first step's a (delta_tot_init keeps the rows before it), as the
+    # single-instance path does on its first get_delta_nu_update
+    B.init(np.full(MT, a_list[0]), nk, keff, dc0)
+    off = B.offsets
+    nbins_total = int(off[-1])
+    # per-step inputs: the generator's delta_cdm grown linearly with a
+    dcdm_h = torch.empty(nbins_total, dtype=torch.float64, pin_memory=True)
+    dnu_h = torch.empty(nbins_total, dtype=torch.float64, pin_memory=True)
+    base = np.zeros(nbins_total)
+    for i in range(M):
+        base[off[i]:off[i + 1]] = np.sqrt(W.spectrum(A["kph"][i]))
+    tune = None
+    if args.autotune:
+        dcdm_h.copy_(torch.from_numpy(base * a_list[0] / a_end))
+        tune = B.autotune(np.full(MT, a_list[0]), dcdm_h, reps=2)
+    dev_ms, host_s, outs = [], [], []
+    with ClockSampler(0) as clk:
+        for i in range(nsteps):
+            dcdm_h.copy_(torch.from_numpy(base * a_list[i] / a_end))
+            t0 = time.perf_counter()
+            B.step(np.full(MT, a_list[i]), dcdm_h, dnu_h)
+            t1 = time.perf_counter()
+            if i >= args.warmup:
+                dev_ms.append(B.last_ms())
+                host_s.append(t1 - t0)
+            outs.append(dnu_h.numpy().copy())
+    t_dev = sum(dev_ms) / 1e3
+    t_host = sum(host_s)
+    # the same instances, one call per instance (the same scale factors and inputs)
+    per_s = []
+    worst = 0.0
+    n_cmp = min(nsteps, args.warmup + 1)
+    for i in range(n_cmp):
+        d = base * a_list[i] / a_end
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        res = []
+        for j in range(MT):
+            k = T["insts"][j]
+            if j < M:
+                res.append(k.get_delta_nu_update(a_list[i], T["kph"][j], d[off[j]:off[j + 1]]))
+            else:
+                k.add_nu_power_to_rhogrid(a_list[i], L, T["grids"][j - M], T["Ns"][j - M])
+                res.append(None)
+        torch.cuda.synchronize()
+        t1 = time.perf_counter()
+        if i >= args.warmup:
+            per_s.append(t1 - t0)
+        for j in range(M):
+            r = res[j]
+            g = outs[i][off[j]:off[j + 1]]
+            nz = np.abs(r) > 0
+            if nz.any():
+                worst = max(worst, float(np.max(np.abs(g[nz] - r[nz]) / np.abs(r[nz]))))
+    per_solves = MT / (sum(per_s) / len(per_s)) if per_s else None
+    value = MT * args.steps / t_dev
+    e2e = MT * args.steps / t_host
+    Na = np.array([p["Na"] for p in ps])
+    nks = np.array([p["nk"] for p in ps])
+    res = {
+        "metric": METRIC, "value": value, "unit": "solves/s", "n_gpus": 1, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": 1e3 * t_dev / args.steps, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f64 integrator / c64 grids",
+        "data": "synthetic (seeded per-instance cosmologies, histories and grids; no dataset)",
+        "config": {"workload": "batch_m%d_g%d" % (M, G), "instances": M, "grids": G, "grid_N": A["Ns"],
+                   "nbins_grid": nbg, "history_rows": [int(Na.min()), int(Na.max()), float(Na.mean())],
+                   "bins": [int(nks.min()), int(nks.max()), float(nks.mean())],
+                   "l2": "history tables %.1f GB (larger than L2): no flush" % (
+                       sum(8.0 * 2 * p["nk"] * (p["Na"] + 2) for p in ps) / 1e9)},
+        "per_instance_calls": {"solves_per_s": per_solves, "steps_timed": len(per_s),
+                               "speedup_batched_device": (value / per_solves) if per_solves else None,
+                               "speedup_batched_e2e": (e2e / per_solves) if per_solves else None},
+        "agreement_vs_per_instance": {"max_rel": worst, "steps_compared": n_cmp, "bar": 1e-10},
+        "autotune": {"warps_per_block_blocks_per_sm": tune[0], "ms": tune[1]} if tune else None,
+        "e2e": {"value": e2e, "unit": "solves/s", "h2d_bytes_per_step": 8 * nbins_total,
+                "d2h_bytes_per_step": 8 * nbins_total},
+        "gpu_launches": args.steps * (8 + 3 * G),
+        "setup_s": t_setup,
+        "clocks": clk.summary(),
+    }
+    B.close()
+    for s_ in sets:
+        for k in s_["insts"]:
+            k.close()
+    return res
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=20)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
-    ap.add_argument("--config", default="cfg1_n512", choices=sorted(W.CONFIGS))
+    ap.add_argument("--config", default="cfg1_n512", choices=sorted(W.CONFIGS) + ["batch"])
+    ap.add_argument("--batch-m", type=int, default=W.BATCH["M"])
+    ap.add_argument("--autotune", type=int, default=1)
     ap.add_argument("--cpu-threads", type=int, default=0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
+    if args.config == "batch":
+        res = run_batch(args, dict(W.BATCH)) if args.impl == "gb300" else None
+        if res is not None:
+            print(json.dumps(res))
+        return
     cfg = dict(W.CONFIGS[args.config])
     cfg["name"] = args.config
     if args.impl == "reference":

@@ -299,7 +299,7 @@ __global__ void __launch_bounds__(128) k_dnu_adj(IntegratorDev I, DnuAdjArgs A, 
                         : "memory");
             }
             for (int i = lane; i < Na; i += 32) { ybar[i] = 0.0; cbar[i] = 0.0; }
-            const bool got = mbar_wait_bounded_a(mybar, phase);
+            const bool got = __all_sync(0xffffffffu, mbar_wait_bounded_a(mybar, phase));  // warp-uniform
             phase ^= 1;
             if (!got) {
                 if (lane == 0) atomicOr(I.status, kStTimeout);

@@ -356,7 +356,7 @@ __global__ void __launch_bounds__(128) kb_dnu_qag(BatchDev b) {
                 ptx::bulk_g2s(row, I.dtot + (size_t)ik * I.ld, bytes, mybar);
                 if (Na > 2) ptx::bulk_g2s(rc, I.coef + (size_t)ik * I.ld, bytes, mybar);
             }
-            const bool got = ptx::mbar_wait_bounded(mybar, phase);
+            const bool got = __all_sync(0xffffffffu, ptx::mbar_wait_bounded(mybar, phase));  // warp-uniform
             phase ^= 1;
             if (!got) {
                 if (lane == 0) atomicOr(I.status, kStTimeout);

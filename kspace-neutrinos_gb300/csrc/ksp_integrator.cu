@@ -468,7 +468,7 @@ __global__ void __launch_bounds__(128) k_dnu_qag(IntegratorDev I, int nk, int Na
                 bulk_g2s(row, I.dtot + (size_t)ik * I.ld, row_bytes, mybar);
                 if (Na > 2) bulk_g2s(rc, I.coef + (size_t)ik * I.ld, row_bytes, mybar);
             }
-            const bool got = mbar_wait_bounded(mybar, phase);
+            const bool got = __all_sync(0xffffffffu, mbar_wait_bounded(mybar, phase));  // warp-uniform
             phase ^= 1;
             if (!got) {
                 if (lane == 0) atomicOr(I.status, kStTimeout);
