@@ -61,9 +61,10 @@ const char *kspace_gpu_error_string(int status);
 int kspace_gpu_set_stream(kspace_ctx *ctx, void *cuda_stream);
 /* Multi-rank slab decomposition: reduction of the per-bin sums (NULL = one rank). */
 int kspace_gpu_set_allreduce(kspace_ctx *ctx, kspace_allreduce_fn fn, void *user);
-/* Kernel variant selection: tma (1 = TMA tile engine, 0 = plain loads), rows per CTA
- * (128/256), pipeline stages (3/4/6), warps per block of the integrator (1..4).
- * Values <= 0 keep the current setting. */
+/* Kernel variant selection: tma (1 = TMA tile engine with a thread per 16-mode row,
+ * 2 = two threads per row, 0 = plain loads), rows per CTA (128/256), pipeline stages
+ * (2/3/4), warps per block of the integrator (1..4).  Values < 0 (rows, stages,
+ * qag_warps: <= 0) keep the current setting. */
 int kspace_gpu_set_tuning(kspace_ctx *ctx, int tma, int rows_per_cta, int stages, int qag_warps);
 
 /* ---- background: Omega_nu(a), H(a) ----
@@ -178,9 +179,11 @@ int kspace_gpu_batch_destroy(kspace_batch *batch);
  * Must precede kspace_gpu_batch_init. */
 int kspace_gpu_batch_bind_grid(kspace_batch *batch, int inst, void *grid, int pmgrid, double BoxSize);
 /* First call of every instance (delta_tot_init, delta_tot_table.c:79-149) at a[i]:
- * nk[i] bins with keff (physical k) and sqrt(P_cdm) in host pools laid out by nk.
- * Bound instances take nk, keff and delta_cdm from their grid (their entries are
- * ignored; pass nk[i] = 0).  Fixes the layout (kspace_gpu_batch_layout). */
+ * nk[i] bins with keff (physical k) and sqrt(P_cdm) in host arrays holding the
+ * unbound instances one after another.  Bound instances take nk, keff and delta_cdm
+ * from their grid and have no entries there (their nk[i] is ignored).  Fixes the
+ * layout of the step pools (kspace_gpu_batch_layout), where bound instances do own
+ * entries (their delta_nu). */
 int kspace_gpu_batch_init(kspace_batch *batch, const double *a, const int *nk, const double *keff,
                           const double *dcdm);
 /* nk[M] and offset[M+1] of the pools */

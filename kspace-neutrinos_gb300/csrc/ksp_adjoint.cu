@@ -315,16 +315,8 @@ __global__ void __launch_bounds__(128) k_dnu_adj(IntegratorDev I, DnuAdjArgs A, 
                 nint = A.nivals[(size_t)mi * I.nk_alloc + ik];
                 iv = A.ivals + ((size_t)mi * I.nk_alloc + ik) * kQagLimit * 2;
             } else {
-                struct F {
-                    const Background* B; double k, m, qc, nfl; const double *fx, *fy, *fc; int nfs; double x0, inv;
-                    const double *kx, *ky, *kc; int na;
-                    __device__ double operator()(double x) const {
-                        DnuNode o = dnu_node(B, k, m, qc, nfl, fx, fy, fc, nfs, x0, inv, kx, ky, kc, na, x);
-                        return o.g * o.J * o.S;
-                    }
-                } f{B, k, mnubykT, qc, B->nufrac_low[0], I.fs_x, I.fs_y, I.fs_c, S.Nfs, S.loga0, fs_inv, knots, row, rc,
-                    Na};
-                QagResult r = qag_warp(f, N, L, S.loga0, S.loga, 0.0, S.relerr, kQagLimit);
+                const DnuIntegrandC f = dnu_integrand(I, S, k, mnubykT, qc, knots, row, rc, Na);
+                QagResult r = qag_warp_c(f, N, L, S.loga0, S.loga, 0.0, S.relerr, kQagLimit);
                 nint = r.nint;
             }
             for (int q = 0; q < nint; q++) {

@@ -96,8 +96,9 @@ extern "C" int kspace_gpu_create(kspace_ctx** out, int device) {
 static void free_table(kspace_ctx* c) {
     IntegratorDev& I = c->I;
     void* ptrs[] = {I.scalefact, I.dtot, I.coef, I.nu_init, I.nu_last, I.wavenum, I.dcdm, I.dnu_s, I.dnu,
-                    I.knot_invdiag, I.knot_fac, I.knot_invh, I.fs_x, I.fs_y, I.fs_c, I.fs_seg, I.t_logk,
-                    I.t_T, I.t_c, I.sc, I.qag_max, I.qag_total};
+                    I.knot_invdiag, I.knot_fac, I.knot_invh, I.knot_h3, I.knot_ih3, I.nc_g, I.nc_fsl,
+                    I.nc_dx, I.nc_j, I.fs_x, I.fs_y, I.fs_c, I.fs_seg, I.t_logk, I.t_T, I.t_c, I.sc,
+                    I.qag_max, I.qag_total};
     for (void* p : ptrs)
         if (p) cudaFree(p);
     memset(&I, 0, sizeof(I));
@@ -356,6 +357,12 @@ extern "C" int kspace_gpu_alloc_table(kspace_ctx* c, int nk_alloc, double TimeTr
     CK(dalloc(&I.knot_invdiag, ld));
     CK(dalloc(&I.knot_fac, ld));
     CK(dalloc(&I.knot_invh, ld));
+    CK(dalloc(&I.knot_h3, ld));
+    CK(dalloc(&I.knot_ih3, ld));
+    CK(dalloc(&I.nc_g, kNcNodes));
+    CK(dalloc(&I.nc_fsl, kNcNodes));
+    CK(dalloc(&I.nc_dx, kNcNodes));
+    CK(dalloc(&I.nc_j, kNcNodes));
     I.fs_cap = 16 * (int)ld + 16;
     CK(dalloc(&I.fs_x, I.fs_cap));
     CK(dalloc(&I.fs_y, I.fs_cap));
@@ -620,7 +627,7 @@ static int delta_tot_init(kspace_ctx* c, int nk_in, const double* keff_d, const 
     const double a_last = exp(c->h_scalefact[c->ia - 1]);
     launch_delta_nu_combined(c->I, c->nk, c->ia, a_last, c->h_scalefact[c->ia - 1], c->loga0, c->TimeTransfer,
                              0, c->nspec, c->spec_ids, c->qag_warps, c->stream);
-    g_launches += 7;
+    g_launches += 8;
     CK(cudaMemcpyAsync(c->I.nu_last, c->I.dnu, sizeof(double) * c->nk, cudaMemcpyDeviceToDevice, c->stream));
     c->fact_valid = 0;
     c->init_done = 1;
@@ -673,7 +680,7 @@ static int update_device(kspace_ctx* c, double a, int nk_in, const double* keff_
     launch_finish_update(I, c->nk, commit ? Na - 1 : -1, a, loga, want_corr ? keff_d : nullptr, dnu_out_d,
                          want_corr ? c->logk_d : nullptr, want_corr ? c->ratio_d : nullptr,
                          want_corr ? c->corr : CorrTable{}, c->norm_d, c->stream);
-    g_launches += 9;
+    g_launches += 10;
     if (commit) {
         c->fact_valid = Na - 2 > 0 ? Na - 2 : 0;
     } else {
@@ -1164,7 +1171,7 @@ extern "C" int kspace_gpu_diff_forward(kspace_ctx* c, double Time, double BoxSiz
     launch_finish_update(I, c->nk, -3, Time, loga, c->keff_d, c->dnu_out_d, c->logk_d, c->ratio_d, c->corr,
                          c->norm_d, c->stream);
     k_square<<<(c->nk + 127) / 128, 128, 0, c->stream>>>(c->dnu_out_d, pnu_out, c->nk);
-    g_launches += 10;
+    g_launches += 11;
     const size_t bytes = sizeof(float) * 2 * (size_t)pmgrid * pmgrid * (pmgrid / 2 + 1);
     if (grid_out != grid_in) CK(cudaMemcpyAsync(grid_out, grid_in, bytes, cudaMemcpyDeviceToDevice, c->stream));
     st = correct_grid(c, G, reinterpret_cast<float*>(grid_out), BoxSize, c->nk);

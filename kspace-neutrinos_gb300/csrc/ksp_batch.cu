@@ -11,6 +11,7 @@
 //   kb_fs_finish    block per instance: suffix sums of the segments -> fslength table
 //   kb_fs_coeffs    thread per (instance, unknown): natural spline of the table
 //   kb_dtot_coeffs  thread per (instance, bin): history-row spline coefficients
+//   kb_nc_build     thread per (instance, node): node tables of the integrand
 //   kb_dnu_qag      persistent warps that pull (instance, species, bin) tasks from an
 //                   atomic queue; knots, row and coefficients staged into shared memory
 //                   by TMA bulk copies; QAG with the 61-point Gauss-Kronrod rule
@@ -67,7 +68,12 @@ __global__ void kb_prologue(BatchDev b) {
                 I.dtot[(size_t)ik * I.ld + Na - 1] =
                     get_delta_tot(I.nu_last[ik], I.dcdm[ik], s3[0], Omeganonu, s3[1], s3[2]);
             const double* xk = I.scalefact;
-            for (int j = threadIdx.x; j + 1 < Na; j += blockDim.x) I.knot_invh[j] = 1.0 / (xk[j + 1] - xk[j]);
+            for (int j = threadIdx.x; j + 1 < Na; j += blockDim.x) {
+                const double h = xk[j + 1] - xk[j];
+                I.knot_invh[j] = 1.0 / h;
+                I.knot_h3[j] = h / 3.0;
+                I.knot_ih3[j] = 1.0 / (3.0 * h);
+            }
         }
         if (threadIdx.x != 0) continue;
         S.a = a;
@@ -274,33 +280,34 @@ __global__ void kb_dtot_coeffs(BatchDev b) {
 }
 
 // ------------------------------------------------------------------ delta_nu integrals
-struct DnuIntegrandB {  // delta_tot_table.c:492-500 (as DnuIntegrand)
-    const Background* B;
-    double k, mnubykT, qc, nufrac_low;
-    const double* fs_x; const double* fs_y; const double* fs_c; int nfs; double fs_x0, fs_inv;
-    const double* kx; const double* ky; const double* kc; int na;
-    __device__ double operator()(double logai) const {
-        int i = (int)((logai - fs_x0) * fs_inv);
-        i = i < 0 ? 0 : (i > nfs - 2 ? nfs - 2 : i);
-        while (i > 0 && logai < __ldg(fs_x + i)) i--;
-        while (i < nfs - 2 && logai >= __ldg(fs_x + i + 1)) i++;
-        double fsl;
-        {
-            const double x0 = __ldg(fs_x + i), x1 = __ldg(fs_x + i + 1);
-            const double y0 = __ldg(fs_y + i), y1 = __ldg(fs_y + i + 1);
-            const double c0 = __ldg(fs_c + i), c1 = __ldg(fs_c + i + 1);
-            const double h = x1 - x0, dx = logai - x0;
-            const double bq = (y1 - y0) / h - h * (c1 + 2.0 * c0) / 3.0;
-            const double d = (c1 - c0) / (3.0 * h);
-            fsl = y0 + dx * (bq + dx * (c0 + dx * d));
-        }
-        const int j = seg_bsearch(kx, na, logai);
-        const double dt = na > 2 ? cspline_seg(kx, ky, kc, j, logai) : linear_seg(kx, ky, j, logai);
-        const double specJ = specialJ(k * fsl / mnubykT, qc, nufrac_low);
-        const double ai = exp(logai);
-        return fsl / (ai * hubble(*B, ai)) * specJ * dt;
+// thread per (instance, slot, node): the node tables (as k_nc_build)
+__global__ void kb_nc_build(BatchDev b) {
+    const double XK[31] = KSP_GK61_XK_INIT;  // the abscissae of gk61_fill
+    const long long total = (long long)b.M * kNcNodes;
+    for (long long g = blockIdx.x * (long long)blockDim.x + threadIdx.x; g < total;
+         g += (long long)gridDim.x * blockDim.x) {
+        const int i = (int)(g / kNcNodes);
+        const int q = (int)(g - (long long)i * kNcNodes);
+        const BatchCall& P = b.calls[i];
+        if (!P.active || P.commit_row == -2 || P.nfs <= 0 || P.Na <= 1) continue;
+        const IntegratorDev& I = b.insts[i];
+        const StepScalars& S = *I.sc;
+        const int slot = q / 61, jn = q - 61 * slot;
+        double lo, hi;
+        nc_interval(slot, S.loga0, S.loga, &lo, &hi);
+        const double c = __dmul_rn(0.5, __dadd_rn(lo, hi));
+        const double h = __dmul_rn(0.5, __dsub_rn(hi, lo));
+        const double xk = jn < 30 ? -XK[jn] : (jn < 60 ? XK[jn - 30] : 0.0);
+        const double x = __dadd_rn(c, __dmul_rn(h, xk));
+        const double fs_inv = (S.Nfs - 1.) / (S.loga - S.loga0);
+        const NodeTerms t =
+            dnu_node_terms(I.B, I.fs_x, I.fs_y, I.fs_c, S.Nfs, S.loga0, fs_inv, I.scalefact, P.Na, x);
+        I.nc_g[q] = t.g;
+        I.nc_fsl[q] = t.fsl;
+        I.nc_dx[q] = t.dx;
+        I.nc_j[q] = t.j;
     }
-};
+}
 
 size_t batch_qag_smem(int ldmax, int wpb) {
     return ((sizeof(Gk61Nodes) + 15) & ~size_t(15)) + wpb * (sizeof(QagList) + 3 * sizeof(double) * ldmax) +
@@ -363,13 +370,9 @@ __global__ void __launch_bounds__(128) kb_dnu_qag(BatchDev b) {
                 ptx::mbar_wait_bounded(mybar, phase ^ 1);  // the copies still in flight
                 return;
             }
-            DnuIntegrandB f;
-            f.B = B; f.k = k; f.mnubykT = mnubykT; f.qc = S.partnu_now > 0 ? B->vcrit * mnubykT : 0.0;
-            f.nufrac_low = B->nufrac_low[0];
-            f.fs_x = I.fs_x; f.fs_y = I.fs_y; f.fs_c = I.fs_c; f.nfs = S.Nfs; f.fs_x0 = S.loga0;
-            f.fs_inv = (S.Nfs - 1.) / (S.loga - S.loga0);
-            f.kx = knots; f.ky = row; f.kc = rc; f.na = Na;
-            const QagResult r = qag_warp(f, N, L, S.loga0, S.loga, 0.0, S.relerr, kQagLimit);
+            const double qc = S.partnu_now > 0 ? B->vcrit * mnubykT : 0.0;
+            const DnuIntegrandC f = dnu_integrand(I, S, k, mnubykT, qc, knots, row, rc, Na);
+            const QagResult r = qag_warp_c(f, N, L, S.loga0, S.loga, 0.0, S.relerr, kQagLimit);
             val += S.prefac * r.result;
             if (!r.ok && lane == 0) atomicOr(I.status, kStGsl);
         }
@@ -476,6 +479,7 @@ void launch_batch_update(const BatchDev& b, cudaStream_t st) {
     kb_fs_finish<<<b.M < 2 * 152 ? b.M : 2 * 152, 1024, 0, st>>>(b);
     kb_fs_coeffs<<<nb, 128, 0, st>>>(b);
     kb_dtot_coeffs<<<nb, 128, 0, st>>>(b);
+    kb_nc_build<<<nb, 128, 0, st>>>(b);
     kb_dnu_qag<<<b.qag_blocks, 32 * b.wpb, batch_qag_smem(b.ldmax, b.wpb), st>>>(b);
     kb_finish<<<nb, 256, 0, st>>>(b);
 }

@@ -305,7 +305,9 @@ extern "C" int kspace_gpu_batch_init(kspace_batch* b, const double* a, const int
     if (st) return st;
     std::vector<char> bound(b->M, 0);
     for (const BoundGrid& g : b->grids) bound[g.inst] = 1;
-    // per instance, as the first call of the single-context path (update_device)
+    // per instance, as the first call of the single-context path (update_device); the
+    // input pools hold the unbound instances only, laid out by nk (bound ones count 0)
+    size_t in_off = 0;
     for (int i = 0; i < b->M; i++) {
         kspace_ctx* c = b->ctx[i];
         if (bound[i]) continue;
@@ -314,9 +316,10 @@ extern "C" int kspace_gpu_batch_init(kspace_batch* b, const double* a, const int
         double* kd = c->io_d;
         double* dd = c->io_d + c->I.nk_alloc;
         if (n > 0) {
-            CKB(cudaMemcpyAsync(kd, keff + b->off[i], sizeof(double) * n, cudaMemcpyHostToDevice, c->stream));
-            CKB(cudaMemcpyAsync(dd, dcdm + b->off[i], sizeof(double) * n, cudaMemcpyHostToDevice, c->stream));
+            CKB(cudaMemcpyAsync(kd, keff + in_off, sizeof(double) * n, cudaMemcpyHostToDevice, c->stream));
+            CKB(cudaMemcpyAsync(dd, dcdm + in_off, sizeof(double) * n, cudaMemcpyHostToDevice, c->stream));
         }
+        in_off += n;
         st = ctx_delta_tot_init(c, n, kd, dd, a[i]);
         if (st) return st;
     }

@@ -341,6 +341,7 @@ __device__ __forceinline__ void gk61_warp(const F& f, const Gk61Nodes& N, int ni
 
 struct QagList {  // per-warp interval list in shared memory
     double a[kQagLimit], b[kQagLimit], r[kQagLimit], e[kQagLimit];
+    int slot[kQagLimit];  // node-cache slot of the interval (-1: not cached)
 };
 
 struct QagResult { double result, abserr; int ok; int nint; };
@@ -418,6 +419,255 @@ __device__ QagResult qag_warp(const F& f, const Gk61Nodes& N, QagList& L, double
     R.ok = errsum <= tol;
     __syncwarp();
     return R;
+}
+// ------------------------------------------------------------------ cached QAG
+// QAG only ever bisects, so its intervals are the dyadic subintervals of [a, b]; those
+// of the first kNcLevels levels are numbered in heap order (root 0, children of s:
+// 2s+1, 2s+2).  A functor with node(slot, j, x) may serve the 61 nodes of such an
+// interval from a table built once; x is passed for the others (slot -1).
+constexpr int kNcLevels = 4;
+constexpr int kNcSlots = (1 << kNcLevels) - 1;  // 15 intervals
+constexpr int kNcNodes = kNcSlots * 61;
+
+__device__ __forceinline__ int nc_child(int s, int right) {
+    return (s >= 0 && 2 * s + 2 < kNcSlots) ? 2 * s + 1 + right : -1;
+}
+
+// gk61_warp with interval slots (same arithmetic)
+template <class F>
+__device__ __forceinline__ void gk61_warp_c(const F& f, const Gk61Nodes& N, int nint, const double* a,
+                                            const double* b, const int* slot, GkOut* out) {
+    const int lane = threadIdx.x & 31;
+    double c[2], h[2];
+    for (int t = 0; t < 2; t++) {
+        c[t] = __dmul_rn(0.5, __dadd_rn(a[t], b[t]));
+        h[t] = __dmul_rn(0.5, __dsub_rn(b[t], a[t]));
+    }
+    double fv[4];
+    double rk[2] = {0, 0}, rg[2] = {0, 0}, ra[2] = {0, 0};
+    const int nslots = 61 * nint;
+#pragma unroll
+    for (int m = 0; m < 4; m++) {
+        const int s = lane + 32 * m;
+        fv[m] = 0.0;
+        if (s < nslots) {
+            const int t = s >= 61 ? 1 : 0;
+            const int j = s - 61 * t;
+            const double x = __dadd_rn(c[t], __dmul_rn(h[t], N.x[j]));
+            const double v = f.node(slot[t], j, x);
+            fv[m] = v;
+            if (t == 0) { rk[0] += N.wk[j] * v; rg[0] += N.wg[j] * v; ra[0] += N.wk[j] * fabs(v); }
+            else { rk[1] += N.wk[j] * v; rg[1] += N.wg[j] * v; ra[1] += N.wk[j] * fabs(v); }
+        }
+    }
+    double mean[2];
+    for (int t = 0; t < nint; t++) {
+        rk[t] = bcast0(warp_sum_to0(rk[t]));
+        rg[t] = bcast0(warp_sum_to0(rg[t]));
+        ra[t] = bcast0(warp_sum_to0(ra[t]));
+        mean[t] = 0.5 * rk[t];
+    }
+    double rs[2] = {0, 0};
+#pragma unroll
+    for (int m = 0; m < 4; m++) {
+        const int s = lane + 32 * m;
+        if (s < nslots) {
+            const int t = s >= 61 ? 1 : 0;
+            const int j = s - 61 * t;
+            const double d = N.wk[j] * fabs(fv[m] - mean[t]);
+            if (t == 0) rs[0] += d; else rs[1] += d;
+        }
+    }
+    for (int t = 0; t < nint; t++) {
+        rs[t] = bcast0(warp_sum_to0(rs[t]));
+        const double err = (rk[t] - rg[t]) * h[t];
+        out[t].result = rk[t] * h[t];
+        out[t].resabs = ra[t] * fabs(h[t]);
+        out[t].resasc = rs[t] * fabs(h[t]);
+        out[t].abserr = rescale_error(err, out[t].resabs, out[t].resasc);
+    }
+}
+
+// qag_warp with interval slots (same decisions)
+template <class F>
+__device__ QagResult qag_warp_c(const F& f, const Gk61Nodes& N, QagList& L, double a, double b, double epsabs,
+                                double epsrel, int limit) {
+    const int lane = threadIdx.x & 31;
+    QagResult R;
+    GkOut g[2];
+    double aa[2] = {a, a}, bb[2] = {b, b};
+    int ss[2] = {0, -1};
+    gk61_warp_c(f, N, 1, aa, bb, ss, g);
+    if (lane == 0) { L.a[0] = a; L.b[0] = b; L.r[0] = g[0].result; L.e[0] = g[0].abserr; L.slot[0] = 0; }
+    __syncwarp();
+    double tol = fmax(epsabs, epsrel * fabs(g[0].result));
+    const double round_off = 50 * DBL_EPSILON * g[0].resabs;
+    R.nint = 1;
+    R.result = g[0].result;
+    R.abserr = g[0].abserr;
+    if (g[0].abserr <= round_off && g[0].abserr > tol) { R.ok = 0; return R; }
+    if ((g[0].abserr <= tol && g[0].abserr != g[0].resasc) || g[0].abserr == 0.0) { R.ok = 1; return R; }
+    if (limit == 1) { R.ok = 0; return R; }
+    double area = g[0].result, errsum = g[0].abserr;
+    int n = 1, roundoff1 = 0, roundoff2 = 0, error_type = 0;
+    do {
+        double best = -1.0;
+        int bk = 0x7fffffff;
+        for (int i = lane; i < n; i += 32) {
+            const double e = L.e[i];
+            if (e > best) { best = e; bk = i; }
+        }
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) {
+            const double ob = __shfl_down_sync(0xffffffffu, best, o);
+            const int ok = __shfl_down_sync(0xffffffffu, bk, o);
+            if (ob > best || (ob == best && ok < bk)) { best = ob; bk = ok; }
+        }
+        const int k = __shfl_sync(0xffffffffu, bk, 0);
+        const double a_i = L.a[k], b_i = L.b[k], r_i = L.r[k], e_i = L.e[k];
+        const int s_i = L.slot[k];
+        const double a1 = a_i, b1 = 0.5 * (a_i + b_i), a2 = b1, b2 = b_i;
+        aa[0] = a1; bb[0] = b1; aa[1] = a2; bb[1] = b2;
+        ss[0] = nc_child(s_i, 0);
+        ss[1] = nc_child(s_i, 1);
+        gk61_warp_c(f, N, 2, aa, bb, ss, g);
+        const double area12 = g[0].result + g[1].result, error12 = g[0].abserr + g[1].abserr;
+        errsum += error12 - e_i;
+        area += area12 - r_i;
+        if (g[0].resasc != g[0].abserr && g[1].resasc != g[1].abserr) {
+            if (fabs(r_i - area12) <= 1.0e-5 * fabs(area12) && error12 >= 0.99 * e_i) roundoff1++;
+            if (n >= 10 && error12 > e_i) roundoff2++;
+        }
+        tol = fmax(epsabs, epsrel * fabs(area));
+        if (errsum > tol) {
+            if (roundoff1 >= 6 || roundoff2 >= 20) error_type = 2;
+            const double tiny = (1 + 100 * DBL_EPSILON) * (fabs(a2) + 1000 * DBL_MIN);
+            if (fabs(a1) <= tiny && fabs(b2) <= tiny) error_type = 3;
+        }
+        __syncwarp();
+        if (lane == 0) {
+            L.b[k] = b1; L.r[k] = g[0].result; L.e[k] = g[0].abserr; L.slot[k] = ss[0];
+            L.a[n] = a2; L.b[n] = b2; L.r[n] = g[1].result; L.e[n] = g[1].abserr; L.slot[n] = ss[1];
+        }
+        __syncwarp();
+        n++;
+    } while (n < limit && !error_type && errsum > tol);
+    double sum = 0;
+    if (lane == 0)
+        for (int i = 0; i < n; i++) sum += L.r[i];
+    R.result = bcast0(sum);
+    R.abserr = errsum;
+    R.nint = n;
+    R.ok = errsum <= tol;
+    __syncwarp();
+    return R;
+}
+
+// ------------------------------------------------------------------ delta_nu integrand
+// delta_tot_table.c:492-500: fslength(x, log a) / (a H(a)) J(k fslength / (m/kT))
+// delta_tot(k, x) at x = log a_i.  Split into the part that depends only on x (and the
+// instance), NodeTerms, and the per-bin rest.
+struct NodeTerms {
+    double g;    // fslength / (a H(a))
+    double fsl;  // fslength(x, log a)
+    double dx;   // x - knot[j]
+    int j;       // history segment: knot[j] <= x < knot[j+1]
+};
+
+// Not inlined: the table builder and the uncached path run the same compiled code and
+// produce the same numbers bit for bit.
+static __device__ __noinline__ NodeTerms dnu_node_terms(const Background* B, const double* fs_x, const double* fs_y,
+                                                 const double* fs_c, int nfs, double fs_x0, double fs_inv,
+                                                 const double* kx, int na, double x) {
+    NodeTerms t;
+    int i = (int)((x - fs_x0) * fs_inv);
+    i = i < 0 ? 0 : (i > nfs - 2 ? nfs - 2 : i);
+    while (i > 0 && x < fs_x[i]) i--;
+    while (i < nfs - 2 && x >= fs_x[i + 1]) i++;
+    {
+        const double x0 = fs_x[i], x1 = fs_x[i + 1];
+        const double y0 = fs_y[i], y1 = fs_y[i + 1];
+        const double c0 = fs_c[i], c1 = fs_c[i + 1];
+        const double h = x1 - x0, dx = x - x0;
+        const double bq = (y1 - y0) / h - h * (c1 + 2.0 * c0) / 3.0;
+        const double d = (c1 - c0) / (3.0 * h);
+        t.fsl = y0 + dx * (bq + dx * (c0 + dx * d));
+    }
+    t.j = seg_bsearch(kx, na, x);
+    t.dx = x - kx[t.j];
+    const double ai = exp(x);
+    t.g = t.fsl / (ai * hubble(*B, ai));
+    return t;
+}
+
+// Per-segment constants of the history knots: 1/h, h/3, 1/(3h).
+struct KnotSeg {
+    const double* ih;
+    const double* h3;
+    const double* ih3;
+};
+
+// The per-bin rest: J and the history row's natural spline (or linear for 2 knots) at
+// the node.  Same for the cached and uncached paths.
+__device__ __forceinline__ double dnu_combine(const NodeTerms& t, double k, double mnubykT, double qc, double nfl,
+                                              const double* ky, const double* kc, int na, const KnotSeg& ks) {
+    const int j = t.j;
+    const double y0 = ky[j], y1 = ky[j + 1];
+    double S;
+    if (na > 2) {
+        const double c0 = kc[j], c1 = kc[j + 1];
+        const double bq = (y1 - y0) * __ldg(ks.ih + j) - (c1 + 2.0 * c0) * __ldg(ks.h3 + j);
+        const double d = (c1 - c0) * __ldg(ks.ih3 + j);
+        S = y0 + t.dx * (bq + t.dx * (c0 + t.dx * d));
+    } else {
+        S = y0 + t.dx * ((y1 - y0) * __ldg(ks.ih + j));
+    }
+    const double J = specialJ(k * t.fsl / mnubykT, qc, nfl);
+    return t.g * J * S;
+}
+
+// Node table of one instance for one call: kNcNodes entries, slot-major.
+struct NodeCache {
+    double* g;
+    double* fsl;
+    double* dx;
+    int* j;
+};
+
+// The full integrand with the node table.
+struct DnuIntegrandC {
+    const Background* B;
+    double k, mnubykT, qc, nfl;
+    const double* fs_x; const double* fs_y; const double* fs_c; int nfs; double fs_x0, fs_inv;
+    const double* kx; const double* ky; const double* kc; int na;
+    KnotSeg ks;
+    NodeCache nc;
+    __device__ double node(int slot, int jn, double x) const {
+        NodeTerms t;
+        if (slot >= 0) {
+            const int q = slot * 61 + jn;
+            t.g = __ldg(nc.g + q);
+            t.fsl = __ldg(nc.fsl + q);
+            t.dx = __ldg(nc.dx + q);
+            t.j = __ldg(nc.j + q);
+        } else {
+            t = dnu_node_terms(B, fs_x, fs_y, fs_c, nfs, fs_x0, fs_inv, kx, na, x);
+        }
+        return dnu_combine(t, k, mnubykT, qc, nfl, ky, kc, na, ks);
+    }
+};
+
+// End points of cache slot s of [a, b], by the bisections QAG performs (b1 = (a+b)/2).
+__device__ __forceinline__ void nc_interval(int s, double a, double b, double* lo, double* hi) {
+    int lvl = 0;
+    while ((2 << lvl) - 1 <= s) lvl++;
+    const int p = s + 1 - (1 << lvl);
+    for (int i = lvl - 1; i >= 0; i--) {
+        const double m = 0.5 * (a + b);
+        if ((p >> i) & 1) a = m; else b = m;
+    }
+    *lo = a;
+    *hi = b;
 }
 #endif  // __CUDACC__
 

@@ -85,11 +85,16 @@ __host__ __device__ inline SmemPlan plan_smem(int rows, int stages, int nrbins, 
 }
 
 // ------------------------------------------------------------------ K1 (TMA)
-template <int ROWS, int STAGES>
-__global__ void __launch_bounds__(ROWS) k_bin_power_tma(const __grid_constant__ CUtensorMap tmap, GridArgs g,
-                                                        const int* __restrict__ thresh, const float* __restrict__ w1g,
-                                                        const float* __restrict__ grid, double* bin_sum, double* F0sq,
-                                                        unsigned* status, int ntiles) {
+// Persistent CTAs stream 128-byte rows (16 modes) through a STAGES-deep TMA ring;
+// 16/MPT threads per row, MPT consecutive modes each.  A thread sums its modes into two
+// adjacent bins as float pairs (BinPairAcc) and hands them to the CTA's float-pair bin
+// totals by FP32 atomics; each CTA adds its totals to the global FP64 sums once.
+template <int ROWS, int STAGES, int MPT>
+__global__ void __launch_bounds__(ROWS * (16 / MPT), 1024 / (ROWS * (16 / MPT)))
+k_bin_power_tma(const __grid_constant__ CUtensorMap tmap, GridArgs g, const int* __restrict__ thresh,
+                const float* __restrict__ w1g, const float* __restrict__ grid, double* bin_sum, double* F0sq,
+                unsigned* status, int ntiles) {
+    constexpr int TPR = 16 / MPT, NT = ROWS * TPR;
     extern __shared__ unsigned char sm_raw[];
     __shared__ int s_abort;
     __shared__ long long s_rowbase;
@@ -97,17 +102,19 @@ __global__ void __launch_bounds__(ROWS) k_bin_power_tma(const __grid_constant__ 
     const SmemPlan P = plan_smem(ROWS, STAGES, g.nrbins, g.nz);
     const uint32_t base_u = smem_addr(sm_raw);
     unsigned char* stage0 = sm_raw + ((1024 - (base_u & 1023)) & 1023);
-    double* s_hist = reinterpret_cast<double*>(sm_raw + P.hist_off);
+    float* s_H = reinterpret_cast<float*>(sm_raw + P.hist_off);  // nrbins high parts
+    float* s_L = s_H + g.nrbins;                                    // nrbins low parts
     int* s_thr = reinterpret_cast<int*>(sm_raw + P.thr_off);
     float* s_w1 = reinterpret_cast<float*>(sm_raw + P.tab_off);
     uint64_t* bars = reinterpret_cast<uint64_t*>(sm_raw + P.bar_off);
     const int tid = threadIdx.x;
-    for (int i = tid; i < g.nrbins; i += ROWS) s_hist[i] = 0.0;
-    for (int i = tid; i <= g.nrbins; i += ROWS) s_thr[i] = thresh[i];
-    for (int i = tid; i < g.nz; i += ROWS) s_w1[i] = w1g[i];
+    const int r = tid / TPR, q = tid - r * TPR;
+    for (int i = tid; i < g.nrbins; i += NT) { s_H[i] = 0.f; s_L[i] = 0.f; }
+    for (int i = tid; i <= g.nrbins; i += NT) s_thr[i] = thresh[i];
+    for (int i = tid; i < g.nz; i += NT) s_w1[i] = w1g[i];
     if (tid == 0) {
         s_abort = 0;
-        for (int s = 0; s < STAGES; s++) mbar_init_(&bars[s], 1);
+        for (int st = 0; st < STAGES; st++) mbar_init_(&bars[st], 1);
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
     }
     __syncthreads();
@@ -119,44 +126,45 @@ __global__ void __launch_bounds__(ROWS) k_bin_power_tma(const __grid_constant__ 
             tma_load_2d(stage0 + (size_t)k * ROWS * 128, &tmap, &bars[k], 0, tile * ROWS);
         }
     }
-    RunAcc run;
+    BinPairAcc acc;
     int k = 0;
     for (; k < my_n; k++) {
-        const int s = k % STAGES;
+        const int st = k % STAGES;
         const int tile = blockIdx.x + k * gridDim.x;
         if (tid == 0) {
-            if (!mbar_wait_bounded_(&bars[s], (k / STAGES) & 1)) s_abort = 1;
+            if (!mbar_wait_bounded_(&bars[st], (k / STAGES) & 1)) s_abort = 1;
             const long long m = (long long)tile * ROWS * 16;
             s_rowbase = m / g.nz;
             s_zbase = (int)(m - s_rowbase * g.nz);
         }
         __syncthreads();
         if (s_abort) break;
-        const long long row = (long long)tile * ROWS + tid;
+        const long long row = (long long)tile * ROWS + r;
         if (row < g.nrows16) {
-            const unsigned char* rp = stage0 + (size_t)s * ROWS * 128 + (size_t)tid * 128;
+            const unsigned char* rp = stage0 + (size_t)st * ROWS * 128 + (size_t)r * 128;
             ModeCursor c;
-            c.init(g, s_w1, s_rowbase, s_zbase, tid * 16);
+            c.init(g, s_w1, s_rowbase, s_zbase, r * 16 + q * MPT);
 #pragma unroll
-            for (int u = 0; u < 8; u++) {
-                const float4 v = *reinterpret_cast<const float4*>(rp + ((u ^ (tid & 7)) << 4));
+            for (int u = q * (MPT / 2); u < (q + 1) * (MPT / 2); u++) {
+                const float4 v = *reinterpret_cast<const float4*>(rp + ((u ^ (r & 7)) << 4));
                 {
                     const int k2 = c.kxy2 + c.z * c.z;
-                    if (k2 != 0) run.add(bin_of(k2, g.c1, s_thr, g.nrbins), mode_power2(v.x, v.y, c, s_w1, g.half), s_hist);
+                    if (k2 != 0) acc.add(k2, mode_power2(v.x, v.y, c, s_w1, g.half), g, s_thr, s_H, s_L);
                     c.next(g, s_w1);
                 }
                 {
                     const int k2 = c.kxy2 + c.z * c.z;
-                    if (k2 != 0) run.add(bin_of(k2, g.c1, s_thr, g.nrbins), mode_power2(v.z, v.w, c, s_w1, g.half), s_hist);
+                    if (k2 != 0) acc.add(k2, mode_power2(v.z, v.w, c, s_w1, g.half), g, s_thr, s_H, s_L);
                     c.next(g, s_w1);
                 }
             }
+            acc.flush(s_H, s_L);
         }
         __syncthreads();
         if (tid == 0 && k + STAGES < my_n) {
             const int nt = blockIdx.x + (k + STAGES) * gridDim.x;
-            mbar_expect_tx_(&bars[s], ROWS * 128);
-            tma_load_2d(stage0 + (size_t)s * ROWS * 128, &tmap, &bars[s], 0, nt * ROWS);
+            mbar_expect_tx_(&bars[st], ROWS * 128);
+            tma_load_2d(stage0 + (size_t)st * ROWS * 128, &tmap, &bars[st], 0, nt * ROWS);
         }
     }
     if (s_abort) {
@@ -168,20 +176,19 @@ __global__ void __launch_bounds__(ROWS) k_bin_power_tma(const __grid_constant__ 
         }
         return;
     }
-    run.flush(s_hist);
     // the modes after the last full 16-mode row (fewer than 16), by CTA 0
     if (blockIdx.x == 0 && tid == 0) {
         for (long long m = g.nrows16 * 16; m < g.nmodes; m++) {
-            const long long r = m / g.nz;
+            const long long rr = m / g.nz;
             ModeCursor c;
-            c.z = (int)(m - r * g.nz);
-            c.il = (int)(r / g.N);
-            c.j = (int)(r - (long long)c.il * g.N);
+            c.z = (int)(m - rr * g.nz);
+            c.il = (int)(rr / g.N);
+            c.j = (int)(rr - (long long)c.il * g.N);
             c.set_row(g, s_w1);
             const int k2 = c.kxy2 + c.z * c.z;
             if (k2 != 0) {
-                const float re = grid[2 * m], im = grid[2 * m + 1];
-                atomicAdd(&s_hist[bin_of(k2, g.c1, s_thr, g.nrbins)], mode_power_d(re, im, c, s_w1, g.half));
+                const ModeP p = mode_power2(grid[2 * m], grid[2 * m + 1], c, s_w1, g.half);
+                pair_atomic_add(s_H, s_L, bin_of(k2, g.c1, s_thr, g.nrbins), p.hi, p.lo);
             }
         }
     }
@@ -190,8 +197,10 @@ __global__ void __launch_bounds__(ROWS) k_bin_power_tma(const __grid_constant__ 
         *F0sq = (double)__fadd_rn(__fmul_rn(re, re), __fmul_rn(im, im));
     }
     __syncthreads();
-    for (int i = tid; i < g.nrbins; i += ROWS)
-        if (s_hist[i] != 0.0) atomicAdd(bin_sum + i, s_hist[i]);
+    for (int i = tid; i < g.nrbins; i += NT) {
+        const double v = (double)s_H[i] + (double)s_L[i];
+        if (v != 0.0) atomicAdd(bin_sum + i, v);
+    }
 }
 
 // ------------------------------------------------------------------ K1 (plain loads)
@@ -228,10 +237,14 @@ __global__ void k_bin_power_plain(GridArgs g, const int* __restrict__ thresh, co
 }
 
 // ------------------------------------------------------------------ K3 (TMA in/out)
-template <int ROWS, int STAGES>
-__global__ void __launch_bounds__(ROWS) k_correct_tma(const __grid_constant__ CUtensorMap tmap, GridArgs g,
-                                                      const int* __restrict__ thresh, const int* __restrict__ cmapg,
-                                                      CorrTable corr, float* grid, unsigned* status, int ntiles) {
+// The same tile engine; each thread multiplies its MPT modes in shared memory by
+// 1 + norm interp(log k), following the table segment of its modes (SegTrack); the tile
+// goes back by a TMA store.
+template <int ROWS, int STAGES, int MPT>
+__global__ void __launch_bounds__(ROWS * (16 / MPT), 1024 / (ROWS * (16 / MPT)))
+k_correct_tma(const __grid_constant__ CUtensorMap tmap, GridArgs g, const int* __restrict__ thresh,
+              const int* __restrict__ cmapg, CorrTable corr, float* grid, unsigned* status, int ntiles) {
+    constexpr int TPR = 16 / MPT, NT = ROWS * TPR;
     extern __shared__ unsigned char sm_raw[];
     __shared__ int s_abort;
     __shared__ long long s_rowbase;
@@ -244,16 +257,17 @@ __global__ void __launch_bounds__(ROWS) k_correct_tma(const __grid_constant__ CU
     int* s_cmap = reinterpret_cast<int*>(s_tab + 3 * g.nk);
     uint64_t* bars = reinterpret_cast<uint64_t*>(sm_raw + P.bar_off);
     const int tid = threadIdx.x;
-    for (int i = tid; i <= g.nrbins; i += ROWS) s_thr[i] = thresh[i];
-    for (int i = tid; i < g.nrbins; i += ROWS) s_cmap[i] = cmapg[i];
-    for (int i = tid; i < g.nk; i += ROWS) {
+    const int r = tid / TPR, q = tid - r * TPR;
+    for (int i = tid; i <= g.nrbins; i += NT) s_thr[i] = thresh[i];
+    for (int i = tid; i < g.nrbins; i += NT) s_cmap[i] = cmapg[i];
+    for (int i = tid; i < g.nk; i += NT) {
         s_tab[i] = corr.xf[i];
         s_tab[g.nk + i] = corr.rn[i];
         s_tab[2 * g.nk + i] = corr.sn[i];
     }
     if (tid == 0) {
         s_abort = 0;
-        for (int s = 0; s < STAGES; s++) mbar_init_(&bars[s], 1);
+        for (int st = 0; st < STAGES; st++) mbar_init_(&bars[st], 1);
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
     }
     __syncthreads();
@@ -267,31 +281,32 @@ __global__ void __launch_bounds__(ROWS) k_correct_tma(const __grid_constant__ CU
         }
     }
     unsigned flags = 0;
+    SegTrack seg;
     int k = 0;
     for (; k < my_n; k++) {
-        const int s = k % STAGES;
+        const int st = k % STAGES;
         const int tile = blockIdx.x + k * gridDim.x;
         if (tid == 0) {
-            if (!mbar_wait_bounded_(&bars[s], (k / STAGES) & 1)) s_abort = 1;
+            if (!mbar_wait_bounded_(&bars[st], (k / STAGES) & 1)) s_abort = 1;
             const long long m = (long long)tile * ROWS * 16;
             s_rowbase = m / g.nz;
             s_zbase = (int)(m - s_rowbase * g.nz);
         }
         __syncthreads();
         if (s_abort) break;
-        const long long row = (long long)tile * ROWS + tid;
+        const long long row = (long long)tile * ROWS + r;
         if (row < g.nrows16) {
-            unsigned char* rp = stage0 + (size_t)s * ROWS * 128 + (size_t)tid * 128;
+            unsigned char* rp = stage0 + (size_t)st * ROWS * 128 + (size_t)r * 128;
             KCursor c;
-            c.init(g, s_rowbase, s_zbase, tid * 16);
+            c.init(g, s_rowbase, s_zbase, r * 16 + q * MPT);
 #pragma unroll
-            for (int u = 0; u < 8; u++) {
-                float4* vp = reinterpret_cast<float4*>(rp + ((u ^ (tid & 7)) << 4));
+            for (int u = q * (MPT / 2); u < (q + 1) * (MPT / 2); u++) {
+                float4* vp = reinterpret_cast<float4*>(rp + ((u ^ (r & 7)) << 4));
                 float4 v = *vp;
                 {
                     const int k2 = c.kxy2 + c.z * c.z;
                     if (k2 != 0) {
-                        const float d = corr_delta(k2, g, T, flags);
+                        const float d = seg.delta(k2, g.lnscale, T, g.nk, flags);
                         v.x = fmaf(v.x, d, v.x);
                         v.y = fmaf(v.y, d, v.y);
                     }
@@ -300,7 +315,7 @@ __global__ void __launch_bounds__(ROWS) k_correct_tma(const __grid_constant__ CU
                 {
                     const int k2 = c.kxy2 + c.z * c.z;
                     if (k2 != 0) {
-                        const float d = corr_delta(k2, g, T, flags);
+                        const float d = seg.delta(k2, g.lnscale, T, g.nk, flags);
                         v.z = fmaf(v.z, d, v.z);
                         v.w = fmaf(v.w, d, v.w);
                     }
@@ -312,7 +327,7 @@ __global__ void __launch_bounds__(ROWS) k_correct_tma(const __grid_constant__ CU
         fence_async_smem();
         __syncthreads();
         if (tid == 0) {
-            tma_store_2d(&tmap, stage0 + (size_t)s * ROWS * 128, 0, tile * ROWS);
+            tma_store_2d(&tmap, stage0 + (size_t)st * ROWS * 128, 0, tile * ROWS);
             bulk_commit();
             if (k + STAGES - 1 < my_n) {
                 const int s2 = (k + STAGES - 1) % STAGES;
@@ -335,13 +350,13 @@ __global__ void __launch_bounds__(ROWS) k_correct_tma(const __grid_constant__ CU
     // trailing modes (fewer than 16) by CTA 0
     if (blockIdx.x == 0 && tid == 0) {
         for (long long m = g.nrows16 * 16; m < g.nmodes; m++) {
-            const long long r = m / g.nz;
-            const int z = (int)(m - r * g.nz);
-            const int il = (int)(r / g.N), j = (int)(r - (long long)il * g.N);
+            const long long rr = m / g.nz;
+            const int z = (int)(m - rr * g.nz);
+            const int il = (int)(rr / g.N), j = (int)(rr - (long long)il * g.N);
             const int kx = kval(g.slab0 + il, g.N), ky = kval(j, g.N);
             const int k2 = kx * kx + ky * ky + z * z;
             if (k2 != 0) {
-                const float d = corr_delta(k2, g, T, flags);
+                const float d = seg.delta(k2, g.lnscale, T, g.nk, flags);
                 grid[2 * m] = fmaf(grid[2 * m], d, grid[2 * m]);
                 grid[2 * m + 1] = fmaf(grid[2 * m + 1], d, grid[2 * m + 1]);
             }
@@ -474,34 +489,44 @@ static int sm_count() {
     return n;
 }
 
-template <int ROWS, int STAGES>
+template <int ROWS, int STAGES, int MPT>
 static int run_bin_tma(const GridGeom& g, const GridArgs& a, const float* grid, double* bin_sum, double* F0sq,
                        unsigned* status, cudaStream_t st) {
+    constexpr int NT = ROWS * (16 / MPT);
     CUtensorMap map;
     if (!make_map(&map, grid, a.nrows16, ROWS)) return -1;
     const SmemPlan P = plan_smem(ROWS, STAGES, g.nrbins, a.nz);
     if (P.total > 220 * 1024) return -1;
-    auto kern = k_bin_power_tma<ROWS, STAGES>;
+    auto kern = k_bin_power_tma<ROWS, STAGES, MPT>;
     cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)P.total);
     int per_sm = 1;
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, ROWS, P.total);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, NT, P.total);
     if (per_sm < 1) per_sm = 1;
     const int ntiles = (int)((a.nrows16 + ROWS - 1) / ROWS);
     int grid_n = sm_count() * per_sm;
     if (grid_n > ntiles) grid_n = ntiles > 0 ? ntiles : 1;
-    kern<<<grid_n, ROWS, P.total, st>>>(map, a, g.thresh, g.w1, grid, bin_sum, F0sq, status, ntiles);
+    kern<<<grid_n, NT, P.total, st>>>(map, a, g.thresh, g.w1, grid, bin_sum, F0sq, status, ntiles);
     return cudaPeekAtLastError() == cudaSuccess ? 0 : -2;
+}
+
+// tile shape: rows per CTA, pipeline stages, modes per thread (16: a thread per row;
+// 8: two threads per row)
+static int bin_variant(const GridGeom& g, const GridArgs& a, const float* grid, double* bin_sum, double* F0sq,
+                       unsigned* status, int rows, int stages, int mpt, cudaStream_t st) {
+#define KSP_BIN_CASE(R, S, M) \
+    if (rows == R && stages == S && mpt == M) return run_bin_tma<R, S, M>(g, a, grid, bin_sum, F0sq, status, st);
+    KSP_BIN_CASE(128, 2, 16) KSP_BIN_CASE(128, 3, 16) KSP_BIN_CASE(128, 4, 16) KSP_BIN_CASE(256, 2, 16)
+    KSP_BIN_CASE(256, 3, 16) KSP_BIN_CASE(128, 2, 8) KSP_BIN_CASE(128, 3, 8) KSP_BIN_CASE(128, 4, 8)
+    KSP_BIN_CASE(256, 2, 8) KSP_BIN_CASE(256, 3, 8)
+#undef KSP_BIN_CASE
+    return run_bin_tma<256, 2, 16>(g, a, grid, bin_sum, F0sq, status, st);
 }
 
 int launch_bin_power(const GridGeom& g, const float* grid, double* bin_sum, double* F0sq, unsigned* status, int tma,
                      int rows_per_cta, int stages, cudaStream_t st) {
     const GridArgs a = make_grid_args(g, 0, 0.f);
     if (tma && a.nrows16 > 0) {
-        int r = -1;
-        if (rows_per_cta == 256 && stages == 3) r = run_bin_tma<256, 3>(g, a, grid, bin_sum, F0sq, status, st);
-        else if (rows_per_cta == 256 && stages == 4) r = run_bin_tma<256, 4>(g, a, grid, bin_sum, F0sq, status, st);
-        else if (rows_per_cta == 128 && stages == 6) r = run_bin_tma<128, 6>(g, a, grid, bin_sum, F0sq, status, st);
-        else r = run_bin_tma<128, 4>(g, a, grid, bin_sum, F0sq, status, st);
+        const int r = bin_variant(g, a, grid, bin_sum, F0sq, status, rows_per_cta, stages, tma == 2 ? 8 : 16, st);
         if (r == 0) return 0;
         if (r == -2) return -2;
     }
@@ -515,34 +540,42 @@ int launch_bin_power(const GridGeom& g, const float* grid, double* bin_sum, doub
     return cudaPeekAtLastError() == cudaSuccess ? 1 : -2;
 }
 
-template <int ROWS, int STAGES>
+template <int ROWS, int STAGES, int MPT>
 static int run_corr_tma(const GridGeom& g, const GridArgs& a, float* grid, CorrTable corr, unsigned* status,
                         cudaStream_t st) {
+    constexpr int NT = ROWS * (16 / MPT);
     CUtensorMap map;
     if (!make_map(&map, grid, a.nrows16, ROWS)) return -1;
     const SmemPlan P = plan_smem(ROWS, STAGES, g.nrbins, 3 * a.nk + g.nrbins);
     if (P.total > 220 * 1024) return -1;
-    auto kern = k_correct_tma<ROWS, STAGES>;
+    auto kern = k_correct_tma<ROWS, STAGES, MPT>;
     cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)P.total);
     int per_sm = 1;
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, ROWS, P.total);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, NT, P.total);
     if (per_sm < 1) per_sm = 1;
     const int ntiles = (int)((a.nrows16 + ROWS - 1) / ROWS);
     int grid_n = sm_count() * per_sm;
     if (grid_n > ntiles) grid_n = ntiles > 0 ? ntiles : 1;
-    kern<<<grid_n, ROWS, P.total, st>>>(map, a, g.thresh, g.cmap, corr, grid, status, ntiles);
+    kern<<<grid_n, NT, P.total, st>>>(map, a, g.thresh, g.cmap, corr, grid, status, ntiles);
     return cudaPeekAtLastError() == cudaSuccess ? 0 : -2;
+}
+
+static int corr_variant(const GridGeom& g, const GridArgs& a, float* grid, CorrTable corr, unsigned* status,
+                        int rows, int stages, int mpt, cudaStream_t st) {
+#define KSP_CORR_CASE(R, S, M) \
+    if (rows == R && stages == S && mpt == M) return run_corr_tma<R, S, M>(g, a, grid, corr, status, st);
+    KSP_CORR_CASE(128, 2, 16) KSP_CORR_CASE(128, 3, 16) KSP_CORR_CASE(128, 4, 16) KSP_CORR_CASE(256, 2, 16)
+    KSP_CORR_CASE(256, 3, 16) KSP_CORR_CASE(128, 2, 8) KSP_CORR_CASE(128, 3, 8) KSP_CORR_CASE(128, 4, 8)
+    KSP_CORR_CASE(256, 2, 8) KSP_CORR_CASE(256, 3, 8)
+#undef KSP_CORR_CASE
+    return run_corr_tma<256, 2, 16>(g, a, grid, corr, status, st);
 }
 
 int launch_apply_correction(const GridGeom& g, float* grid, CorrTable corr, float lnscale, unsigned* status, int tma,
                             int rows_per_cta, int stages, cudaStream_t st) {
     const GridArgs a = make_grid_args(g, corr.nk, lnscale);
     if (tma && a.nrows16 > 0) {
-        int r = -1;
-        if (rows_per_cta == 256 && stages == 3) r = run_corr_tma<256, 3>(g, a, grid, corr, status, st);
-        else if (rows_per_cta == 256 && stages == 4) r = run_corr_tma<256, 4>(g, a, grid, corr, status, st);
-        else if (rows_per_cta == 128 && stages == 6) r = run_corr_tma<128, 6>(g, a, grid, corr, status, st);
-        else r = run_corr_tma<128, 4>(g, a, grid, corr, status, st);
+        const int r = corr_variant(g, a, grid, corr, status, rows_per_cta, stages, tma == 2 ? 8 : 16, st);
         if (r == 0) return 0;
         if (r == -2) return -2;
     }

@@ -153,9 +153,151 @@ struct RunAcc {
     }
 };
 
+// Per-CTA bin totals as float pairs (H, L) in shared memory, updated with FP32 atomics
+// only: H[b] += v by an atomic that returns the old value; the rounding error of that
+// addition is recomputed exactly (TwoSum of the old value and v; the hardware adds with
+// round-to-nearest) and added, with v's own low part, to L[b].  H + L then carries the
+// bin total to ~2^-48 relative, without the FP64 pipe.
+__device__ __forceinline__ void pair_atomic_add(float* H, float* L, int b, float hi, float lo) {
+    const float old = atomicAdd(H + b, hi);
+    const float s = __fadd_rn(old, hi);
+    const float bb = __fsub_rn(s, old);
+    const float e = __fadd_rn(__fsub_rn(old, __fsub_rn(s, bb)), __fsub_rn(hi, bb));
+    atomicAdd(L + b, __fadd_rn(e, lo));
+}
+
+// A run of modes in one bin, accumulated as a float pair with TwoSum; the bin is
+// tracked by its integer k^2 range [tlo, thi), so a mode costs two compares unless it
+// leaves the range.
+struct RunAcc32 {
+    int b = -1, tlo = 1, thi = 0;
+    float hi = 0.f, lo = 0.f;
+    __device__ __forceinline__ void flush(float* H, float* L) {
+        if (b >= 0) pair_atomic_add(H, L, b, hi, lo);
+        hi = 0.f;
+        lo = 0.f;
+    }
+    __device__ __forceinline__ void enter(int k2, const GridArgs& g, const int* thr, float* H, float* L) {
+        if (k2 < tlo || k2 >= thi) {
+            flush(H, L);
+            b = bin_of(k2, g.c1, thr, g.nrbins);
+            tlo = thr[b];
+            thi = b + 1 < g.nrbins ? thr[b + 1] : 0x7fffffff;
+        }
+    }
+    __device__ __forceinline__ void add(ModeP p) {
+        const float s = __fadd_rn(hi, p.hi);
+        const float bb = __fsub_rn(s, hi);
+        const float e = __fadd_rn(__fsub_rn(hi, __fsub_rn(s, bb)), __fsub_rn(p.hi, bb));
+        const float t = __fadd_rn(e, __fadd_rn(lo, p.lo));
+        hi = __fadd_rn(s, t);
+        lo = __fsub_rn(t, __fsub_rn(hi, s));
+    }
+};
+
+// Two adjacent bins b, b+1 accumulated as float pairs: a mode costs two compares and a
+// select unless it leaves [thr[b], thr[b+2]), where both pairs go to the CTA totals and
+// the window restarts at the mode's bin.  At the end of a thread's modes the pairs are
+// flushed by all threads together.
+struct BinPairAcc {
+    int b = -1, tlo = 1, thi2 = 0, thi = 0;
+    float ha = 0.f, la = 0.f, hb = 0.f, lb = 0.f;
+    __device__ __forceinline__ void flush(float* H, float* L) {
+        if (ha != 0.f || la != 0.f) pair_atomic_add(H, L, b, ha, la);
+        if (hb != 0.f || lb != 0.f) pair_atomic_add(H, L, b + 1, hb, lb);
+        ha = la = hb = lb = 0.f;
+    }
+    __device__ __forceinline__ void add(int k2, ModeP p, const GridArgs& g, const int* thr, float* H, float* L) {
+        if (k2 < tlo || k2 >= thi2) {
+            flush(H, L);
+            b = bin_of(k2, g.c1, thr, g.nrbins);
+            tlo = thr[b];
+            thi = thr[b + 1];
+            thi2 = b + 2 <= g.nrbins ? thr[b + 2] : 0x7fffffff;
+        }
+        const bool up = k2 >= thi;
+        float h = up ? hb : ha, l = up ? lb : la;
+        const float s = __fadd_rn(h, p.hi);
+        const float bb = __fsub_rn(s, h);
+        const float e = __fadd_rn(__fsub_rn(h, __fsub_rn(s, bb)), __fsub_rn(p.hi, bb));
+        const float t = __fadd_rn(e, __fadd_rn(l, p.lo));
+        h = __fadd_rn(s, t);
+        l = __fsub_rn(t, __fsub_rn(h, s));
+        if (up) { hb = h; lb = l; } else { ha = h; la = l; }
+    }
+};
+
 // ------------------------------------------------------------------ K3 helpers
 struct CorrSmem {
     const int* thr; const int* cmap; const float* xf; const float* rn; const float* sn;
+};
+
+// The correction factor of one bin's modes, resolved once per bin: modes with
+// x = log k below the bin's node use segment (x0a, sa, ra), the others (x0b, sb, rb);
+// the same arithmetic as corr_delta.
+struct CorrRun {
+    int b = -1, tlo = 1, thi = 0;
+    float xc, x0a, sa, ra, x0b, sb, rb, xwarn;
+    bool bad;
+    __device__ __forceinline__ void enter(int k2, const GridArgs& g, const CorrSmem& t) {
+        if (k2 >= tlo && k2 < thi) return;
+        b = bin_of(k2, g.c1, t.thr, g.nrbins);
+        tlo = t.thr[b];
+        thi = b + 1 < g.nrbins ? t.thr[b + 1] : 0x7fffffff;
+        const int c = t.cmap[b];
+        bad = c < 0;
+        xwarn = -3.0e38f;
+        if (bad) { xc = 0.f; x0a = x0b = 0.f; sa = sb = 0.f; ra = rb = 0.f; return; }
+        const int nk = g.nk;
+        xc = t.xf[c];
+        if (c == 0) {  // below the first node: constant (delta_pow.c:26-29)
+            x0a = 0.f; sa = 0.f; ra = t.rn[0];
+            xwarn = t.xf[0] - 0.69314718f;
+        } else {
+            x0a = t.xf[c - 1]; sa = t.sn[c - 1]; ra = t.rn[c - 1];
+        }
+        if (c >= nk - 1) { x0b = 0.f; sb = 0.f; rb = t.rn[nk - 1]; }
+        else { x0b = t.xf[c]; sb = t.sn[c]; rb = t.rn[c]; }
+    }
+    // correction minus one for a mode of this bin with integer k^2
+    __device__ __forceinline__ float delta(int k2, float lnscale, unsigned& flags) const {
+        const float x = fmaf(0.5f, __logf((float)k2), lnscale);
+        if (bad) { flags |= kStGsl; return 0.f; }
+        if (x < xwarn) flags |= kStKWarn;
+        const bool below = x < xc;
+        const float x0 = below ? x0a : x0b, sl = below ? sa : sb, r0 = below ? ra : rb;
+        return fmaf(x - x0, sl, r0);  // the constant ends have sl = 0: exactly r0
+    }
+};
+
+// The correction as a function of x = log k (delta_pow.c:19-37): linear on the
+// segments [xf[j], xf[j+1]) of the table, constant below xf[0] and from xf[nk-1] on.
+// A thread keeps its current segment and moves it only when x leaves [xlo, xhi).
+struct SegTrack {
+    float xlo = 3.0e38f, xhi = -3.0e38f, x0 = 0.f, sl = 0.f, r0 = 0.f, xwarn = -3.0e38f;
+    __device__ __forceinline__ void locate(float x, const CorrSmem& t, int nk) {
+        // largest j with xf[j] <= x (j = -1 below the table)
+        int lo = -1, hi = nk;
+        while (hi - lo > 1) {
+            const int mid = (lo + hi) >> 1;
+            if (t.xf[mid] <= x) lo = mid; else hi = mid;
+        }
+        xwarn = -3.0e38f;
+        if (lo < 0) {  // below the first node: constant
+            xlo = -3.0e38f; xhi = t.xf[0]; x0 = 0.f; sl = 0.f; r0 = t.rn[0];
+            xwarn = t.xf[0] - 0.69314718f;
+        } else if (lo >= nk - 1) {  // from the last node on: constant
+            xlo = t.xf[nk - 1]; xhi = 3.0e38f; x0 = 0.f; sl = 0.f; r0 = t.rn[nk - 1];
+        } else {
+            xlo = t.xf[lo]; xhi = t.xf[lo + 1]; x0 = t.xf[lo]; sl = t.sn[lo]; r0 = t.rn[lo];
+        }
+    }
+    __device__ __forceinline__ float delta(int k2, float lnscale, const CorrSmem& t, int nk, unsigned& flags) {
+        const float x = fmaf(0.5f, __logf((float)k2), lnscale);
+        if (x < xlo || x >= xhi) locate(x, t, nk);
+        if (x < xwarn) flags |= kStKWarn;
+        return fmaf(x - x0, sl, r0);
+    }
 };
 
 // 1 + norm*interp(log k) - 1 for a mode with integer k^2 (delta_pow.c:19-37 clamping)

@@ -203,7 +203,12 @@ void launch_delta_tot_init(const IntegratorDev& I, int nk, const double* wavenum
 __global__ void k_scalars(IntegratorDev I, int Na, double a, double loga, double loga0, double TimeTransfer,
                           int start_row) {
     const double* xk = I.scalefact;
-    for (int i = threadIdx.x; i + 1 < Na; i += blockDim.x) I.knot_invh[i] = 1.0 / (xk[i + 1] - xk[i]);
+    for (int i = threadIdx.x; i + 1 < Na; i += blockDim.x) {
+        const double h = xk[i + 1] - xk[i];
+        I.knot_invh[i] = 1.0 / h;
+        I.knot_h3[i] = h / 3.0;
+        I.knot_ih3[i] = 1.0 / (3.0 * h);
+    }
     if (threadIdx.x != 0) return;
     const Background& B = *I.B;
     StepScalars& S = *I.sc;
@@ -389,36 +394,30 @@ __global__ void k_dtot_coeffs(IntegratorDev I, int nk, int Na) {
     }
 }
 
-// ------------------------------------------------------------------ delta_nu integral
-struct DnuIntegrand {  // delta_tot_table.c:492-500
-    const Background* B;
-    double k, mnubykT, qc, nufrac_low;
-    const double* fs_x; const double* fs_y; const double* fs_c; int nfs; double fs_x0, fs_inv;
-    const double* kx; const double* ky; const double* kc; int na;
-    __device__ double operator()(double logai) const {
-        // free-streaming spline (uniform knots: direct index, settled against stored knots)
-        int i = (int)((logai - fs_x0) * fs_inv);
-        i = i < 0 ? 0 : (i > nfs - 2 ? nfs - 2 : i);
-        while (i > 0 && logai < __ldg(fs_x + i)) i--;
-        while (i < nfs - 2 && logai >= __ldg(fs_x + i + 1)) i++;
-        double fsl;
-        {
-            const double x0 = __ldg(fs_x + i), x1 = __ldg(fs_x + i + 1);
-            const double y0 = __ldg(fs_y + i), y1 = __ldg(fs_y + i + 1);
-            const double c0 = __ldg(fs_c + i), c1 = __ldg(fs_c + i + 1);
-            const double h = x1 - x0, dx = logai - x0;
-            const double b = (y1 - y0) / h - h * (c1 + 2.0 * c0) / 3.0;
-            const double d = (c1 - c0) / (3.0 * h);
-            fsl = y0 + dx * (b + dx * (c0 + dx * d));
-        }
-        const int j = seg_bsearch(kx, na, logai);
-        const double dt = na > 2 ? cspline_seg(kx, ky, kc, j, logai) : linear_seg(kx, ky, j, logai);
-        const double specJ = specialJ(k * fsl / mnubykT, qc, nufrac_low);
-        const double ai = exp(logai);
-        return fsl / (ai * hubble(*B, ai)) * specJ * dt;
-    }
-};
+// ------------------------------------------------------------------ node table
+// The k-independent terms of the delta_nu integrand at the 61 nodes of the first
+// kNcLevels levels of QAG's bisection of [log a0, log a]: thread per (slot, node).
+__global__ void k_nc_build(IntegratorDev I, int Na) {
+    const int q = blockIdx.x * blockDim.x + threadIdx.x;
+    if (q >= kNcNodes) return;
+    const StepScalars& S = *I.sc;
+    const int slot = q / 61, jn = q - 61 * slot;
+    double lo, hi;
+    nc_interval(slot, S.loga0, S.loga, &lo, &hi);
+    const double c = __dmul_rn(0.5, __dadd_rn(lo, hi));
+    const double h = __dmul_rn(0.5, __dsub_rn(hi, lo));
+    const double XK[31] = KSP_GK61_XK_INIT;  // the abscissae of gk61_fill
+    const double xk = jn < 30 ? -XK[jn] : (jn < 60 ? XK[jn - 30] : 0.0);
+    const double x = __dadd_rn(c, __dmul_rn(h, xk));
+    const double fs_inv = (S.Nfs - 1.) / (S.loga - S.loga0);
+    const NodeTerms t = dnu_node_terms(I.B, I.fs_x, I.fs_y, I.fs_c, S.Nfs, S.loga0, fs_inv, I.scalefact, Na, x);
+    I.nc_g[q] = t.g;
+    I.nc_fsl[q] = t.fsl;
+    I.nc_dx[q] = t.dx;
+    I.nc_j[q] = t.j;
+}
 
+// ------------------------------------------------------------------ delta_nu integral
 // Shared memory per CTA: Gk61Nodes | knots[ld] | per warp: QagList, row[ld], coef[ld] | mbarriers
 __global__ void __launch_bounds__(128) k_dnu_qag(IntegratorDev I, int nk, int Na, int nspec, int4 spec_ids) {
     extern __shared__ __align__(16) unsigned char sm[];
@@ -477,12 +476,8 @@ __global__ void __launch_bounds__(128) k_dnu_qag(IntegratorDev I, int nk, int Na
                 return;
             }
             const double qc = S.partnu_now > 0 ? B->vcrit * mnubykT : 0.0;
-            DnuIntegrand f;
-            f.B = B; f.k = k; f.mnubykT = mnubykT; f.qc = qc; f.nufrac_low = B->nufrac_low[0];
-            f.fs_x = I.fs_x; f.fs_y = I.fs_y; f.fs_c = I.fs_c; f.nfs = S.Nfs; f.fs_x0 = S.loga0;
-            f.fs_inv = (S.Nfs - 1.) / (S.loga - S.loga0);
-            f.kx = knots; f.ky = row; f.kc = rc; f.na = Na;
-            QagResult r = qag_warp(f, N, L, S.loga0, S.loga, 0.0, S.relerr, kQagLimit);
+            const DnuIntegrandC f = dnu_integrand(I, S, k, mnubykT, qc, knots, row, rc, Na);
+            QagResult r = qag_warp_c(f, N, L, S.loga0, S.loga, 0.0, S.relerr, kQagLimit);
             val += S.prefac * r.result;
             if (I.ivals) {  // keep the final subdivision for the adjoint
                 double* dst = I.ivals + ((size_t)mi * I.nk_alloc + ik) * kQagLimit * 2;
@@ -564,6 +559,7 @@ void launch_delta_nu_combined(const IntegratorDev& I, int nk, int Na, double a, 
         cudaMemsetAsync(&I.sc->Nfs, 0, sizeof(int), st);
     }
     if (Na > 2) k_dtot_coeffs<<<(nk + 127) / 128, 128, 0, st>>>(I, nk, Na);
+    if (loga > loga0 && Na > 1) k_nc_build<<<(kNcNodes + 127) / 128, 128, 0, st>>>(I, Na);
     const int wpb = warps_per_block < 1 ? 1 : (warps_per_block > 4 ? 4 : warps_per_block);
     const size_t smem = dnu_qag_smem(I.ld, wpb);
     static bool attr_set = false;

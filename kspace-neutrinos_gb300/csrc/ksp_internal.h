@@ -40,6 +40,12 @@ struct IntegratorDev {
     double* knot_invdiag;            // [namax] factorised spline system of the knots
     double* knot_fac;                // [namax]
     double* knot_invh;               // [namax] 1/(x_{i+1}-x_i)
+    double* knot_h3;                 // [namax] (x_{i+1}-x_i)/3
+    double* knot_ih3;                // [namax] 1/(3 (x_{i+1}-x_i))
+    double* nc_g;                    // [kNcNodes] node table of the delta_nu integrand (NodeCache)
+    double* nc_fsl;
+    double* nc_dx;
+    int* nc_j;
     double* fs_x;                    // [fs_cap]
     double* fs_y;                    // [fs_cap]
     double* fs_c;                    // [fs_cap]
@@ -56,6 +62,23 @@ struct IntegratorDev {
     double* ivals;                   // optional: final QAG intervals [kNuSpecies][nk_alloc][kQagLimit][2]
     int* nivals;                     // [kNuSpecies][nk_alloc]
 };
+
+#ifdef __CUDACC__
+// The delta_nu integrand of one (species, bin) with the instance's node table; knots,
+// row and rc may be staged copies (shared memory) of the instance's arrays.
+__device__ __forceinline__ DnuIntegrandC dnu_integrand(const IntegratorDev& I, const StepScalars& S, double k,
+                                                       double mnubykT, double qc, const double* knots,
+                                                       const double* row, const double* rc, int Na) {
+    DnuIntegrandC f;
+    f.B = I.B; f.k = k; f.mnubykT = mnubykT; f.qc = qc; f.nfl = I.B->nufrac_low[0];
+    f.fs_x = I.fs_x; f.fs_y = I.fs_y; f.fs_c = I.fs_c; f.nfs = S.Nfs; f.fs_x0 = S.loga0;
+    f.fs_inv = (S.Nfs - 1.) / (S.loga - S.loga0);
+    f.kx = knots; f.ky = row; f.kc = rc; f.na = Na;
+    f.ks = KnotSeg{I.knot_invh, I.knot_h3, I.knot_ih3};
+    f.nc = NodeCache{I.nc_g, I.nc_fsl, I.nc_dx, I.nc_j};
+    return f;
+}
+#endif
 
 // Interpolation table for the grid correction (delta_pow.c:19-37), float, per
 // non-empty bin, plus the bin -> compact index map.

@@ -24,8 +24,9 @@ L = 512.0
 
 def make_params(M, seed):
     ps = W.batch_instances(M, seed=seed, Na_range=(16, 48), nk_range=(64, 96))
-    ps[3]["MNu"] = (0.02, 0.03, 0.06)  # non-degenerate: three species
-    ps[5]["MNu"] = (0.05, 0.05, 0.1)   # two species
+    if M > 5:
+        ps[3]["MNu"] = (0.02, 0.03, 0.06)  # non-degenerate: three species
+        ps[5]["MNu"] = (0.05, 0.05, 0.1)   # two species
     return ps
 
 

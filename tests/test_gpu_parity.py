@@ -75,6 +75,9 @@ def test_full_step(gpu, oracle, N, nb, Na):
     g_o = c["grid"].copy()
     g_d = torch.as_tensor(c["grid"]).cuda()
     for a in (0.51, 0.512):
+        # both sides start the step from the same grid (the corrected grids of the
+        # previous step agree to TOL_GRID, not bit for bit)
+        g_d.copy_(torch.as_tensor(g_o))
         st, out = oracle.add_nu_power_to_rhogrid(s, a, c["L"], g_o, N)
         assert st == 0
         k.add_nu_power_to_rhogrid(a, c["L"], g_d, N)
