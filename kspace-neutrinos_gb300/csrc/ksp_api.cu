@@ -89,6 +89,10 @@ extern "C" int kspace_gpu_create(kspace_ctx** out, int device) {
     if (const char* e = getenv("KSPACE_GPU_ROWS")) c->rows = atoi(e);
     if (const char* e = getenv("KSPACE_GPU_STAGES")) c->stages = atoi(e);
     if (const char* e = getenv("KSPACE_GPU_QAG_WARPS")) c->qag_warps = atoi(e);
+    if (const char* e = getenv("KSPACE_GPU_NC_LEVELS")) {
+        const int l = atoi(e);
+        c->nc_levels = l < 0 ? 0 : (l > kNcMaxLevels ? kNcMaxLevels : l);
+    }
     *out = c;
     return KSPACE_OK;
 }
@@ -363,6 +367,7 @@ extern "C" int kspace_gpu_alloc_table(kspace_ctx* c, int nk_alloc, double TimeTr
     CK(dalloc(&I.nc_fsl, kNcNodes));
     CK(dalloc(&I.nc_dx, kNcNodes));
     CK(dalloc(&I.nc_j, kNcNodes));
+    I.nc_slots = (1 << c->nc_levels) - 1;
     I.fs_cap = 16 * (int)ld + 16;
     CK(dalloc(&I.fs_x, I.fs_cap));
     CK(dalloc(&I.fs_y, I.fs_cap));

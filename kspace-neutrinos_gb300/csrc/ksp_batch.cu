@@ -10,7 +10,7 @@
 //   kb_fs_segments  every instance's fslength segments (4-point Gauss-Legendre)
 //   kb_fs_finish    block per instance: suffix sums of the segments -> fslength table
 //   kb_fs_coeffs    thread per (instance, unknown): natural spline of the table
-//   kb_dtot_coeffs  thread per (instance, bin): history-row spline coefficients
+//   kb_dtot_coeffs  warp per (instance, bin): history-row spline coefficients
 //   kb_nc_build     thread per (instance, node): node tables of the integrand
 //   kb_dnu_qag      persistent warps that pull (instance, species, bin) tasks from an
 //                   atomic queue; knots, row and coefficients staged into shared memory
@@ -40,65 +40,35 @@ __device__ __forceinline__ int owner_of(const int* off, int n, int v) {
 constexpr int kBatchSmallBlocks = 4 * 152;
 
 // ------------------------------------------------------------------ prologue
-// update_delta_tot's provisional row (as k_update_row), then the call scalars and the
-// knot factorisation (as k_scalars).
+// The call scalars (as k_scalars), update_delta_tot's provisional row (as k_update_row)
+// and the knot factorisation (as k_scalars).
 __global__ void kb_prologue(BatchDev b) {
     if (blockIdx.x == 0 && threadIdx.x == 0) b.hdr->counter = 0;
-    __shared__ double s3[3];
     for (int i = blockIdx.x; i < b.M; i += gridDim.x) {
         const BatchCall& P = b.calls[i];
-        __syncthreads();  // s3 reuse across instances
+        __syncthreads();  // the previous instance's scalars are complete
         if (!P.active) continue;
         const IntegratorDev& I = b.insts[i];
-        const Background& B = *I.B;
         StepScalars& S = *I.sc;
         const double a = P.a;
         const int Na = P.Na;
         const bool integrate = P.commit_row != -2;
-        if (threadIdx.x == 0) {
-            s3[0] = omega_nu_nopart(B, a) * (a * a * a);
-            s3[1] = omega_nu(B, 1);
-            s3[2] = particle_nu_fraction(B, a, 0);
-            if (integrate) I.scalefact[Na - 1] = P.loga;
-        }
+        if (threadIdx.x < 32) call_scalars_warp(*I.B, a, P.loga, P.loga0, P.TimeTransfer, integrate ? Na : 1, S);
+        if (threadIdx.x == 0 && integrate) I.scalefact[Na - 1] = P.loga;
         __syncthreads();
-        if (integrate) {
-            const double Omeganonu = S.Omeganonu;
-            for (int ik = threadIdx.x; ik < P.nk; ik += blockDim.x)
-                I.dtot[(size_t)ik * I.ld + Na - 1] =
-                    get_delta_tot(I.nu_last[ik], I.dcdm[ik], s3[0], Omeganonu, s3[1], s3[2]);
-            const double* xk = I.scalefact;
-            for (int j = threadIdx.x; j + 1 < Na; j += blockDim.x) {
-                const double h = xk[j + 1] - xk[j];
-                I.knot_invh[j] = 1.0 / h;
-                I.knot_h3[j] = h / 3.0;
-                I.knot_ih3[j] = 1.0 / (3.0 * h);
-            }
+        if (!integrate) continue;
+        const double OmegaNua3 = S.OmegaNua3, OmegaNu1 = S.OmegaNu1, partnu = S.partnu, Omeganonu = S.Omeganonu;
+        for (int ik = threadIdx.x; ik < P.nk; ik += blockDim.x)
+            I.dtot[(size_t)ik * I.ld + Na - 1] =
+                get_delta_tot(I.nu_last[ik], I.dcdm[ik], OmegaNua3, Omeganonu, OmegaNu1, partnu);
+        const double* xk = I.scalefact;
+        for (int j = threadIdx.x; j + 1 < Na; j += blockDim.x) {
+            const double h = xk[j + 1] - xk[j];
+            I.knot_invh[j] = 1.0 / h;
+            I.knot_h3[j] = h / 3.0;
+            I.knot_ih3[j] = 1.0 / (3.0 * h);
         }
         if (threadIdx.x != 0) continue;
-        S.a = a;
-        S.loga = P.loga;
-        S.loga0 = P.loga0;
-        S.Na = integrate ? Na : 1;
-        S.OmegaNua3 = omega_nu_nopart(B, a) * (a * a * a);
-        S.OmegaNu1 = omega_nu(B, 1);
-        S.partnu = particle_nu_fraction(B, a, 0);
-        S.Omega_nu_tot = omega_nu_nopart(B, a);
-        for (int mi = 0; mi < kNuSpecies; mi++)
-            S.omeganu[mi] = B.deg[mi] > 0 ? B.deg[mi] * omega_nu_single(B, a, mi) : 0.0;
-        const double TT = P.TimeTransfer;
-        S.deriv_prefac = TT * (hubble(B, TT) / S.light) * TT;
-        S.relerr = 1e-6;
-        S.partnu_now = particle_nu_fraction(B, a, 0);
-        S.skip_integral = 0;
-        if (S.partnu_now > 0) {
-            if (1 - S.partnu_now < 1e-3) S.skip_integral = 1;
-            S.relerr /= (1. + 1e-5 - S.partnu_now);
-        }
-        const double OmegaNu_nop = omega_nu_nopart(B, a);
-        const double omega_hybrid = omega_nu(B, a) - OmegaNu_nop;
-        S.kspace_prefac = OmegaNu_nop / (S.Omeganonu / (a * a * a) + omega_hybrid);
-        if (!integrate) continue;
         if (P.nfs == 0) {
             S.fsl_A0a = 0.0;
             S.Nfs = 0;
@@ -246,48 +216,32 @@ __global__ void kb_fs_coeffs(BatchDev b) {
 }
 
 // ------------------------------------------------------------------ history splines
+// warp per (instance, bin), as k_dtot_coeffs
 __global__ void kb_dtot_coeffs(BatchDev b) {
+    extern __shared__ __align__(16) double sdc[];
+    const int warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+    const bool staged = 8 * sizeof(double) * (size_t)b.ldmax <= 200 * 1024;
+    double* sy = staged ? sdc + (size_t)warp * 2 * b.ldmax : nullptr;
+    double* sc = staged ? sy + b.ldmax : nullptr;
     const int total = b.hdr->total_bins;
-    for (int g = blockIdx.x * blockDim.x + threadIdx.x; g < total; g += gridDim.x * blockDim.x) {
+    for (int g = blockIdx.x * nw + warp; g < total; g += gridDim.x * nw) {
         const int i = owner_of(b.bin_off, b.M, g);
         const int ik = g - __ldg(b.bin_off + i);
         const BatchCall& P = b.calls[i];
-        const int Na = P.Na;
-        if (!P.active || P.commit_row == -2 || Na <= 2) continue;
-        const IntegratorDev& I = b.insts[i];
-        const double* y = I.dtot + (size_t)ik * I.ld;
-        double* c = I.coef + (size_t)ik * I.ld;
-        const double* ih = I.knot_invh;
-        const int m = Na - 2;
-        double prev = 0;
-        for (int k = 0; k < m; k++) {
-            double r = 3.0 * ((y[k + 2] - y[k + 1]) * ih[k + 1] - (y[k + 1] - y[k]) * ih[k]);
-            if (k > 0) r -= I.knot_fac[k] * prev;
-            prev = r;
-            c[k + 1] = r;
-        }
-        c[0] = 0.0;
-        c[Na - 1] = 0.0;
-        double next = c[m] * I.knot_invdiag[m - 1];
-        c[m] = next;
-        const double* x = I.scalefact;
-        for (int k = m - 1; k-- > 0;) {
-            const double off = x[k + 2] - x[k + 1];
-            next = (c[k + 1] - off * next) * I.knot_invdiag[k];
-            c[k + 1] = next;
-        }
+        if (!P.active || P.commit_row == -2 || P.Na <= 2) continue;
+        dtot_row_coeffs_warp(b.insts[i], ik, P.Na, sy, sc);
     }
 }
 
-// ------------------------------------------------------------------ delta_nu integrals
 // thread per (instance, slot, node): the node tables (as k_nc_build)
 __global__ void kb_nc_build(BatchDev b) {
     const double XK[31] = KSP_GK61_XK_INIT;  // the abscissae of gk61_fill
-    const long long total = (long long)b.M * kNcNodes;
+    const int per = b.nc_slots * 61;
+    const long long total = (long long)b.M * per;
     for (long long g = blockIdx.x * (long long)blockDim.x + threadIdx.x; g < total;
          g += (long long)gridDim.x * blockDim.x) {
-        const int i = (int)(g / kNcNodes);
-        const int q = (int)(g - (long long)i * kNcNodes);
+        const int i = (int)(g / per);
+        const int q = (int)(g - (long long)i * per);
         const BatchCall& P = b.calls[i];
         if (!P.active || P.commit_row == -2 || P.nfs <= 0 || P.Na <= 1) continue;
         const IntegratorDev& I = b.insts[i];
@@ -464,6 +418,7 @@ static void gl_nodes_b(int n, double* X, double* Wt) {  // Newton on P_n, positi
 
 void batch_set_attributes() {
     cudaFuncSetAttribute(kb_dnu_qag, cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024);
+    cudaFuncSetAttribute(kb_dtot_coeffs, cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024);
 }
 
 void launch_batch_update(const BatchDev& b, cudaStream_t st) {
@@ -478,7 +433,8 @@ void launch_batch_update(const BatchDev& b, cudaStream_t st) {
     kb_fs_segments<<<nb, 256, 0, st>>>(b, gl);
     kb_fs_finish<<<b.M < 2 * 152 ? b.M : 2 * 152, 1024, 0, st>>>(b);
     kb_fs_coeffs<<<nb, 128, 0, st>>>(b);
-    kb_dtot_coeffs<<<nb, 128, 0, st>>>(b);
+    const size_t dc_smem = 4 * 2 * sizeof(double) * (size_t)b.ldmax;
+    kb_dtot_coeffs<<<nb, 128, dc_smem <= 200 * 1024 ? dc_smem : 0, st>>>(b);
     kb_nc_build<<<nb, 128, 0, st>>>(b);
     kb_dnu_qag<<<b.qag_blocks, 32 * b.wpb, batch_qag_smem(b.ldmax, b.wpb), st>>>(b);
     kb_finish<<<nb, 256, 0, st>>>(b);

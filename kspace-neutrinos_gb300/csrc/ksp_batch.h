@@ -44,6 +44,7 @@ struct BatchDev {
     const int* task_off;
     double* dnu_pool;   // [total_bins] delta_nu returned by every instance
     int M, ldmax, wpb, qag_blocks;
+    int nc_slots;       // node-table slots of every instance (their IntegratorDev.nc_slots)
 };
 
 // Correction table of a grid bound to instance `inst` (interface_common.c:134-146).

@@ -10,6 +10,7 @@
 #include <math.h>
 #include <stdio.h>
 #include <string.h>
+#include <stdlib.h>
 #include <algorithm>
 #include <vector>
 #include "ksp_batch.h"
@@ -48,6 +49,7 @@ struct kspace_batch {
     int total_bins = 0, ldmax = 0;
     // tuning
     int wpb = 4, blocks_per_sm = 2, use_graph = 1;
+    int nc_slots = 15;  // node-table slots per instance (4 levels)
     bool eager_done = false;
     cudaGraph_t graph = nullptr;
     cudaGraphExec_t exec = nullptr;
@@ -105,6 +107,10 @@ extern "C" int kspace_gpu_batch_create(kspace_batch** out, kspace_ctx* const* ct
         b->ldmax = std::max(b->ldmax, ctxs[i]->I.ld);
     }
     b->last_status.assign(M, 0);
+    if (const char* e = getenv("KSPACE_GPU_NC_LEVELS")) {
+        const int l = atoi(e);
+        b->nc_slots = (1 << (l < 0 ? 0 : (l > kNcMaxLevels ? kNcMaxLevels : l))) - 1;
+    }
     batch_set_attributes();
     *out = b;
     return KSPACE_OK;
@@ -181,6 +187,7 @@ static BatchDev dev_view(kspace_batch* b) {
     d.ldmax = b->ldmax;
     d.wpb = b->wpb;
     d.qag_blocks = b->sm_count * b->blocks_per_sm;
+    d.nc_slots = b->nc_slots;
     return d;
 }
 
@@ -211,6 +218,7 @@ static int lay_out(kspace_batch* b, const int* nk_in) {
         desc[i].status = b->status_d + i;
         desc[i].ivals = nullptr;
         desc[i].nivals = nullptr;
+        desc[i].nc_slots = b->nc_slots;
     }
     CKB(cudaMemcpy(b->insts_d, desc.data(), sizeof(IntegratorDev) * M, cudaMemcpyHostToDevice));
     if (!b->grids.empty()) {

@@ -33,7 +33,8 @@ struct kspace_ctx {
     cudaStream_t stream = nullptr, own_stream = nullptr;
     kspace_allreduce_fn ar_fn = nullptr;
     void* ar_user = nullptr;
-    int tma = 1, rows = 256, stages = 2, qag_warps = 1;  // measured best on the N=512 step
+    int tma = 2, rows = 128, stages = 2, qag_warps = 1;  // measured best on the N=512 step
+    int nc_levels = 4;  // levels of QAG's bisection tree kept in the integrand node table
     // background
     bool bg_ready = false, hubble_ready = false;
     Background hB;

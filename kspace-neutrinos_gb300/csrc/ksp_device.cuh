@@ -425,12 +425,13 @@ __device__ QagResult qag_warp(const F& f, const Gk61Nodes& N, QagList& L, double
 // of the first kNcLevels levels are numbered in heap order (root 0, children of s:
 // 2s+1, 2s+2).  A functor with node(slot, j, x) may serve the 61 nodes of such an
 // interval from a table built once; x is passed for the others (slot -1).
-constexpr int kNcLevels = 4;
-constexpr int kNcSlots = (1 << kNcLevels) - 1;  // 15 intervals
-constexpr int kNcNodes = kNcSlots * 61;
+constexpr int kNcMaxLevels = 6;
+constexpr int kNcMaxSlots = (1 << kNcMaxLevels) - 1;  // 63 intervals
+constexpr int kNcNodes = kNcMaxSlots * 61;               // capacity of a node table
 
-__device__ __forceinline__ int nc_child(int s, int right) {
-    return (s >= 0 && 2 * s + 2 < kNcSlots) ? 2 * s + 1 + right : -1;
+// child slot of s (right = 0, 1) in a table of nslots = 2^levels - 1 slots
+__device__ __forceinline__ int nc_child(int s, int right, int nslots) {
+    return (s >= 0 && 2 * s + 2 < nslots) ? 2 * s + 1 + right : -1;
 }
 
 // gk61_warp with interval slots (same arithmetic)
@@ -496,9 +497,9 @@ __device__ QagResult qag_warp_c(const F& f, const Gk61Nodes& N, QagList& L, doub
     QagResult R;
     GkOut g[2];
     double aa[2] = {a, a}, bb[2] = {b, b};
-    int ss[2] = {0, -1};
+    int ss[2] = {f.nc.nslots > 0 ? 0 : -1, -1};
     gk61_warp_c(f, N, 1, aa, bb, ss, g);
-    if (lane == 0) { L.a[0] = a; L.b[0] = b; L.r[0] = g[0].result; L.e[0] = g[0].abserr; L.slot[0] = 0; }
+    if (lane == 0) { L.a[0] = a; L.b[0] = b; L.r[0] = g[0].result; L.e[0] = g[0].abserr; L.slot[0] = ss[0]; }
     __syncwarp();
     double tol = fmax(epsabs, epsrel * fabs(g[0].result));
     const double round_off = 50 * DBL_EPSILON * g[0].resabs;
@@ -528,8 +529,8 @@ __device__ QagResult qag_warp_c(const F& f, const Gk61Nodes& N, QagList& L, doub
         const int s_i = L.slot[k];
         const double a1 = a_i, b1 = 0.5 * (a_i + b_i), a2 = b1, b2 = b_i;
         aa[0] = a1; bb[0] = b1; aa[1] = a2; bb[1] = b2;
-        ss[0] = nc_child(s_i, 0);
-        ss[1] = nc_child(s_i, 1);
+        ss[0] = nc_child(s_i, 0, f.nc.nslots);
+        ss[1] = nc_child(s_i, 1, f.nc.nslots);
         gk61_warp_c(f, N, 2, aa, bb, ss, g);
         const double area12 = g[0].result + g[1].result, error12 = g[0].abserr + g[1].abserr;
         errsum += error12 - e_i;
@@ -609,7 +610,9 @@ struct KnotSeg {
 
 // The per-bin rest: J and the history row's natural spline (or linear for 2 knots) at
 // the node.  Same for the cached and uncached paths.
-__device__ __forceinline__ double dnu_combine(const NodeTerms& t, double k, double mnubykT, double qc, double nfl,
+// k_over_m = k / (m / kT): J's argument is fslength * k_over_m (one division per bin
+// instead of one per node).
+__device__ __forceinline__ double dnu_combine(const NodeTerms& t, double k_over_m, double qc, double nfl,
                                               const double* ky, const double* kc, int na, const KnotSeg& ks) {
     const int j = t.j;
     const double y0 = ky[j], y1 = ky[j + 1];
@@ -622,22 +625,23 @@ __device__ __forceinline__ double dnu_combine(const NodeTerms& t, double k, doub
     } else {
         S = y0 + t.dx * ((y1 - y0) * __ldg(ks.ih + j));
     }
-    const double J = specialJ(k * t.fsl / mnubykT, qc, nfl);
+    const double J = specialJ(t.fsl * k_over_m, qc, nfl);
     return t.g * J * S;
 }
 
-// Node table of one instance for one call: kNcNodes entries, slot-major.
+// Node table of one instance for one call: nslots * 61 entries, slot-major.
 struct NodeCache {
     double* g;
     double* fsl;
     double* dx;
     int* j;
+    int nslots;
 };
 
 // The full integrand with the node table.
 struct DnuIntegrandC {
     const Background* B;
-    double k, mnubykT, qc, nfl;
+    double k_over_m, qc, nfl;
     const double* fs_x; const double* fs_y; const double* fs_c; int nfs; double fs_x0, fs_inv;
     const double* kx; const double* ky; const double* kc; int na;
     KnotSeg ks;
@@ -653,7 +657,7 @@ struct DnuIntegrandC {
         } else {
             t = dnu_node_terms(B, fs_x, fs_y, fs_c, nfs, fs_x0, fs_inv, kx, na, x);
         }
-        return dnu_combine(t, k, mnubykT, qc, nfl, ky, kc, na, ks);
+        return dnu_combine(t, k_over_m, qc, nfl, ky, kc, na, ks);
     }
 };
 

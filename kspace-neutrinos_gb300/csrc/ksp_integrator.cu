@@ -209,30 +209,8 @@ __global__ void k_scalars(IntegratorDev I, int Na, double a, double loga, double
         I.knot_h3[i] = h / 3.0;
         I.knot_ih3[i] = 1.0 / (3.0 * h);
     }
+    if (threadIdx.x < 32) call_scalars_warp(*I.B, a, loga, loga0, TimeTransfer, Na, *I.sc);
     if (threadIdx.x != 0) return;
-    const Background& B = *I.B;
-    StepScalars& S = *I.sc;
-    S.a = a;
-    S.loga = loga;
-    S.loga0 = loga0;
-    S.Na = Na;
-    S.OmegaNua3 = omega_nu_nopart(B, a) * (a * a * a);
-    S.OmegaNu1 = omega_nu(B, 1);
-    S.partnu = particle_nu_fraction(B, a, 0);
-    S.Omega_nu_tot = omega_nu_nopart(B, a);
-    for (int mi = 0; mi < kNuSpecies; mi++)
-        S.omeganu[mi] = B.deg[mi] > 0 ? B.deg[mi] * omega_nu_single(B, a, mi) : 0.0;
-    S.deriv_prefac = TimeTransfer * (hubble(B, TimeTransfer) / S.light) * TimeTransfer;
-    S.relerr = 1e-6;
-    S.partnu_now = particle_nu_fraction(B, a, 0);
-    S.skip_integral = 0;
-    if (S.partnu_now > 0) {
-        if (1 - S.partnu_now < 1e-3) S.skip_integral = 1;
-        S.relerr /= (1. + 1e-5 - S.partnu_now);
-    }
-    const double OmegaNu_nop = omega_nu_nopart(B, a);
-    const double omega_hybrid = omega_nu(B, a) - OmegaNu_nop;
-    S.kspace_prefac = OmegaNu_nop / (S.Omeganonu / (a * a * a) + omega_hybrid);
     const double* x = I.scalefact;
     if (Na > 2) {
         const int m = Na - 2;
@@ -367,31 +345,14 @@ __global__ void k_fs_coeffs(IntegratorDev I, int Nfs, double loga0, double loga)
 }
 
 // ------------------------------------------------------------------ history splines
-// Forward/back substitution of every history row against the shared factorisation.
-__global__ void k_dtot_coeffs(IntegratorDev I, int nk, int Na) {
-    const int ik = blockIdx.x * blockDim.x + threadIdx.x;
-    if (ik >= nk || Na <= 2) return;
-    const double* y = I.dtot + (size_t)ik * I.ld;
-    double* c = I.coef + (size_t)ik * I.ld;
-    const double* ih = I.knot_invh;
-    const int m = Na - 2;
-    double prev = 0;
-    for (int i = 0; i < m; i++) {
-        double r = 3.0 * ((y[i + 2] - y[i + 1]) * ih[i + 1] - (y[i + 1] - y[i]) * ih[i]);
-        if (i > 0) r -= I.knot_fac[i] * prev;
-        prev = r;
-        c[i + 1] = r;
-    }
-    c[0] = 0.0;
-    c[Na - 1] = 0.0;
-    double next = c[m] * I.knot_invdiag[m - 1];
-    c[m] = next;
-    const double* x = I.scalefact;
-    for (int i = m - 1; i-- > 0;) {
-        const double off = x[i + 2] - x[i + 1];
-        next = (c[i + 1] - off * next) * I.knot_invdiag[i];
-        c[i + 1] = next;
-    }
+// Forward/back substitution of every history row against the shared factorisation,
+// warp per row.
+__global__ void k_dtot_coeffs(IntegratorDev I, int nk, int Na, int staged) {
+    extern __shared__ __align__(16) double sdc[];
+    const int warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+    double* sy = staged ? sdc + (size_t)warp * 2 * I.ld : nullptr;
+    double* sc = staged ? sy + I.ld : nullptr;
+    for (int ik = blockIdx.x * nw + warp; ik < nk; ik += gridDim.x * nw) dtot_row_coeffs_warp(I, ik, Na, sy, sc);
 }
 
 // ------------------------------------------------------------------ node table
@@ -399,7 +360,7 @@ __global__ void k_dtot_coeffs(IntegratorDev I, int nk, int Na) {
 // kNcLevels levels of QAG's bisection of [log a0, log a]: thread per (slot, node).
 __global__ void k_nc_build(IntegratorDev I, int Na) {
     const int q = blockIdx.x * blockDim.x + threadIdx.x;
-    if (q >= kNcNodes) return;
+    if (q >= I.nc_slots * 61) return;
     const StepScalars& S = *I.sc;
     const int slot = q / 61, jn = q - 61 * slot;
     double lo, hi;
@@ -558,8 +519,18 @@ void launch_delta_nu_combined(const IntegratorDev& I, int nk, int Na, double a, 
         cudaMemsetAsync(&I.sc->fsl_A0a, 0, sizeof(double), st);
         cudaMemsetAsync(&I.sc->Nfs, 0, sizeof(int), st);
     }
-    if (Na > 2) k_dtot_coeffs<<<(nk + 127) / 128, 128, 0, st>>>(I, nk, Na);
-    if (loga > loga0 && Na > 1) k_nc_build<<<(kNcNodes + 127) / 128, 128, 0, st>>>(I, Na);
+    if (Na > 2) {
+        static bool dc_attr = false;
+        if (!dc_attr) {
+            cudaFuncSetAttribute(k_dtot_coeffs, cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024);
+            dc_attr = true;
+        }
+        const size_t smem = 4 * 2 * sizeof(double) * I.ld;
+        const int staged = smem <= 200 * 1024;
+        k_dtot_coeffs<<<(nk + 3) / 4, 128, staged ? smem : 0, st>>>(I, nk, Na, staged);
+    }
+    if (loga > loga0 && Na > 1 && I.nc_slots > 0)
+        k_nc_build<<<(I.nc_slots * 61 + 127) / 128, 128, 0, st>>>(I, Na);
     const int wpb = warps_per_block < 1 ? 1 : (warps_per_block > 4 ? 4 : warps_per_block);
     const size_t smem = dnu_qag_smem(I.ld, wpb);
     static bool attr_set = false;

@@ -46,6 +46,7 @@ struct IntegratorDev {
     double* nc_fsl;
     double* nc_dx;
     int* nc_j;
+    int nc_slots;                    // slots of the node table in use (2^levels - 1, 0 = none)
     double* fs_x;                    // [fs_cap]
     double* fs_y;                    // [fs_cap]
     double* fs_c;                    // [fs_cap]
@@ -64,18 +65,103 @@ struct IntegratorDev {
 };
 
 #ifdef __CUDACC__
+// The scalars of a call at a (as k_scalars, delta_tot_table.c:153-172,507-548,
+// interface_common.c:139-145), by one warp: the background evaluations, which are long
+// FP64 dependency chains, run on different lanes; lane 0 combines them.
+__device__ __forceinline__ void call_scalars_warp(const Background& B, double a, double loga, double loga0,
+                                                  double TT, int Na, StepScalars& S) {
+    const int lane = threadIdx.x & 31;
+    double v = 0.0;
+    if (lane == 0) v = omega_nu(B, a);
+    else if (lane == 1) v = omega_nu(B, 1);
+    else if (lane < 2 + kNuSpecies) v = B.deg[lane - 2] > 0 ? B.deg[lane - 2] * omega_nu_single(B, a, lane - 2) : 0.0;
+    else if (lane == 2 + kNuSpecies) v = hubble(B, TT);
+    const double om_a = __shfl_sync(0xffffffffu, v, 0);
+    const double om_1 = __shfl_sync(0xffffffffu, v, 1);
+    double om_s[kNuSpecies];
+    for (int mi = 0; mi < kNuSpecies; mi++) om_s[mi] = __shfl_sync(0xffffffffu, v, 2 + mi);
+    const double h_tt = __shfl_sync(0xffffffffu, v, 2 + kNuSpecies);
+    if (lane != 0) return;
+    const double partnu = particle_nu_fraction(B, a, 0);
+    const double nop = om_a - om_1 * partnu / (a * a * a);  // omega_nu_nopart (omega_nu_single.c:69-74)
+    S.a = a;
+    S.loga = loga;
+    S.loga0 = loga0;
+    S.Na = Na;
+    S.OmegaNua3 = nop * (a * a * a);
+    S.OmegaNu1 = om_1;
+    S.partnu = partnu;
+    S.Omega_nu_tot = nop;
+    for (int mi = 0; mi < kNuSpecies; mi++) S.omeganu[mi] = om_s[mi];
+    S.deriv_prefac = TT * (h_tt / S.light) * TT;
+    S.relerr = 1e-6;
+    S.partnu_now = partnu;
+    S.skip_integral = 0;
+    if (S.partnu_now > 0) {
+        if (1 - S.partnu_now < 1e-3) S.skip_integral = 1;
+        S.relerr /= (1. + 1e-5 - S.partnu_now);
+    }
+    S.kspace_prefac = nop / (S.Omeganonu / (a * a * a) + (om_a - nop));
+}
+
+// Natural-spline coefficients of one history row against the shared factorisation of
+// the knot system (knot_fac, knot_invdiag from k_scalars), by one warp: the row is
+// staged in shared memory with coalesced loads, lane 0 runs the forward and back
+// substitutions there, and the warp writes the coefficients back coalesced.
+// sy, sc: ld doubles of shared memory each, or null to work in global memory (rows
+// too long for shared memory).
+__device__ __forceinline__ void dtot_row_coeffs_warp(const IntegratorDev& I, int ik, int Na, double* sy,
+                                                     double* sc) {
+    const int lane = threadIdx.x & 31;
+    const double* y = I.dtot + (size_t)ik * I.ld;
+    double* c = I.coef + (size_t)ik * I.ld;
+    const bool staged = sy != nullptr;
+    if (staged) {
+        for (int k = lane; k < Na; k += 32) sy[k] = y[k];
+    } else {
+        sy = const_cast<double*>(y);
+        sc = c;
+    }
+    __syncwarp();
+    if (lane == 0) {
+        const double* ih = I.knot_invh;
+        const int m = Na - 2;
+        double prev = 0;
+        for (int k = 0; k < m; k++) {
+            double r = 3.0 * ((sy[k + 2] - sy[k + 1]) * ih[k + 1] - (sy[k + 1] - sy[k]) * ih[k]);
+            if (k > 0) r -= I.knot_fac[k] * prev;
+            prev = r;
+            sc[k + 1] = r;
+        }
+        sc[0] = 0.0;
+        sc[Na - 1] = 0.0;
+        double next = sc[m] * I.knot_invdiag[m - 1];
+        sc[m] = next;
+        const double* x = I.scalefact;
+        for (int k = m - 1; k-- > 0;) {
+            const double off = x[k + 2] - x[k + 1];
+            next = (sc[k + 1] - off * next) * I.knot_invdiag[k];
+            sc[k + 1] = next;
+        }
+    }
+    __syncwarp();
+    if (staged)
+        for (int k = lane; k < Na; k += 32) c[k] = sc[k];
+    __syncwarp();
+}
+
 // The delta_nu integrand of one (species, bin) with the instance's node table; knots,
 // row and rc may be staged copies (shared memory) of the instance's arrays.
 __device__ __forceinline__ DnuIntegrandC dnu_integrand(const IntegratorDev& I, const StepScalars& S, double k,
                                                        double mnubykT, double qc, const double* knots,
                                                        const double* row, const double* rc, int Na) {
     DnuIntegrandC f;
-    f.B = I.B; f.k = k; f.mnubykT = mnubykT; f.qc = qc; f.nfl = I.B->nufrac_low[0];
+    f.B = I.B; f.k_over_m = k / mnubykT; f.qc = qc; f.nfl = I.B->nufrac_low[0];
     f.fs_x = I.fs_x; f.fs_y = I.fs_y; f.fs_c = I.fs_c; f.nfs = S.Nfs; f.fs_x0 = S.loga0;
     f.fs_inv = (S.Nfs - 1.) / (S.loga - S.loga0);
     f.kx = knots; f.ky = row; f.kc = rc; f.na = Na;
     f.ks = KnotSeg{I.knot_invh, I.knot_h3, I.knot_ih3};
-    f.nc = NodeCache{I.nc_g, I.nc_fsl, I.nc_dx, I.nc_j};
+    f.nc = NodeCache{I.nc_g, I.nc_fsl, I.nc_dx, I.nc_j, I.nc_slots};
     return f;
 }
 #endif
