@@ -206,6 +206,20 @@ int kspace_gpu_batch_autotune(kspace_batch *batch, const double *a, const double
 /* device time (ms) of the last step's kernels */
 int kspace_gpu_batch_last_ms(kspace_batch *batch, float *ms);
 
+/* ---- allocation-free binning ----
+ * No counterpart in the reference.  The per-bin sums of total_powerspectrum's binning
+ * pass (powerspectrum.c:56-89) without a context and without allocating any memory,
+ * for hosts that cannot let a library allocate (a host that owns all device memory in
+ * its own pool, a PM code with no device memory to spare).  bin_sums[nrbins + 1] (host
+ * or device) receives sum w |F|^2 W^4 per bin, not normalised, and |F(0)|^2 last;
+ * divide by |F(0)|^2 and the mode counts for the power.  grid: device memory.  Limits:
+ * nrbins <= 4096, dims <= 4096 (KSPACE_ERR_ARG beyond).  Scratch is one fixed device
+ * array shared by all calls: overlapping calls race.  The first call on a device sets
+ * up the scratch address; make it before any stream capture.  cuda_stream: a
+ * cudaStream_t (NULL = the default stream); returns after the sums are in bin_sums. */
+int kspace_gpu_bin_power_noalloc(int dims, const void *grid, int nrbins, int startslab, int nslab,
+                                 double *bin_sums, void *cuda_stream);
+
 /* ---- diagnostics ---- */
 /* last call: nk, log k, ratio and norm of the correction (arrays of nk_alloc) */
 int kspace_gpu_last_correction(kspace_ctx *ctx, int *nk, double *logk, double *ratio, double *norm, double *dcdm,

@@ -78,6 +78,7 @@ _SIGS = {
     "kspace_gpu_batch_set_tuning": (_i, [_vp, _i, _i, _i]),
     "kspace_gpu_batch_autotune": (_i, [_vp, _PD, _vp, _i, _PI, C.POINTER(C.c_float)]),
     "kspace_gpu_batch_last_ms": (_i, [_vp, C.POINTER(C.c_float)]),
+    "kspace_gpu_bin_power_noalloc": (_i, [_i, _vp, _i, _i, _i, _vp, _vp]),
 }
 
 _lib = None
