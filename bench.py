@@ -237,10 +237,122 @@ def run_gb300(args, cfg):
     }
     if rank == 0 and not args.no_cpu_baseline:
         res["cpu_baseline"] = cpu_baseline(cfg, wl, args.cpu_threads, sample_steps=1)
+    if rank == 0 and world == 1 and not args.no_extras:
+        mx, tot = k.qag_stats()
+        res["integrator"] = {"qag_max_intervals": mx, "qag_total_intervals_last_step": tot}
+        res["fwd_adjoint"] = fwd_adjoint()
+        res["errors"] = errors_vs_oracle(cfg, wl, args.cpu_threads or os.cpu_count() or 1)
     k.close()
     if world > 1:
         dist.destroy_process_group()
     return res if rank == 0 else None
+
+
+def fwd_adjoint(steps=5, warmup=3):
+    """The differentiation workload (N=256, 128 bins, 128-row history, sum M_nu=0.15 eV):
+    device time of the plain step against the forward + adjoint step (store and
+    recompute variants), grid resident in HBM."""
+    import torch
+    import kspace_gpu as kg
+    cfg = dict(W.CONFIGS["cfg3_n256"])
+    N, nb, L = cfg["N"], cfg["nbins"], cfg["L"]
+    wl = setup_workload(cfg)
+    k = kg.make_instance(cfg["MNu"], 0.01, 0.7, 0.3, nb, time_max(cfg, 2 * (steps + warmup) + 4), wl["logk"],
+                         wl["T"], UnitLength_in_cm=W.UNIT_LENGTH_MPC)
+    k.set_nu_state(wl["sf"], wl["dt"])
+    grid = W.make_grid_torch(N, L, seed=3)
+    work = grid.clone()
+    a = cfg["a_end"] + 0.01
+    k.add_nu_power_to_rhogrid(a, L, work, N)  # initialisation + one committed row
+    nk = k.table_info()["nk"]
+
+    def timed(fn, n):
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        for _ in range(n):
+            fn()
+        torch.cuda.synchronize()
+        return (time.perf_counter() - t0) / n
+
+    state = {"a": a}
+
+    def plain():
+        state["a"] += 0.001
+        work.copy_(grid)
+        k.add_nu_power_to_rhogrid(state["a"], L, work, N)
+
+    out = torch.empty_like(grid)
+    pnu = torch.empty(nk, dtype=torch.float64, device="cuda")
+    gin = torch.empty_like(grid)
+    gbar = torch.randn(grid.shape, dtype=torch.complex64, device="cuda")
+    pbar = torch.rand(nk, dtype=torch.float64, device="cuda")
+    Dbar = torch.empty((nk, k.table_info()["ia"]), dtype=torch.float64, device="cuda")
+    ad = state["a"] + 0.005
+
+    def fa(recompute):
+        def run():
+            k.diff_forward(ad, L, grid, out, N, pnu, store_intervals=not recompute)
+            k.diff_backward(gbar, grid, pbar, gin, Dbar, recompute=recompute)
+        return run
+
+    def copy_only():
+        work.copy_(grid)
+
+    for f in (plain, fa(False), fa(True)):
+        for _ in range(warmup):
+            f()
+    t_copy = timed(copy_only, steps)
+    t_plain = timed(plain, steps) - t_copy
+    t_store = timed(fa(False), steps)
+    t_rec = timed(fa(True), steps)
+    k.close()
+    return {"workload": "cfg3_n256 (N=256, 128 bins, 128-row history, sum M_nu=0.15 eV)",
+            "plain_ms": 1e3 * t_plain, "fwd_adj_store_ms": 1e3 * t_store, "fwd_adj_recompute_ms": 1e3 * t_rec,
+            "ratio_store": t_store / t_plain, "ratio_recompute": t_rec / t_plain,
+            "timing": "host clock around synchronous calls, %d steps after %d warm-up" % (steps, warmup)}
+
+
+def errors_vs_oracle(cfg, wl, threads):
+    """One step on a fresh instance and the oracle (the reference algorithm in C), and on
+    the all-FP64 oracle (double |F|^2 and window, exact delta_nu integral): max relative
+    differences of P(k), delta_nu/delta_cdm and the corrected grid."""
+    import torch
+    import kspace_gpu as kg
+    sys.path.insert(0, os.path.join(ROOT, "tests"))
+    from oracle_lib import Oracle
+    O = Oracle()
+    N, nb, L = cfg["N"], cfg["nbins"], cfg["L"]
+    TimeMax = time_max(cfg, 4)
+    a = cfg["a_end"] + 0.01
+    g = W.make_grid(N, L, seed=1)
+    k = kg.make_instance(cfg["MNu"], 0.01, 0.7, 0.3, nb, TimeMax, wl["logk"], wl["T"],
+                         UnitLength_in_cm=W.UNIT_LENGTH_MPC)
+    k.set_nu_state(wl["sf"], wl["dt"])
+    gd = torch.as_tensor(g).cuda()
+    k.add_nu_power_to_rhogrid(a, L, gd, N)
+    lc = k.last_correction()
+    gg = gd.cpu().numpy()
+    k.close()
+    res = {}
+    for name, exact in (("vs_reference_oracle", 0), ("vs_fp64_oracle", 1)):
+        bg = O.bg(cfg["MNu"], a0=0.01, h=0.7, Omega0=0.3, UnitTime_in_s=W.UNIT_TIME)
+        s = O.state(bg, nb, 0.01, TimeMax, Omega0=0.3, UnitTime_in_s=W.UNIT_TIME, UnitLength_in_cm=W.UNIT_LENGTH_MPC)
+        O.set_transfer(s, wl["logk"], wl["T"])
+        assert O.set_nu_state(s, wl["sf"], wl["dt"]) == 0
+        O.L.ko_state_options(s, 0, exact)
+        if exact:
+            st, out, go = O.add_nu_power_to_rhogrid_fp64(s, a, L, g, N, nthreads=threads, nk_alloc=nb)
+        else:
+            go = g.copy()
+            st, out = O.add_nu_power_to_rhogrid(s, a, L, go, N, nthreads=threads, nk_alloc=nb)
+        assert st == 0, st
+        m = out["ratio"] != 0
+        res[name] = {
+            "P_k": float(np.max(np.abs((lc["dcdm"] / out["dcdm"]) ** 2 - 1))),
+            "delta_nu_over_delta_cdm": float(np.max(np.abs(lc["ratio"][m] / out["ratio"][m] - 1))),
+            "corrected_grid": float(np.max(np.abs(gg - go) / np.maximum(np.abs(go), 1e-30))),
+        }
+    return res
 
 
 def cpu_baseline(cfg, wl, threads, sample_steps=1):
@@ -465,6 +577,7 @@ def main():
     ap.add_argument("--autotune", type=int, default=1)
     ap.add_argument("--cpu-threads", type=int, default=0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-extras", action="store_true", help="skip the fwd+adjoint and error measurements")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3

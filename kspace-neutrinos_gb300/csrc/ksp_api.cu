@@ -89,6 +89,7 @@ extern "C" int kspace_gpu_create(kspace_ctx** out, int device) {
     if (const char* e = getenv("KSPACE_GPU_ROWS")) c->rows = atoi(e);
     if (const char* e = getenv("KSPACE_GPU_STAGES")) c->stages = atoi(e);
     if (const char* e = getenv("KSPACE_GPU_QAG_WARPS")) c->qag_warps = atoi(e);
+    if (const char* e = getenv("KSPACE_GPU_QAG_SPLIT")) c->qag_split = atoi(e);
     if (const char* e = getenv("KSPACE_GPU_NC_LEVELS")) {
         const int l = atoi(e);
         c->nc_levels = l < 0 ? 0 : (l > kNcMaxLevels ? kNcMaxLevels : l);
@@ -631,7 +632,7 @@ static int delta_tot_init(kspace_ctx* c, int nk_in, const double* keff_d, const 
     // delta_nu_last = delta_nu at the last stored time (delta_tot_table.c:146)
     const double a_last = exp(c->h_scalefact[c->ia - 1]);
     launch_delta_nu_combined(c->I, c->nk, c->ia, a_last, c->h_scalefact[c->ia - 1], c->loga0, c->TimeTransfer,
-                             0, c->nspec, c->spec_ids, c->qag_warps, c->stream);
+                             0, c->nspec, c->spec_ids, c->qag_warps, c->stream, c->qag_split);
     g_launches += 8;
     CK(cudaMemcpyAsync(c->I.nu_last, c->I.dnu, sizeof(double) * c->nk, cudaMemcpyDeviceToDevice, c->stream));
     c->fact_valid = 0;
@@ -679,7 +680,7 @@ static int update_device(kspace_ctx* c, double a, int nk_in, const double* keff_
     c->ia++;
     const int Na = c->ia;
     launch_delta_nu_combined(I, c->nk, Na, a, loga, c->loga0, c->TimeTransfer, c->fact_valid, c->nspec, c->spec_ids,
-                             c->qag_warps, c->stream);
+                             c->qag_warps, c->stream, c->qag_split);
     // keep the row if far enough from the previous one (delta_tot_table.c:229-237)
     const bool commit = a >= exp(c->h_scalefact[Na - 2]) + 0.009;
     launch_finish_update(I, c->nk, commit ? Na - 1 : -1, a, loga, want_corr ? keff_d : nullptr, dnu_out_d,
@@ -1171,7 +1172,7 @@ extern "C" int kspace_gpu_diff_forward(kspace_ctx* c, double Time, double BoxSiz
     CK(cudaMemsetAsync(I.qag_max, 0, sizeof(int), c->stream));
     CK(cudaMemsetAsync(I.qag_total, 0, sizeof(long long), c->stream));
     launch_delta_nu_combined(Is, c->nk, Na, Time, loga, c->loga0, c->TimeTransfer, start, c->nspec, c->spec_ids,
-                             c->qag_warps, c->stream);
+                             c->qag_warps, c->stream, c->qag_split);
     c->fact_valid = start;
     launch_finish_update(I, c->nk, -3, Time, loga, c->keff_d, c->dnu_out_d, c->logk_d, c->ratio_d, c->corr,
                          c->norm_d, c->stream);

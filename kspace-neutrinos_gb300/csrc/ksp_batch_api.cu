@@ -49,7 +49,7 @@ struct kspace_batch {
     int total_bins = 0, ldmax = 0;
     // tuning
     int wpb = 4, blocks_per_sm = 2, use_graph = 1;
-    int nc_slots = 15;  // node-table slots per instance (4 levels)
+    int nc_slots = 63;  // node-table slots per instance (6 levels)
     bool eager_done = false;
     cudaGraph_t graph = nullptr;
     cudaGraphExec_t exec = nullptr;

@@ -564,6 +564,167 @@ __device__ QagResult qag_warp_c(const F& f, const Gk61Nodes& N, QagList& L, doub
     return R;
 }
 
+// ------------------------------------------------------------------ block-cooperative QAG
+// The same rule and decisions with the node evaluations spread over the warps of a block
+// (blockDim.x = 32 * W, W = 2 or 4): thread t evaluates slot t, t + 32W, ...; warp 0
+// then forms every lane's partial sums over the slots lane + 32m in the order m = 0..3
+// and reduces them with the butterfly of gk61_warp_c, so the results are bit for bit
+// those of qag_warp_c.  Shared scratch: QagBlockSmem.
+struct QagBlockSmem {
+    double fv[128];
+    GkOut out[2];
+    double a[2], b[2];
+    int slot[2];
+};
+
+template <class F>
+__device__ __forceinline__ void gk61_block_c(const F& f, const Gk61Nodes& N, int nint, const double* a,
+                                             const double* b, const int* slot, GkOut* out, QagBlockSmem& sh) {
+    const int tid = threadIdx.x, lane = tid & 31;
+    double c[2], h[2];
+    for (int t = 0; t < 2; t++) {
+        c[t] = __dmul_rn(0.5, __dadd_rn(a[t], b[t]));
+        h[t] = __dmul_rn(0.5, __dsub_rn(b[t], a[t]));
+    }
+    const int nslots = 61 * nint;
+    for (int s = tid; s < nslots; s += blockDim.x) {
+        const int t = s >= 61 ? 1 : 0;
+        const int j = s - 61 * t;
+        const double x = __dadd_rn(c[t], __dmul_rn(h[t], N.x[j]));
+        sh.fv[s] = f.node(slot[t], j, x);
+    }
+    __syncthreads();
+    if (tid < 32) {
+        double fv[4];
+        double rk[2] = {0, 0}, rg[2] = {0, 0}, ra[2] = {0, 0};
+#pragma unroll
+        for (int m = 0; m < 4; m++) {
+            const int s = lane + 32 * m;
+            fv[m] = 0.0;
+            if (s < nslots) {
+                const int t = s >= 61 ? 1 : 0;
+                const int j = s - 61 * t;
+                const double v = sh.fv[s];
+                fv[m] = v;
+                if (t == 0) { rk[0] += N.wk[j] * v; rg[0] += N.wg[j] * v; ra[0] += N.wk[j] * fabs(v); }
+                else { rk[1] += N.wk[j] * v; rg[1] += N.wg[j] * v; ra[1] += N.wk[j] * fabs(v); }
+            }
+        }
+        double mean[2];
+        for (int t = 0; t < nint; t++) {
+            rk[t] = bcast0(warp_sum_to0(rk[t]));
+            rg[t] = bcast0(warp_sum_to0(rg[t]));
+            ra[t] = bcast0(warp_sum_to0(ra[t]));
+            mean[t] = 0.5 * rk[t];
+        }
+        double rs[2] = {0, 0};
+#pragma unroll
+        for (int m = 0; m < 4; m++) {
+            const int s = lane + 32 * m;
+            if (s < nslots) {
+                const int t = s >= 61 ? 1 : 0;
+                const int j = s - 61 * t;
+                const double d = N.wk[j] * fabs(fv[m] - mean[t]);
+                if (t == 0) rs[0] += d; else rs[1] += d;
+            }
+        }
+        for (int t = 0; t < nint; t++) {
+            rs[t] = bcast0(warp_sum_to0(rs[t]));
+            if (lane == 0) {
+                const double err = (rk[t] - rg[t]) * h[t];
+                GkOut o;
+                o.result = rk[t] * h[t];
+                o.resabs = ra[t] * fabs(h[t]);
+                o.resasc = rs[t] * fabs(h[t]);
+                o.abserr = rescale_error(err, o.resabs, o.resasc);
+                sh.out[t] = o;
+            }
+        }
+    }
+    __syncthreads();
+    for (int t = 0; t < nint; t++) out[t] = sh.out[t];
+}
+
+// qag_warp_c run by a whole block: every thread follows the same decisions (they read the
+// same shared list); thread 0 writes the list.
+template <class F>
+__device__ QagResult qag_block_c(const F& f, const Gk61Nodes& N, QagList& L, double a, double b, double epsabs,
+                                 double epsrel, int limit, QagBlockSmem& sh) {
+    const int tid = threadIdx.x, lane = tid & 31;
+    QagResult R;
+    GkOut g[2];
+    double aa[2] = {a, a}, bb[2] = {b, b};
+    int ss[2] = {f.nc.nslots > 0 ? 0 : -1, -1};
+    gk61_block_c(f, N, 1, aa, bb, ss, g, sh);
+    if (tid == 0) { L.a[0] = a; L.b[0] = b; L.r[0] = g[0].result; L.e[0] = g[0].abserr; L.slot[0] = ss[0]; }
+    __syncthreads();
+    double tol = fmax(epsabs, epsrel * fabs(g[0].result));
+    const double round_off = 50 * DBL_EPSILON * g[0].resabs;
+    R.nint = 1;
+    R.result = g[0].result;
+    R.abserr = g[0].abserr;
+    if (g[0].abserr <= round_off && g[0].abserr > tol) { R.ok = 0; return R; }
+    if ((g[0].abserr <= tol && g[0].abserr != g[0].resasc) || g[0].abserr == 0.0) { R.ok = 1; return R; }
+    if (limit == 1) { R.ok = 0; return R; }
+    double area = g[0].result, errsum = g[0].abserr;
+    int n = 1, roundoff1 = 0, roundoff2 = 0, error_type = 0;
+    do {
+        // every warp computes the same argmax (lowest index on ties)
+        double best = -1.0;
+        int bk = 0x7fffffff;
+        for (int i = lane; i < n; i += 32) {
+            const double e = L.e[i];
+            if (e > best) { best = e; bk = i; }
+        }
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) {
+            const double ob = __shfl_down_sync(0xffffffffu, best, o);
+            const int ok = __shfl_down_sync(0xffffffffu, bk, o);
+            if (ob > best || (ob == best && ok < bk)) { best = ob; bk = ok; }
+        }
+        const int k = __shfl_sync(0xffffffffu, bk, 0);
+        const double a_i = L.a[k], b_i = L.b[k], r_i = L.r[k], e_i = L.e[k];
+        const int s_i = L.slot[k];
+        const double a1 = a_i, b1 = 0.5 * (a_i + b_i), a2 = b1, b2 = b_i;
+        aa[0] = a1; bb[0] = b1; aa[1] = a2; bb[1] = b2;
+        ss[0] = nc_child(s_i, 0, f.nc.nslots);
+        ss[1] = nc_child(s_i, 1, f.nc.nslots);
+        gk61_block_c(f, N, 2, aa, bb, ss, g, sh);
+        const double area12 = g[0].result + g[1].result, error12 = g[0].abserr + g[1].abserr;
+        errsum += error12 - e_i;
+        area += area12 - r_i;
+        if (g[0].resasc != g[0].abserr && g[1].resasc != g[1].abserr) {
+            if (fabs(r_i - area12) <= 1.0e-5 * fabs(area12) && error12 >= 0.99 * e_i) roundoff1++;
+            if (n >= 10 && error12 > e_i) roundoff2++;
+        }
+        tol = fmax(epsabs, epsrel * fabs(area));
+        if (errsum > tol) {
+            if (roundoff1 >= 6 || roundoff2 >= 20) error_type = 2;
+            const double tiny = (1 + 100 * DBL_EPSILON) * (fabs(a2) + 1000 * DBL_MIN);
+            if (fabs(a1) <= tiny && fabs(b2) <= tiny) error_type = 3;
+        }
+        if (tid == 0) {
+            L.b[k] = b1; L.r[k] = g[0].result; L.e[k] = g[0].abserr; L.slot[k] = ss[0];
+            L.a[n] = a2; L.b[n] = b2; L.r[n] = g[1].result; L.e[n] = g[1].abserr; L.slot[n] = ss[1];
+        }
+        __syncthreads();
+        n++;
+    } while (n < limit && !error_type && errsum > tol);
+    double sum = 0;
+    if (lane == 0)
+        for (int i = 0; i < n; i++) sum += L.r[i];
+    R.result = bcast0(sum);
+    R.abserr = errsum;
+    R.nint = n;
+    R.ok = errsum <= tol;
+    __syncthreads();
+    return R;
+}
+
+}  // namespace ksp
+#include "ksp_jfit.cuh"
+namespace ksp {
+
 // ------------------------------------------------------------------ delta_nu integrand
 // delta_tot_table.c:492-500: fslength(x, log a) / (a H(a)) J(k fslength / (m/kT))
 // delta_tot(k, x) at x = log a_i.  Split into the part that depends only on x (and the
@@ -625,7 +786,7 @@ __device__ __forceinline__ double dnu_combine(const NodeTerms& t, double k_over_
     } else {
         S = y0 + t.dx * ((y1 - y0) * __ldg(ks.ih + j));
     }
-    const double J = specialJ(t.fsl * k_over_m, qc, nfl);
+    const double J = specialJ_tab(t.fsl * k_over_m, qc, nfl);
     return t.g * J * S;
 }
 

@@ -66,12 +66,12 @@ __device__ __forceinline__ void fence_async_smem() { asm volatile("fence.proxy.a
 struct SmemPlan {
     size_t stages_off, hist_off, thr_off, tab_off, bar_off, total;
 };
-__host__ __device__ inline SmemPlan plan_smem(int rows, int stages, int nrbins, int ntab_floats) {
+__host__ __device__ inline SmemPlan plan_smem(int rows, int stages, int nrbins, int ntab_floats, int hist_copies = 1) {
     SmemPlan p;
     p.stages_off = 0;  // aligned to 1024 at run time (slack included)
     size_t o = (size_t)stages * rows * 128 + 1024;
     p.hist_off = o;
-    o += sizeof(double) * (size_t)nrbins;
+    o += sizeof(double) * (size_t)nrbins * hist_copies;
     p.thr_off = o;
     o += sizeof(int) * (size_t)(nrbins + 1);
     o = (o + 15) & ~size_t(15);
@@ -87,31 +87,37 @@ __host__ __device__ inline SmemPlan plan_smem(int rows, int stages, int nrbins, 
 // ------------------------------------------------------------------ K1 (TMA)
 // Persistent CTAs stream 128-byte rows (16 modes) through a STAGES-deep TMA ring;
 // 16/MPT threads per row, MPT consecutive modes each.  A thread sums its modes into two
-// adjacent bins as float pairs (BinPairAcc) and hands them to the CTA's float-pair bin
-// totals by FP32 atomics; each CTA adds its totals to the global FP64 sums once.
+// adjacent bins as float pairs (BinPairAcc2) and hands them, at the end of its modes, to
+// its warp's own float-pair bin totals by FP32 atomics (no other warp writes them); each
+// CTA adds its warps' totals to the global FP64 sums once.
 template <int ROWS, int STAGES, int MPT>
 __global__ void __launch_bounds__(ROWS * (16 / MPT), 1024 / (ROWS * (16 / MPT)))
 k_bin_power_tma(const __grid_constant__ CUtensorMap tmap, GridArgs g, const int* __restrict__ thresh,
                 const float* __restrict__ w1g, const float* __restrict__ grid, double* bin_sum, double* F0sq,
                 unsigned* status, int ntiles) {
-    constexpr int TPR = 16 / MPT, NT = ROWS * TPR;
+    constexpr int TPR = 16 / MPT, NT = ROWS * TPR, NW = NT / 32;
     extern __shared__ unsigned char sm_raw[];
     __shared__ int s_abort;
     __shared__ long long s_rowbase;
     __shared__ int s_zbase;
-    const SmemPlan P = plan_smem(ROWS, STAGES, g.nrbins, g.nz);
+    const SmemPlan P = plan_smem(ROWS, STAGES, g.nrbins, 2 * g.nz, NW);
     const uint32_t base_u = smem_addr(sm_raw);
     unsigned char* stage0 = sm_raw + ((1024 - (base_u & 1023)) & 1023);
-    float* s_H = reinterpret_cast<float*>(sm_raw + P.hist_off);  // nrbins high parts
-    float* s_L = s_H + g.nrbins;                                    // nrbins low parts
+    float* s_hist = reinterpret_cast<float*>(sm_raw + P.hist_off);  // per warp: nrbins high, nrbins low parts
     int* s_thr = reinterpret_cast<int*>(sm_raw + P.thr_off);
     float* s_w1 = reinterpret_cast<float*>(sm_raw + P.tab_off);
+    float* s_wt = s_w1 + g.nz;  // k_z weights
     uint64_t* bars = reinterpret_cast<uint64_t*>(sm_raw + P.bar_off);
     const int tid = threadIdx.x;
     const int r = tid / TPR, q = tid - r * TPR;
-    for (int i = tid; i < g.nrbins; i += NT) { s_H[i] = 0.f; s_L[i] = 0.f; }
+    float* s_H = s_hist + (size_t)(tid >> 5) * 2 * g.nrbins;  // this warp's totals
+    float* s_L = s_H + g.nrbins;
+    for (int i = tid; i < 2 * NW * g.nrbins; i += NT) s_hist[i] = 0.f;
     for (int i = tid; i <= g.nrbins; i += NT) s_thr[i] = thresh[i];
-    for (int i = tid; i < g.nz; i += NT) s_w1[i] = w1g[i];
+    for (int i = tid; i < g.nz; i += NT) {
+        s_w1[i] = w1g[i];
+        s_wt[i] = (i == 0 || i == g.half) ? 1.f : 2.f;
+    }
     if (tid == 0) {
         s_abort = 0;
         for (int st = 0; st < STAGES; st++) mbar_init_(&bars[st], 1);
@@ -126,7 +132,7 @@ k_bin_power_tma(const __grid_constant__ CUtensorMap tmap, GridArgs g, const int*
             tma_load_2d(stage0 + (size_t)k * ROWS * 128, &tmap, &bars[k], 0, tile * ROWS);
         }
     }
-    BinPairAcc acc;
+    BinPairAcc2 acc;
     int k = 0;
     for (; k < my_n; k++) {
         const int st = k % STAGES;
@@ -149,12 +155,12 @@ k_bin_power_tma(const __grid_constant__ CUtensorMap tmap, GridArgs g, const int*
                 const float4 v = *reinterpret_cast<const float4*>(rp + ((u ^ (r & 7)) << 4));
                 {
                     const int k2 = c.kxy2 + c.z * c.z;
-                    if (k2 != 0) acc.add(k2, mode_power2(v.x, v.y, c, s_w1, g.half), g, s_thr, s_H, s_L);
+                    if (k2 != 0) acc.add(k2, mode_power2w(v.x, v.y, c, s_w1, s_wt), g, s_thr, s_H, s_L);
                     c.next(g, s_w1);
                 }
                 {
                     const int k2 = c.kxy2 + c.z * c.z;
-                    if (k2 != 0) acc.add(k2, mode_power2(v.z, v.w, c, s_w1, g.half), g, s_thr, s_H, s_L);
+                    if (k2 != 0) acc.add(k2, mode_power2w(v.z, v.w, c, s_w1, s_wt), g, s_thr, s_H, s_L);
                     c.next(g, s_w1);
                 }
             }
@@ -198,7 +204,9 @@ k_bin_power_tma(const __grid_constant__ CUtensorMap tmap, GridArgs g, const int*
     }
     __syncthreads();
     for (int i = tid; i < g.nrbins; i += NT) {
-        const double v = (double)s_H[i] + (double)s_L[i];
+        double v = 0.0;
+        for (int w = 0; w < NW; w++)
+            v += (double)s_hist[(size_t)w * 2 * g.nrbins + i] + (double)s_hist[(size_t)w * 2 * g.nrbins + g.nrbins + i];
         if (v != 0.0) atomicAdd(bin_sum + i, v);
     }
 }
@@ -495,7 +503,7 @@ static int run_bin_tma(const GridGeom& g, const GridArgs& a, const float* grid, 
     constexpr int NT = ROWS * (16 / MPT);
     CUtensorMap map;
     if (!make_map(&map, grid, a.nrows16, ROWS)) return -1;
-    const SmemPlan P = plan_smem(ROWS, STAGES, g.nrbins, a.nz);
+    const SmemPlan P = plan_smem(ROWS, STAGES, g.nrbins, 2 * a.nz, NT / 32);
     if (P.total > 220 * 1024) return -1;
     auto kern = k_bin_power_tma<ROWS, STAGES, MPT>;
     cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)P.total);

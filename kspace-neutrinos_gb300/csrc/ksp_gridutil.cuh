@@ -119,6 +119,20 @@ __device__ __forceinline__ ModeP mode_power2(float re, float im, const ModeCurso
     if (c.z != 0 && c.z != half) { p.hi = p.hi + p.hi; p.lo = p.lo + p.lo; }
     return p;
 }
+// mode_power2 with the k_z weight taken from a table (1 on the z = 0 and N/2 planes, 2
+// elsewhere): multiplying |F|^2 by it is exact, so the pair equals mode_power2's.
+__device__ __forceinline__ ModeP mode_power2w(float re, float im, const ModeCursor& c, const float* w1,
+                                              const float* wt) {
+    const float t = __fmul_rn(c.iwxy, w1[c.z]);
+    const float inv = __fmul_rn(t, t);
+    const float f_hi = __fmul_rn(inv, inv);
+    const float f_lo = fmaf(inv, inv, -f_hi);
+    const float F2 = __fmul_rn(__fadd_rn(__fmul_rn(re, re), __fmul_rn(im, im)), wt[c.z]);
+    ModeP p;
+    p.hi = __fmul_rn(F2, f_hi);
+    p.lo = __fadd_rn(fmaf(F2, f_hi, -p.hi), __fmul_rn(F2, f_lo));
+    return p;
+}
 // the same value in double (plain and tail paths)
 __device__ __forceinline__ double mode_power_d(float re, float im, const ModeCursor& c, const float* w1, int half) {
     const float t = __fmul_rn(c.iwxy, w1[c.z]);
@@ -195,35 +209,103 @@ struct RunAcc32 {
     }
 };
 
-// Two adjacent bins b, b+1 accumulated as float pairs: a mode costs two compares and a
-// select unless it leaves [thr[b], thr[b+2]), where both pairs go to the CTA totals and
-// the window restarts at the mode's bin.  At the end of a thread's modes the pairs are
-// flushed by all threads together.
-struct BinPairAcc {
-    int b = -1, tlo = 1, thi2 = 0, thi = 0;
-    float ha = 0.f, la = 0.f, hb = 0.f, lb = 0.f;
+// (h, l) += (oh, ol) for float pairs: TwoSum of the high parts, the low parts and the
+// error carried in the low part, then renormalised.
+__device__ __forceinline__ void pair_add(float& h, float& l, float oh, float ol) {
+    const float s = __fadd_rn(h, oh);
+    const float bb = __fsub_rn(s, h);
+    const float e = __fadd_rn(__fsub_rn(h, __fsub_rn(s, bb)), __fsub_rn(oh, bb));
+    const float t = __fadd_rn(e, __fadd_rn(l, ol));
+    h = __fadd_rn(s, t);
+    l = __fsub_rn(t, __fsub_rn(h, s));
+}
+
+// Warp-wide flush of one float pair per lane into the CTA totals: lanes are consecutive
+// stretches of the grid, so equal bins sit in runs of neighbouring lanes; a segmented
+// scan (TwoSum pairs) leaves each run's total on its last lane, which alone touches the
+// shared totals.  key < 0: nothing to add.  Called by all 32 lanes together.
+__device__ __forceinline__ void warp_flush_pairs(int key, float h, float l, float* H, float* L) {
+    const int lane = threadIdx.x & 31;
+    const int up = __shfl_up_sync(0xffffffffu, key, 1);
+    const bool head = lane == 0 || up != key;
+    const unsigned heads = __ballot_sync(0xffffffffu, head);
+    const int my_head = 31 - __clz(heads & (0xffffffffu >> (31 - lane)));
+#pragma unroll
+    for (int d = 1; d < 32; d <<= 1) {
+        const float oh = __shfl_up_sync(0xffffffffu, h, d);
+        const float ol = __shfl_up_sync(0xffffffffu, l, d);
+        if (lane - d >= my_head) pair_add(h, l, oh, ol);
+    }
+    const bool tail = lane == 31 || ((heads >> (lane + 1)) & 1u);
+    if (tail && key >= 0 && (h != 0.f || l != 0.f)) pair_atomic_add(H, L, key, h, l);
+}
+
+// Two adjacent bins b, b+1 as float pairs (h: the exact float sum of the high parts,
+// l: the sum of their TwoSum errors and of the low parts).  A mode outside
+// [thr[b], thr[b+2]) -- in practice a thread's first mode of a row -- sends the pairs to
+// the warp's own bin totals and restarts the window at the mode's bin.
+struct BinPairAcc2 {
+    int b = -1, tlo = 1, t1 = 0, t2 = 0;
+    float h0 = 0.f, l0 = 0.f, h1 = 0.f, l1 = 0.f;
     __device__ __forceinline__ void flush(float* H, float* L) {
-        if (ha != 0.f || la != 0.f) pair_atomic_add(H, L, b, ha, la);
-        if (hb != 0.f || lb != 0.f) pair_atomic_add(H, L, b + 1, hb, lb);
-        ha = la = hb = lb = 0.f;
+        if (h0 != 0.f || l0 != 0.f) pair_atomic_add(H, L, b, h0, l0);
+        if (h1 != 0.f || l1 != 0.f) pair_atomic_add(H, L, b + 1, h1, l1);
+        h0 = l0 = h1 = l1 = 0.f;
     }
     __device__ __forceinline__ void add(int k2, ModeP p, const GridArgs& g, const int* thr, float* H, float* L) {
-        if (k2 < tlo || k2 >= thi2) {
+        if (k2 < tlo || k2 >= t2) {
             flush(H, L);
             b = bin_of(k2, g.c1, thr, g.nrbins);
             tlo = thr[b];
-            thi = thr[b + 1];
-            thi2 = b + 2 <= g.nrbins ? thr[b + 2] : 0x7fffffff;
+            t1 = thr[b + 1];
+            t2 = b + 2 <= g.nrbins ? thr[b + 2] : 0x7fffffff;
         }
-        const bool up = k2 >= thi;
-        float h = up ? hb : ha, l = up ? lb : la;
+        const bool up = k2 >= t1;
+        const float h = up ? h1 : h0;
         const float s = __fadd_rn(h, p.hi);
         const float bb = __fsub_rn(s, h);
         const float e = __fadd_rn(__fsub_rn(h, __fsub_rn(s, bb)), __fsub_rn(p.hi, bb));
-        const float t = __fadd_rn(e, __fadd_rn(l, p.lo));
-        h = __fadd_rn(s, t);
-        l = __fsub_rn(t, __fsub_rn(h, s));
-        if (up) { hb = h; lb = l; } else { ha = h; la = l; }
+        const float l = __fadd_rn(up ? l1 : l0, __fadd_rn(e, p.lo));
+        if (up) { h1 = s; l1 = l; } else { h0 = s; l0 = l; }
+    }
+};
+
+// Three adjacent bins b, b+1, b+2 accumulated as float pairs: a mode costs three
+// compares and a few selects unless it leaves [thr[b], thr[b+3]) -- in practice only at
+// a thread's first mode of a row, where the window restarts at the mode's bin (a row
+// of 8 modes spans more than three bins rarely: k^2 grows slowly along z).  The pairs
+// go to the CTA totals at the end of the row, by all lanes together (flush_warp).
+struct BinWinAcc {
+    int b = -1, tlo = 1, t1 = 0, t2 = 0, t3 = 0;
+    float h0 = 0.f, l0 = 0.f, h1 = 0.f, l1 = 0.f, h2 = 0.f, l2 = 0.f;
+    // single-thread flush (the rare window restarts inside a row)
+    __device__ __forceinline__ void flush(float* H, float* L) {
+        if (h0 != 0.f || l0 != 0.f) pair_atomic_add(H, L, b, h0, l0);
+        if (h1 != 0.f || l1 != 0.f) pair_atomic_add(H, L, b + 1, h1, l1);
+        if (h2 != 0.f || l2 != 0.f) pair_atomic_add(H, L, b + 2, h2, l2);
+        h0 = l0 = h1 = l1 = h2 = l2 = 0.f;
+    }
+    // end of a row: all lanes of the warp
+    __device__ __forceinline__ void flush_warp(float* H, float* L) {
+        warp_flush_pairs(b >= 0 ? b : -1, h0, l0, H, L);
+        warp_flush_pairs(b >= 0 ? b + 1 : -1, h1, l1, H, L);
+        warp_flush_pairs(b >= 0 ? b + 2 : -1, h2, l2, H, L);
+        h0 = l0 = h1 = l1 = h2 = l2 = 0.f;
+    }
+    __device__ __forceinline__ void add(int k2, ModeP p, const GridArgs& g, const int* thr, float* H, float* L) {
+        if (k2 < tlo || k2 >= t3) {
+            flush(H, L);
+            b = bin_of(k2, g.c1, thr, g.nrbins);
+            tlo = thr[b];
+            t1 = thr[b + 1];
+            t2 = b + 2 <= g.nrbins ? thr[b + 2] : 0x7fffffff;
+            t3 = b + 3 <= g.nrbins ? thr[b + 3] : 0x7fffffff;
+        }
+        const bool u1 = k2 >= t1, u2 = k2 >= t2;
+        float h = u2 ? h2 : (u1 ? h1 : h0);
+        float l = u2 ? l2 : (u1 ? l1 : l0);
+        pair_add(h, l, p.hi, p.lo);
+        if (u2) { h2 = h; l2 = l; } else if (u1) { h1 = h; l1 = l; } else { h0 = h; l0 = l; }
     }
 };
 
@@ -274,29 +356,38 @@ struct CorrRun {
 // segments [xf[j], xf[j+1]) of the table, constant below xf[0] and from xf[nk-1] on.
 // A thread keeps its current segment and moves it only when x leaves [xlo, xhi).
 struct SegTrack {
+    int j = -2;  // segment index: -1 below the table, nk-1 from the last node on
     float xlo = 3.0e38f, xhi = -3.0e38f, x0 = 0.f, sl = 0.f, r0 = 0.f, xwarn = -3.0e38f;
+    __device__ __forceinline__ void set(int jj, const CorrSmem& t, int nk) {
+        j = jj;
+        xwarn = -3.0e38f;
+        if (jj < 0) {  // below the first node: constant
+            xlo = -3.0e38f; xhi = t.xf[0]; x0 = 0.f; sl = 0.f; r0 = t.rn[0];
+            xwarn = t.xf[0] - 0.69314718f;
+        } else if (jj >= nk - 1) {  // from the last node on: constant
+            xlo = t.xf[nk - 1]; xhi = 3.0e38f; x0 = 0.f; sl = 0.f; r0 = t.rn[nk - 1];
+        } else {
+            xlo = t.xf[jj]; xhi = t.xf[jj + 1]; x0 = xlo; sl = t.sn[jj]; r0 = t.rn[jj];
+        }
+    }
     __device__ __forceinline__ void locate(float x, const CorrSmem& t, int nk) {
-        // largest j with xf[j] <= x (j = -1 below the table)
-        int lo = -1, hi = nk;
+        int lo = -1, hi = nk;  // largest j with xf[j] <= x
         while (hi - lo > 1) {
             const int mid = (lo + hi) >> 1;
             if (t.xf[mid] <= x) lo = mid; else hi = mid;
         }
-        xwarn = -3.0e38f;
-        if (lo < 0) {  // below the first node: constant
-            xlo = -3.0e38f; xhi = t.xf[0]; x0 = 0.f; sl = 0.f; r0 = t.rn[0];
-            xwarn = t.xf[0] - 0.69314718f;
-        } else if (lo >= nk - 1) {  // from the last node on: constant
-            xlo = t.xf[nk - 1]; xhi = 3.0e38f; x0 = 0.f; sl = 0.f; r0 = t.rn[nk - 1];
-        } else {
-            xlo = t.xf[lo]; xhi = t.xf[lo + 1]; x0 = t.xf[lo]; sl = t.sn[lo]; r0 = t.rn[lo];
-        }
+        set(lo, t, nk);
     }
     __device__ __forceinline__ float delta(int k2, float lnscale, const CorrSmem& t, int nk, unsigned& flags) {
         const float x = fmaf(0.5f, __logf((float)k2), lnscale);
-        if (x < xlo || x >= xhi) locate(x, t, nk);
+        if (x >= xhi && j > -2) {  // along a column x grows: usually the next segment
+            set(j + 1, t, nk);
+            if (x >= xhi) locate(x, t, nk);
+        } else if (x < xlo) {
+            locate(x, t, nk);
+        }
         if (x < xwarn) flags |= kStKWarn;
-        return fmaf(x - x0, sl, r0);
+        return fmaf(x - x0, sl, r0);  // the constant ends have sl = 0: exactly r0
     }
 };
 

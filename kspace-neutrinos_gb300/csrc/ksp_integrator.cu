@@ -460,6 +460,92 @@ __global__ void __launch_bounds__(128) k_dnu_qag(IntegratorDev I, int nk, int Na
     }
 }
 
+// One (species, bin) task per block of W warps: the same integral as k_dnu_qag with the
+// GK61 nodes of each step spread over the block (qag_block_c, bit-identical results).
+// For calls with few tasks, where one warp per task leaves the SMs' FP64 pipes idle
+// between the long dependent chains of a single warp.
+// Shared memory: Gk61Nodes | knots[ld] | row[ld] | coef[ld] | QagList | QagBlockSmem | mbarrier
+__global__ void __launch_bounds__(128) k_dnu_qag_blk(IntegratorDev I, int nk, int Na, int nspec, int4 spec_ids) {
+    extern __shared__ __align__(16) unsigned char sm[];
+    Gk61Nodes& N = *reinterpret_cast<Gk61Nodes*>(sm);
+    size_t off = (sizeof(Gk61Nodes) + 15) & ~size_t(15);
+    double* knots = reinterpret_cast<double*>(sm + off);
+    off += sizeof(double) * I.ld;
+    double* row = reinterpret_cast<double*>(sm + off);
+    off += sizeof(double) * I.ld;
+    double* rc = reinterpret_cast<double*>(sm + off);
+    off += sizeof(double) * I.ld;
+    QagList& L = *reinterpret_cast<QagList*>(sm + off);
+    off += (sizeof(QagList) + 15) & ~size_t(15);
+    QagBlockSmem& sh = *reinterpret_cast<QagBlockSmem*>(sm + off);
+    off += (sizeof(QagBlockSmem) + 15) & ~size_t(15);
+    uint64_t* bar = reinterpret_cast<uint64_t*>(sm + off);
+    const int tid = threadIdx.x;
+    gk61_fill(N, tid, blockDim.x);
+    for (int i = tid; i < Na; i += blockDim.x) knots[i] = I.scalefact[i];
+    if (tid == 0) mbar_init(bar, 1);
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    __syncthreads();
+    const Background* B = I.B;
+    const StepScalars& S = *I.sc;
+    const int ntask = nspec * nk;
+    const unsigned row_bytes = (unsigned)(((Na + 1) & ~1) * sizeof(double));
+    unsigned phase = 0;
+    int my_max = 0;
+    long long my_tot = 0;
+    for (int task = blockIdx.x; task < ntask; task += gridDim.x) {
+        const int si = task / nk, ik = task % nk;
+        const int mi = si == 0 ? spec_ids.x : (si == 1 ? spec_ids.y : spec_ids.z);
+        const double mnu = B->mnu_J[mi];
+        const double mnubykT = mnu / B->kBtnu;
+        const double k = I.wavenum[ik];
+        const double specJ0 = specialJ(k * S.fsl_A0a / (mnubykT > 0 ? mnubykT : 1), 0.0, B->nufrac_low[0]);
+        double val = specJ0 * I.nu_init[ik] * (1. + S.deriv_prefac * S.fsl_A0a);
+        const bool integrate = !S.skip_integral && Na > 1 && mnubykT > 0;
+        if (integrate) {
+            __syncthreads();  // the previous task's readers of row / rc are done
+            if (tid == 0) {
+                asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+                mbar_expect_tx(bar, Na > 2 ? 2 * row_bytes : row_bytes);
+                bulk_g2s(row, I.dtot + (size_t)ik * I.ld, row_bytes, bar);
+                if (Na > 2) bulk_g2s(rc, I.coef + (size_t)ik * I.ld, row_bytes, bar);
+            }
+            const bool got = __syncthreads_and(mbar_wait_bounded(bar, phase));  // block-uniform
+            phase ^= 1;
+            if (!got) {
+                if (tid == 0) atomicOr(I.status, kStTimeout);
+                mbar_wait_bounded(bar, phase ^ 1);
+                return;
+            }
+            const double qc = S.partnu_now > 0 ? B->vcrit * mnubykT : 0.0;
+            const DnuIntegrandC f = dnu_integrand(I, S, k, mnubykT, qc, knots, row, rc, Na);
+            const QagResult r = qag_block_c(f, N, L, S.loga0, S.loga, 0.0, S.relerr, kQagLimit, sh);
+            val += S.prefac * r.result;
+            if (I.ivals) {  // keep the final subdivision for the adjoint
+                double* dst = I.ivals + ((size_t)mi * I.nk_alloc + ik) * kQagLimit * 2;
+                for (int q = tid; q < r.nint; q += blockDim.x) {
+                    dst[2 * q] = L.a[q];
+                    dst[2 * q + 1] = L.b[q];
+                }
+                if (tid == 0) I.nivals[(size_t)mi * I.nk_alloc + ik] = r.nint;
+            }
+            if (!r.ok && tid == 0) atomicOr(I.status, kStGsl);
+            my_max = max(my_max, r.nint);
+            my_tot += r.nint;
+        }
+        if (tid == 0) I.dnu_s[(size_t)mi * I.nk_alloc + ik] = val;
+    }
+    if (tid == 0 && my_tot) {
+        atomicMax(I.qag_max, my_max);
+        atomicAdd(reinterpret_cast<unsigned long long*>(I.qag_total), (unsigned long long)my_tot);
+    }
+}
+
+size_t dnu_qag_blk_smem(int ld) {
+    return ((sizeof(Gk61Nodes) + 15) & ~size_t(15)) + 3 * sizeof(double) * ld + ((sizeof(QagList) + 15) & ~size_t(15)) +
+           ((sizeof(QagBlockSmem) + 15) & ~size_t(15)) + sizeof(uint64_t);
+}
+
 // delta_tot_table.c:155-170: combine the species
 __global__ void k_combine(IntegratorDev I, int nk) {
     const int ik = blockIdx.x * blockDim.x + threadIdx.x;
@@ -504,7 +590,7 @@ size_t dnu_qag_smem(int ld, int wpb) {
 
 void launch_delta_nu_combined(const IntegratorDev& I, int nk, int Na, double a, double loga, double loga0,
                               double TimeTransfer, int start_row, int nspec, const int* spec_ids,
-                              int warps_per_block, cudaStream_t st) {
+                              int warps_per_block, cudaStream_t st, int qag_split) {
     static const GL4 gl = gl4_host();
     k_scalars<<<1, 256, 0, st>>>(I, Na, a, loga, loga0, TimeTransfer, start_row);
     if (nk <= 0) return;  // scalars only
@@ -540,9 +626,29 @@ void launch_delta_nu_combined(const IntegratorDev& I, int nk, int Na, double a, 
     }
     const int ntask = nspec * nk;
     if (ntask > 0) {
-        const int blocks = (ntask + wpb - 1) / wpb;
-        k_dnu_qag<<<blocks, 32 * wpb, smem, st>>>(I, nk, Na, nspec,
-                                                  make_int4(spec_ids[0], spec_ids[1], spec_ids[2], 0));
+        static int nsm = 0;
+        if (!nsm) {
+            int dev = 0;
+            cudaGetDevice(&dev);
+            cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
+            if (nsm <= 0) nsm = 1;
+        }
+        // few tasks: a block of 4 warps per task; many: a warp per task
+        const int split = qag_split > 0 ? qag_split : (ntask < 4 * nsm ? 4 : 1);
+        const size_t bsmem = dnu_qag_blk_smem(I.ld);
+        if (split > 1 && bsmem <= 227 * 1024) {
+            static bool blk_attr = false;
+            if (!blk_attr) {
+                cudaFuncSetAttribute(k_dnu_qag_blk, cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024);
+                blk_attr = true;
+            }
+            k_dnu_qag_blk<<<ntask, 32 * (split >= 4 ? 4 : 2), bsmem, st>>>(
+                I, nk, Na, nspec, make_int4(spec_ids[0], spec_ids[1], spec_ids[2], 0));
+        } else {
+            const int blocks = (ntask + wpb - 1) / wpb;
+            k_dnu_qag<<<blocks, 32 * wpb, smem, st>>>(I, nk, Na, nspec,
+                                                      make_int4(spec_ids[0], spec_ids[1], spec_ids[2], 0));
+        }
     }
     k_combine<<<(nk + 255) / 256, 256, 0, st>>>(I, nk);
 }

@@ -188,9 +188,10 @@ void launch_delta_tot_init(const IntegratorDev& I, int nk, const double* wavenum
                            int fresh, double TimeTransfer, cudaStream_t st);
 // get_delta_nu_combined (delta_tot_table.c:153-172) with Na rows: writes I.dnu
 // start_row: leading rows of the knot factorisation still valid from an earlier call
+// qag_split: warps per (species, bin) task (1, 2 or 4; 0 = chosen by the task count)
 void launch_delta_nu_combined(const IntegratorDev& I, int nk, int Na, double a, double loga, double loga0,
                               double TimeTransfer, int start_row, int nspec, const int* spec_ids,
-                              int warps_per_block, cudaStream_t st);
+                              int warps_per_block, cudaStream_t st, int qag_split = 0);
 size_t dnu_qag_smem(int ld, int wpb);
 // end of get_delta_nu_update (delta_tot_table.c:226-248) + interface_common.c:134-146:
 // delta_nu_last, committed row, NaN check, clamp, ratio/log k/kspace_prefac, grid table

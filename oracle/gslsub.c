@@ -263,6 +263,23 @@ void gslsub_qag_counters(long long *calls, long long *intervals)
     *calls = g_total_qag_calls;
     *intervals = g_total_qag_intervals;
 }
+/* rule applications by depth in the bisection tree of [a, b] (diagnostics) */
+static long long g_depth_rules[32];
+static double g_depth_a, g_depth_w;
+static void count_rule(double lo, double hi)
+{
+    const double r = g_depth_w / (hi - lo);
+    int d = 0;
+    while (d < 31 && r > 1.5 * (double)(1LL << d)) d++;
+    g_depth_rules[d]++;
+}
+void gslsub_depth_rules(long long *out32, int reset)
+{
+    for (int i = 0; i < 32; i++) {
+        out32[i] = g_depth_rules[i];
+        if (reset) g_depth_rules[i] = 0;
+    }
+}
 void gslsub_reset_counters(void) { g_total_qag_calls = 0; g_total_qag_intervals = 0; }
 
 int gsl_integration_qag(const gsl_function *f, double a, double b, double epsabs, double epsrel,
@@ -287,6 +304,9 @@ int gsl_integration_qag(const gsl_function *f, double a, double b, double epsabs
         return GSL_EBADTOL;
     }
     g_total_qag_calls++;
+    g_depth_a = a;
+    g_depth_w = b - a;
+    count_rule(a, b);
     gk61(f, a, b, &res0, &err0, &rabs0, &rasc0);
     w->size = 1;
     w->alist[0] = a;
@@ -324,6 +344,8 @@ int gsl_integration_qag(const gsl_function *f, double a, double b, double epsabs
         const double a_i = w->alist[k], b_i = w->blist[k], r_i = w->rlist[k], e_i = w->elist[k];
         const double a1 = a_i, b1 = 0.5 * (a_i + b_i), a2 = b1, b2 = b_i;
         double area1, error1, rabs1, rasc1, area2, error2, rabs2, rasc2;
+        count_rule(a1, b1);
+        count_rule(a2, b2);
         gk61(f, a1, b1, &area1, &error1, &rabs1, &rasc1);
         gk61(f, a2, b2, &area2, &error2, &rabs2, &rasc2);
         const double area12 = area1 + area2, error12 = error1 + error2;

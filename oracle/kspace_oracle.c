@@ -1287,6 +1287,51 @@ int ko_add_nu_power_to_rhogrid(ko_state *s, double Time, double BoxSize, float *
     return st;
 }
 
+/* The same step in FP64 throughout (test infrastructure: the precision reference):
+ * |F|^2 and the window in double (ko_total_powerspectrum mode 1), the delta_nu integral
+ * as the state's options say (exact = 1 for ~1e-13), the correction applied to a double
+ * copy of the grid.  grid_in: float complex [nslab][N][N/2+1]; grid_out: double complex. */
+int ko_add_nu_power_to_rhogrid_fp64(ko_state *s, double Time, double BoxSize, const float *grid_in, double *grid_out,
+                                    int pmgrid, int nthreads, int *nk_out, double *keff_o, double *dcdm_o,
+                                    double *dnu_o, double *ratio_o, double *norm_o)
+{
+    const int nb = s->nk_alloc;
+    double *power = (double *)malloc(nb * sizeof(double));
+    double *keff = (double *)malloc(nb * sizeof(double));
+    double *dnu = (double *)malloc(nb * sizeof(double));
+    long long *count = (long long *)malloc(nb * sizeof(long long));
+    const int nk = ko_total_powerspectrum(pmgrid, grid_in, nb, 0, pmgrid, power, count, keff, 1, 0, NULL, nthreads);
+    const double scale = pow(BoxSize, -3);
+    for (int i = 0; i < nk; i++) {
+        power[i] = sqrt(power[i] / scale);
+        keff[i] *= (2 * M_PI / BoxSize);
+    }
+    if (keff_o)
+        memcpy(keff_o, keff, nk * sizeof(double));
+    if (dcdm_o)
+        memcpy(dcdm_o, power, nk * sizeof(double));
+    double norm = 0;
+    int st = ko_neutrino_power_internal(s, Time, keff, power, dnu, nk, &norm);
+    const size_t n2 = (size_t)2 * pmgrid * pmgrid * (pmgrid / 2 + 1);
+    for (size_t i = 0; i < n2; i++)
+        grid_out[i] = grid_in[i];
+    if (!st)
+        st = ko_apply_correction(grid_out, pmgrid, 0, pmgrid, BoxSize, keff, power, nk, norm, 1, nthreads);
+    if (nk_out)
+        *nk_out = nk;
+    if (dnu_o)
+        memcpy(dnu_o, dnu, nk * sizeof(double));
+    if (ratio_o)
+        memcpy(ratio_o, power, nk * sizeof(double));
+    if (norm_o)
+        *norm_o = norm;
+    free(power);
+    free(keff);
+    free(dnu);
+    free(count);
+    return st;
+}
+
 /* ================================================================== differentiation (test infrastructure) */
 int ko_state_set_vectors(ko_state *s, const double *nu_init, const double *nu_last, const double *wavenum, int nk)
 {

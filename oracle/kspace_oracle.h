@@ -98,6 +98,10 @@ int ko_neutrino_power_internal(ko_state *s, double Time, double *keff, double *d
 
 /* interface_gadget.c:158-194 add_nu_power_to_rhogrid as one call (single rank).
  * Outputs (optional): nk, keff (k), dcdm, dnu, logk/ratio/norm of the interpolator. */
+/* the same step in FP64 throughout (binning mode 1, correction on a double grid) */
+int ko_add_nu_power_to_rhogrid_fp64(ko_state *s, double Time, double BoxSize, const float *grid_in, double *grid_out,
+                                    int pmgrid, int nthreads, int *nk_out, double *keff_o, double *dcdm_o,
+                                    double *dnu_o, double *ratio_o, double *norm_o);
 int ko_add_nu_power_to_rhogrid(ko_state *s, double Time, double BoxSize, float *grid, int pmgrid, int slab0,
                                int nslab, int nthreads, int *nk_out, double *keff, double *dcdm, double *dnu,
                                double *logk, double *ratio, double *norm, double *t_stages);

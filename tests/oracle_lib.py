@@ -205,6 +205,24 @@ class Oracle:
                         norm=norm.value, t_stages=t)
 
 
+    def add_nu_power_to_rhogrid_fp64(self, s, Time, BoxSize, grid, pmgrid, nthreads=1, nk_alloc=None):
+        """The step in FP64 throughout; returns (status, outputs, corrected complex128 grid)."""
+        assert grid.dtype == np.complex64 and grid.flags.c_contiguous
+        nb = nk_alloc or self.get_state(s)["nk_alloc"]
+        keff, dcdm, dnu, ratio = (np.zeros(nb) for _ in range(4))
+        norm = d()
+        nk = C.c_int()
+        out = np.zeros(grid.shape, dtype=np.complex128)
+        L = self.L
+        L.ko_add_nu_power_to_rhogrid_fp64.argtypes = [vp, d, d, vp, vp, i32, i32, C.POINTER(C.c_int), PD, PD, PD, PD,
+                                                       C.POINTER(d)]
+        L.ko_add_nu_power_to_rhogrid_fp64.restype = i32
+        st = L.ko_add_nu_power_to_rhogrid_fp64(s, Time, BoxSize, grid.ctypes.data, out.ctypes.data, pmgrid, nthreads,
+                                                C.byref(nk), _p(keff), _p(dcdm), _p(dnu), _p(ratio), C.byref(norm))
+        n = nk.value
+        return st, dict(nk=n, keff=keff[:n], dcdm=dcdm[:n], dnu=dnu[:n], ratio=ratio[:n], norm=norm.value), out
+
+
 class RefLib:
     """The unmodified reference C (oracle/_ref/libkspace_ref.so)."""
     _lib = None
