@@ -9,7 +9,7 @@
 //   r_b    = max(dnu_b, 0) / dcdm_b,   P_nu,b = max(dnu_b,0)^2
 //   y_m    = x_m (1 + norm interp_r(log|k_m|))                (correction, K3)
 // Adjoint (subdivision of every QAG held fixed, background Omega_nu(a), H(a) fixed):
-//   B1  k_adj_reduce_plain   rbar_j = norm sum_m (gbar_m . x_m) dinterp/dr_j   (reads gbar, x)
+//   B1  k_adj_reduce8        rbar_j = norm sum_m (gbar_m . x_m) dinterp/dr_j   (reads gbar, x)
 //   B2a k_adj_bins           dnubar_b from rbar and the P_nu cotangent
 //   B2  k_dnu_adj            warp per (species, bin): history row and spline
 //                            coefficients staged by TMA bulk copies; the GK61 nodes of the
@@ -75,6 +75,114 @@ __device__ __forceinline__ void corr_weights(int k2, const GridArgs& g, const Co
     const float tt = (x - t.xf[j0]) / (t.xf[j0 + 1] - t.xf[j0]);
     w0 = 1.f - tt;
     w1 = tt;
+}
+
+// B1, 8 consecutive modes per thread: the table segment of the modes is followed in
+// x = log k (as the correction pass does), and a run of modes in one segment j
+// accumulates A = sum u and B = sum u t (u = gbar . x, t the position in the segment) in
+// FP32, so d/dr_j gets A - B and d/dr_{j+1} gets B once per run, into the warp's own
+// float totals; each block adds its warps' totals to the FP64 node sums once.
+__global__ void __launch_bounds__(256) k_adj_reduce8(GridArgs g, CorrTable corr, const float* __restrict__ gbar,
+                                                     const float* __restrict__ x, double* node_sum, long long nchunks,
+                                                     int adv_il, int adv_j, int adv_z) {
+    extern __shared__ __align__(16) unsigned char sm_raw[];
+    const int nw = blockDim.x >> 5, warp = threadIdx.x >> 5;
+    float* s_xf = reinterpret_cast<float*>(sm_raw);
+    float* s_acc = s_xf + g.nk;  // [nw][nk]
+    for (int i = threadIdx.x; i < g.nk; i += blockDim.x) s_xf[i] = corr.xf[i];
+    for (int i = threadIdx.x; i < nw * g.nk; i += blockDim.x) s_acc[i] = 0.f;
+    __syncthreads();
+    float* acc = s_acc + warp * g.nk;
+    const int nk = g.nk;
+    // current segment: node j0, t = (x - x0) * inv + tadd, valid for xlo <= x < xhi
+    int j0 = -1;
+    float xlo = 3.0e38f, xhi = -3.0e38f, x0 = 0.f, inv = 0.f, tadd = 0.f;
+    float A = 0.f, B = 0.f;
+    auto flush = [&]() {
+        if (j0 >= 0 && (A != 0.f || B != 0.f)) {
+            atomicAdd(acc + j0, A - B);
+            atomicAdd(acc + j0 + 1, B);
+        }
+        A = 0.f;
+        B = 0.f;
+    };
+    auto locate = [&](float xm) {
+        int lo = -1, hi = nk;  // largest j with xf[j] <= xm
+        while (hi - lo > 1) {
+            const int mid = (lo + hi) >> 1;
+            if (s_xf[mid] <= xm) lo = mid; else hi = mid;
+        }
+        if (lo < 0) {  // constant below the first node: all to node 0
+            j0 = 0; xlo = -3.0e38f; xhi = s_xf[0]; x0 = 0.f; inv = 0.f; tadd = 0.f;
+        } else if (lo >= nk - 1) {  // constant from the last node: all to node nk-1
+            j0 = nk - 2; xlo = s_xf[nk - 1]; xhi = 3.0e38f; x0 = 0.f; inv = 0.f; tadd = 1.f;
+        } else {
+            j0 = lo; xlo = s_xf[lo]; xhi = s_xf[lo + 1]; x0 = xlo; inv = 1.f / (xhi - xlo); tadd = 0.f;
+        }
+    };
+    const long long stride = (long long)gridDim.x * blockDim.x;
+    long long ci = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    if (ci < nchunks) {
+        const long long m0 = ci * 8;
+        KCursor c;
+        c.init(g, m0 / g.nz, (int)(m0 % g.nz), 0);
+        for (; ci < nchunks; ci += stride) {
+            const long long mb = ci * 8;
+            const bool full = mb + 8 <= g.nmodes;
+            float gv[16], xv[16];
+            if (full) {
+                const float4* gp = reinterpret_cast<const float4*>(gbar + 2 * mb);
+                const float4* xp = reinterpret_cast<const float4*>(x + 2 * mb);
+#pragma unroll
+                for (int q = 0; q < 4; q++) {
+                    const float4 a = __ldg(gp + q), bq = __ldg(xp + q);
+                    gv[4 * q] = a.x; gv[4 * q + 1] = a.y; gv[4 * q + 2] = a.z; gv[4 * q + 3] = a.w;
+                    xv[4 * q] = bq.x; xv[4 * q + 1] = bq.y; xv[4 * q + 2] = bq.z; xv[4 * q + 3] = bq.w;
+                }
+            } else {
+#pragma unroll
+                for (int q = 0; q < 16; q++) {
+                    const bool in = mb * 2 + q < 2 * g.nmodes;
+                    gv[q] = in ? gbar[2 * mb + q] : 0.f;
+                    xv[q] = in ? x[2 * mb + q] : 0.f;
+                }
+            }
+            KCursor cc = c;
+#pragma unroll
+            for (int e = 0; e < 8; e++) {
+                const int k2 = cc.kxy2 + cc.z * cc.z;
+                if (k2 != 0 && mb + e < g.nmodes) {
+                    const float xm = fmaf(0.5f, __logf((float)k2), g.lnscale);
+                    if (xm < xlo || xm >= xhi) {
+                        flush();
+                        locate(xm);
+                    }
+                    const float u = fmaf(gv[2 * e], xv[2 * e], gv[2 * e + 1] * xv[2 * e + 1]);
+                    const float t = fmaf(xm - x0, inv, tadd);
+                    A += u;
+                    B = fmaf(u, t, B);
+                }
+                cc.next(g);
+            }
+            // advance the cursor by the grid stride (stride * 8 modes = adv_il slabs, adv_j
+            // rows, adv_z modes)
+            c.z += adv_z;
+            int carry = 0;
+            if (c.z >= g.nz) { c.z -= g.nz; carry = 1; }
+            c.j += adv_j + carry;
+            carry = 0;
+            if (c.j >= g.N) { c.j -= g.N; carry = 1; }
+            c.il += adv_il + carry;
+            c.set_row(g);
+        }
+    }
+    flush();
+    __syncthreads();
+    for (int i = threadIdx.x; i < nk; i += blockDim.x) {
+        double v = 0.0;
+        for (int w = 0; w < nw; w++) v += (double)s_acc[w * nk + i];
+        if (v != 0.0) atomicAdd(node_sum + i, v);
+    }
 }
 
 __global__ void k_adj_reduce_plain(GridArgs g, const int* __restrict__ thresh, const int* __restrict__ cmapg,
@@ -319,26 +427,53 @@ __global__ void __launch_bounds__(128) k_dnu_adj(IntegratorDev I, DnuAdjArgs A, 
                 QagResult r = qag_warp_c(f, N, L, S.loga0, S.loga, 0.0, S.relerr, kQagLimit);
                 nint = r.nint;
             }
+            const DnuIntegrandC fi = dnu_integrand(I, S, k, mnubykT, qc, knots, row, rc, Na);
+            const double ckm = -sbar * S.prefac * fi.k_over_m / mnu;  // d(J's argument)/dm per fsl
             for (int q = 0; q < nint; q++) {
                 const double a_i = iv ? iv[2 * q] : L.a[q];
                 const double b_i = iv ? iv[2 * q + 1] : L.b[q];
                 const double c = __dmul_rn(0.5, __dadd_rn(a_i, b_i));
                 const double h = __dmul_rn(0.5, __dsub_rn(b_i, a_i));
-                for (int jn = lane; jn < 61; jn += 32) {
-                    const double xn = __dadd_rn(c, __dmul_rn(h, N.x[jn]));
-                    const DnuNode o = dnu_node(B, k, mnubykT, qc, B->nufrac_low[0], I.fs_x, I.fs_y, I.fs_c, S.Nfs,
-                                               S.loga0, fs_inv, knots, row, rc, Na, xn);
-                    const double wt = N.wk[jn] * h;
-                    const double u = wt * o.g * o.J;
-                    const double t = o.dx / o.h;
-                    atomicAdd(&ybar[o.seg], u * (1 - t));
-                    atomicAdd(&ybar[o.seg + 1], u * t);
-                    if (Na > 2) {
-                        const double dx = o.dx, hh = o.h;
-                        atomicAdd(&cbar[o.seg], u * (dx * (-2 * hh / 3) + dx * dx - dx * dx * dx / (3 * hh)));
-                        atomicAdd(&cbar[o.seg + 1], u * (dx * (-hh / 3) + dx * dx * dx / (3 * hh)));
+                const int slot = nc_slot_of(a_i, b_i, S.loga0, S.loga, I.nc_slots);
+                // nodes in ascending x (lane order): the history segments grow with the
+                // lane, so a segmented warp sum per segment replaces atomic updates
+                for (int m = 0; m < 2; m++) {
+                    const int sidx = lane + 32 * m;
+                    double ya = 0.0, yb = 0.0, ca = 0.0, cb = 0.0;
+                    int key = -1;
+                    if (sidx < 61) {
+                        const int jn = sidx < 30 ? sidx : (sidx == 30 ? 60 : 90 - sidx);
+                        const double xn = __dadd_rn(c, __dmul_rn(h, N.x[jn]));
+                        const NodeTerms t = fi.terms(slot, jn, xn);
+                        double J, Jd;
+                        if (qc > 0) {
+                            J = specialJ(t.fsl * fi.k_over_m, qc, fi.nfl);
+                            Jd = 0.0;
+                        } else {
+                            specialJ_fit_tab_d(t.fsl * fi.k_over_m, J, Jd);
+                        }
+                        const double hh = knots[t.j + 1] - knots[t.j];
+                        const double dx = t.dx;
+                        const double wt = N.wk[jn] * h;
+                        const double u = wt * t.g * J;
+                        const double tt = dx / hh;
+                        ya = u * (1 - tt);
+                        yb = u * tt;
+                        if (Na > 2) {
+                            ca = u * (dx * (-2 * hh / 3) + dx * dx - dx * dx * dx / (3 * hh));
+                            cb = u * (dx * (-hh / 3) + dx * dx * dx / (3 * hh));
+                        }
+                        key = t.j;
+                        mder += ckm * wt * t.g * Jd * t.fsl * dnu_S(t, row, rc, Na, fi.ks);
                     }
-                    mder += S.prefac * sbar * wt * o.g * o.Jd * (-o.xj / mnu) * o.S;
+                    bool tail;
+                    warp_seg_sum4(key, ya, yb, ca, cb, tail);
+                    // each run's last lane adds its run; left ends first, then right ends
+                    // (two runs may share a knot), so no two lanes touch one entry at once
+                    if (tail && key >= 0) { ybar[key] += ya; cbar[key] += ca; }
+                    __syncwarp();
+                    if (tail && key >= 0) { ybar[key + 1] += yb; cbar[key + 1] += cb; }
+                    __syncwarp();
                 }
             }
             __syncwarp();
@@ -451,6 +586,21 @@ static int sm_count_a() {
 void launch_adj_reduce(const GridGeom& gg, CorrTable corr, float lnscale, const float* gbar, const float* x,
                        double* node_sum, cudaStream_t st) {
     GridArgs a = make_grid_args(gg, corr.nk, lnscale);
+    const bool aligned = ((reinterpret_cast<uintptr_t>(gbar) | reinterpret_cast<uintptr_t>(x)) & 15) == 0;
+    if (aligned && corr.nk >= 2) {
+        const long long nchunks = (gg.nmodes + 7) / 8;
+        long long blocks = (nchunks + 255) / 256;
+        if (blocks > 4LL * sm_count_a()) blocks = 4LL * sm_count_a();
+        if (blocks < 1) blocks = 1;
+        const long long adv = blocks * 256 * 8;  // modes per grid stride
+        const int nz = gg.N / 2 + 1;
+        const size_t smem = sizeof(float) * corr.nk * (1 + 8);
+        cudaFuncSetAttribute(k_adj_reduce8, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        const long long adv_rows = adv / nz;
+        k_adj_reduce8<<<(int)blocks, 256, smem, st>>>(a, corr, gbar, x, node_sum, nchunks, (int)(adv_rows / gg.N),
+                                                      (int)(adv_rows % gg.N), (int)(adv % nz));
+        return;
+    }
     const size_t smem = sizeof(double) * corr.nk + sizeof(int) * (2 * gg.nrbins + 1) + sizeof(float) * 3 * corr.nk + 64;
     cudaFuncSetAttribute(k_adj_reduce_plain, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     long long blocks = (gg.nmodes + 255) / 256;

@@ -85,6 +85,9 @@ extern "C" int kspace_gpu_create(kspace_ctx** out, int device) {
     CK(cudaMallocHost(reinterpret_cast<void**>(&c->status_h), sizeof(unsigned)));
     CK(dalloc(&c->dB, 1));
     for (int i = 0; i < 5; i++) CK(cudaEventCreate(&c->ev[i]));
+    CK(cudaStreamCreateWithFlags(&c->side, cudaStreamNonBlocking));
+    CK(cudaEventCreateWithFlags(&c->ev_fork, cudaEventDisableTiming));
+    CK(cudaEventCreateWithFlags(&c->ev_join, cudaEventDisableTiming));
     if (const char* e = getenv("KSPACE_GPU_TMA")) c->tma = atoi(e);
     if (const char* e = getenv("KSPACE_GPU_ROWS")) c->rows = atoi(e);
     if (const char* e = getenv("KSPACE_GPU_STAGES")) c->stages = atoi(e);
@@ -132,6 +135,7 @@ extern "C" int kspace_gpu_destroy(kspace_ctx* c) {
     if (!c) return KSPACE_OK;
     cudaSetDevice(c->device);
     cudaStreamSynchronize(c->stream);
+    if (c->side) cudaStreamSynchronize(c->side);
     free_table(c);
     for (auto& kv : c->geos) {
         Geo& g = kv.second;
@@ -148,6 +152,9 @@ extern "C" int kspace_gpu_destroy(kspace_ctx* c) {
     if (c->status_h) cudaFreeHost(c->status_h);
     for (int i = 0; i < 5; i++)
         if (c->ev[i]) cudaEventDestroy(c->ev[i]);
+    if (c->ev_fork) cudaEventDestroy(c->ev_fork);
+    if (c->ev_join) cudaEventDestroy(c->ev_join);
+    if (c->side) cudaStreamDestroy(c->side);
     if (c->own_stream) cudaStreamDestroy(c->own_stream);
     delete c;
     return KSPACE_OK;
@@ -679,8 +686,15 @@ static int update_device(kspace_ctx* c, double a, int nk_in, const double* keff_
     c->h_scalefact[c->ia] = loga;
     c->ia++;
     const int Na = c->ia;
-    launch_delta_nu_combined(I, c->nk, Na, a, loga, c->loga0, c->TimeTransfer, c->fact_valid, c->nspec, c->spec_ids,
-                             c->qag_warps, c->stream, c->qag_split);
+    if (c->prep_valid && c->prep_Na == Na && c->prep_loga == loga) {
+        // the delta_cdm-independent part already ran beside the binning pass
+        CK(cudaStreamWaitEvent(c->stream, c->ev_join, 0));
+        launch_integrator_rest(I, c->nk, Na, c->nspec, c->spec_ids, c->qag_warps, c->stream, c->qag_split);
+    } else {
+        launch_delta_nu_combined(I, c->nk, Na, a, loga, c->loga0, c->TimeTransfer, c->fact_valid, c->nspec,
+                                 c->spec_ids, c->qag_warps, c->stream, c->qag_split);
+    }
+    c->prep_valid = false;
     // keep the row if far enough from the previous one (delta_tot_table.c:229-237)
     const bool commit = a >= exp(c->h_scalefact[Na - 2]) + 0.009;
     launch_finish_update(I, c->nk, commit ? Na - 1 : -1, a, loga, want_corr ? keff_d : nullptr, dnu_out_d,
@@ -898,6 +912,26 @@ extern "C" int kspace_gpu_add_nu_power_to_rhogrid(kspace_ctx* c, double Time, do
     bool staged;
     st = grid_in(c, grid, bytes, &gd, &staged);
     if (st) return st;
+    // The integrator work that does not depend on this step's delta_cdm (scalars, knot
+    // factorisation, fslength and node tables) starts now on the side stream, beside
+    // the binning pass; update_device waits for it.  Only for the common case: a new
+    // scale factor on an initialised table with room for the provisional row.
+    c->prep_valid = false;
+    if (c->init_done && c->ia >= 1 && c->ia < c->I.namax && G->nk == c->nk && c->nk >= 2) {
+        const double loga = log(Time);
+        if (!(loga - c->h_scalefact[c->ia - 1] < kFloatAcc)) {
+            const int Na = c->ia + 1;
+            CK(cudaEventRecord(c->ev_fork, c->stream));
+            CK(cudaStreamWaitEvent(c->side, c->ev_fork, 0));
+            launch_integrator_prepare(c->I, Na, Time, loga, c->loga0, c->TimeTransfer, c->fact_valid, 1, false,
+                                      c->side);
+            CK(cudaEventRecord(c->ev_join, c->side));
+            g_launches += 5;
+            c->prep_valid = true;
+            c->prep_Na = Na;
+            c->prep_loga = loga;
+        }
+    }
     // compute_neutrino_power_spectrum (interface_gadget.c:75-102)
     st = bin_grid(c, G, gd, pmgrid, slab0, nslab, BoxSize);
     if (st) return st;

@@ -182,11 +182,11 @@ __global__ void __launch_bounds__(1024) kb_fs_finish(BatchDev b) {
 // thread per (instance, unknown): closed-form inverse of tridiag(1,4,1), as k_fs_coeffs
 __global__ void kb_fs_coeffs(BatchDev b) {
     __shared__ double mupow[82];
-    if (threadIdx.x < 82) {
+    for (int e = threadIdx.x; e < 82; e += blockDim.x) {  // any block size
         const double mu = 2.0 - sqrt(3.0);
         double p = 1.0;
-        for (int k = 0; k < (int)threadIdx.x; k++) p *= mu;
-        mupow[threadIdx.x] = p;
+        for (int k = 0; k < e; k++) p *= mu;
+        mupow[e] = p;
     }
     __syncthreads();
     const int total = b.hdr->total_fsc;

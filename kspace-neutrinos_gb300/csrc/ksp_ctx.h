@@ -76,6 +76,13 @@ struct kspace_ctx {
     int diff_ia = 0, diff_Na = 0, diff_nk = 0, diff_store = 0;
     double diff_time = 0, diff_box = 0;
     int diff_pmgrid = 0;
+    // the delta_cdm-independent integrator work of a step, run on a side stream while the
+    // binning pass runs (add_nu_power_to_rhogrid)
+    cudaStream_t side = nullptr;
+    cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
+    bool prep_valid = false;
+    int prep_Na = 0;
+    double prep_loga = 0;
     // profiling
     bool prof = false;
     cudaEvent_t ev[5] = {nullptr, nullptr, nullptr, nullptr, nullptr};

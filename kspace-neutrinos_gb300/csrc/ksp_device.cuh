@@ -267,11 +267,13 @@ __device__ __forceinline__ double warp_sum_to0(double v) {
 __device__ __forceinline__ double bcast0(double v) { return __shfl_sync(0xffffffffu, v, 0); }
 
 // QUADPACK error estimate: err = resasc * min(1, (200 |err|/resasc)^1.5), floored at
-// 50 eps resabs (Piessens et al. 1983, qk rules).
+// 50 eps resabs (Piessens et al. 1983, qk rules).  t^1.5 as t sqrt(t): within an ulp of
+// pow(t, 1.5), without pow's long FP64 dependency chain on the QAG's critical path.
 __device__ __forceinline__ double rescale_error(double err, double resabs, double resasc) {
     err = fabs(err);
     if (resasc != 0.0 && err != 0.0) {
-        const double s = pow(200.0 * err / resasc, 1.5);
+        const double t = 200.0 * err / resasc;
+        const double s = t * sqrt(t);
         err = s < 1.0 ? resasc * s : resasc;
     }
     if (resabs > DBL_MIN / (50.0 * DBL_EPSILON)) {
@@ -628,17 +630,18 @@ __device__ __forceinline__ void gk61_block_c(const F& f, const Gk61Nodes& N, int
                 if (t == 0) rs[0] += d; else rs[1] += d;
             }
         }
-        for (int t = 0; t < nint; t++) {
-            rs[t] = bcast0(warp_sum_to0(rs[t]));
-            if (lane == 0) {
-                const double err = (rk[t] - rg[t]) * h[t];
-                GkOut o;
-                o.result = rk[t] * h[t];
-                o.resabs = ra[t] * fabs(h[t]);
-                o.resasc = rs[t] * fabs(h[t]);
-                o.abserr = rescale_error(err, o.resabs, o.resasc);
-                sh.out[t] = o;
-            }
+        for (int t = 0; t < nint; t++) rs[t] = bcast0(warp_sum_to0(rs[t]));
+        if (lane < nint) {  // the intervals' estimates on separate lanes
+            const int t = lane;
+            const double rkt = t ? rk[1] : rk[0], rgt = t ? rg[1] : rg[0], rat = t ? ra[1] : ra[0];
+            const double rst = t ? rs[1] : rs[0], ht = t ? h[1] : h[0];
+            const double err = (rkt - rgt) * ht;
+            GkOut o;
+            o.result = rkt * ht;
+            o.resabs = rat * fabs(ht);
+            o.resasc = rst * fabs(ht);
+            o.abserr = rescale_error(err, o.resabs, o.resasc);
+            sh.out[t] = o;
         }
     }
     __syncthreads();
@@ -769,23 +772,27 @@ struct KnotSeg {
     const double* ih3;
 };
 
+// The history row's natural spline (or linear for 2 knots) at a node.
+__device__ __forceinline__ double dnu_S(const NodeTerms& t, const double* ky, const double* kc, int na,
+                                        const KnotSeg& ks) {
+    const int j = t.j;
+    const double y0 = ky[j], y1 = ky[j + 1];
+    if (na > 2) {
+        const double c0 = kc[j], c1 = kc[j + 1];
+        const double bq = (y1 - y0) * __ldg(ks.ih + j) - (c1 + 2.0 * c0) * __ldg(ks.h3 + j);
+        const double d = (c1 - c0) * __ldg(ks.ih3 + j);
+        return y0 + t.dx * (bq + t.dx * (c0 + t.dx * d));
+    }
+    return y0 + t.dx * ((y1 - y0) * __ldg(ks.ih + j));
+}
+
 // The per-bin rest: J and the history row's natural spline (or linear for 2 knots) at
 // the node.  Same for the cached and uncached paths.
 // k_over_m = k / (m / kT): J's argument is fslength * k_over_m (one division per bin
 // instead of one per node).
 __device__ __forceinline__ double dnu_combine(const NodeTerms& t, double k_over_m, double qc, double nfl,
                                               const double* ky, const double* kc, int na, const KnotSeg& ks) {
-    const int j = t.j;
-    const double y0 = ky[j], y1 = ky[j + 1];
-    double S;
-    if (na > 2) {
-        const double c0 = kc[j], c1 = kc[j + 1];
-        const double bq = (y1 - y0) * __ldg(ks.ih + j) - (c1 + 2.0 * c0) * __ldg(ks.h3 + j);
-        const double d = (c1 - c0) * __ldg(ks.ih3 + j);
-        S = y0 + t.dx * (bq + t.dx * (c0 + t.dx * d));
-    } else {
-        S = y0 + t.dx * ((y1 - y0) * __ldg(ks.ih + j));
-    }
+    const double S = dnu_S(t, ky, kc, na, ks);
     const double J = specialJ_tab(t.fsl * k_over_m, qc, nfl);
     return t.g * J * S;
 }
@@ -820,7 +827,48 @@ struct DnuIntegrandC {
         }
         return dnu_combine(t, k_over_m, qc, nfl, ky, kc, na, ks);
     }
+    __device__ NodeTerms terms(int slot, int jn, double x) const {
+        if (slot >= 0) {
+            const int q = slot * 61 + jn;
+            NodeTerms t;
+            t.g = __ldg(nc.g + q);
+            t.fsl = __ldg(nc.fsl + q);
+            t.dx = __ldg(nc.dx + q);
+            t.j = __ldg(nc.j + q);
+            return t;
+        }
+        return dnu_node_terms(B, fs_x, fs_y, fs_c, nfs, fs_x0, fs_inv, kx, na, x);
+    }
 };
+
+// Slot of the dyadic interval [a, b] of [lo, hi] in a node table of nslots slots (-1: not
+// one of them), by the bisections QAG performs.
+__device__ __forceinline__ int nc_slot_of(double a, double b, double lo, double hi, int nslots) {
+    int s = 0;
+    while (s < nslots) {
+        if (lo == a && hi == b) return s;
+        const double m = 0.5 * (lo + hi);
+        if (a >= m) { lo = m; s = 2 * s + 2; } else { hi = m; s = 2 * s + 1; }
+    }
+    return -1;
+}
+
+// Segmented sums over the lanes of a warp: runs of equal key (in lane order) are summed
+// onto the run's last lane, for four values at once.
+__device__ __forceinline__ void warp_seg_sum4(int key, double& a, double& b, double& c, double& d, bool& tail) {
+    const int lane = threadIdx.x & 31;
+    const int up = __shfl_up_sync(0xffffffffu, key, 1);
+    const bool head = lane == 0 || up != key;
+    const unsigned heads = __ballot_sync(0xffffffffu, head);
+    const int my_head = 31 - __clz(heads & (0xffffffffu >> (31 - lane)));
+#pragma unroll
+    for (int dd = 1; dd < 32; dd <<= 1) {
+        const double oa = __shfl_up_sync(0xffffffffu, a, dd), ob = __shfl_up_sync(0xffffffffu, b, dd);
+        const double oc = __shfl_up_sync(0xffffffffu, c, dd), od = __shfl_up_sync(0xffffffffu, d, dd);
+        if (lane - dd >= my_head) { a += oa; b += ob; c += oc; d += od; }
+    }
+    tail = lane == 31 || ((heads >> (lane + 1)) & 1u);
+}
 
 // End points of cache slot s of [a, b], by the bisections QAG performs (b1 = (a+b)/2).
 __device__ __forceinline__ void nc_interval(int s, double a, double b, double* lo, double* hi) {

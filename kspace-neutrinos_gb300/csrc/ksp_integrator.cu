@@ -201,7 +201,11 @@ void launch_delta_tot_init(const IntegratorDev& I, int nk, const double* wavenum
 // by an earlier call with the same leading knots and are kept.  Reciprocals are stored
 // so the per-row sweeps need no divisions.
 __global__ void k_scalars(IntegratorDev I, int Na, double a, double loga, double loga0, double TimeTransfer,
-                          int start_row) {
+                          int start_row, int write_knot) {
+    if (write_knot) {  // the provisional knot (update_row writes the same value)
+        if (threadIdx.x == 0) I.scalefact[Na - 1] = loga;
+        __syncthreads();
+    }
     const double* xk = I.scalefact;
     for (int i = threadIdx.x; i + 1 < Na; i += blockDim.x) {
         const double h = xk[i + 1] - xk[i];
@@ -316,11 +320,11 @@ __global__ void k_fs_finish(IntegratorDev I, int Nfs) {
 // Terms with |i-j| > 40 are below 1e-22 relative and dropped.
 __global__ void k_fs_coeffs(IntegratorDev I, int Nfs, double loga0, double loga) {
     __shared__ double mupow[82];
-    if (threadIdx.x < 82) {
+    for (int e = threadIdx.x; e < 82; e += blockDim.x) {  // any block size
         const double mu = 2.0 - sqrt(3.0);
         double p = 1.0;
-        for (int k = 0; k < (int)threadIdx.x; k++) p *= mu;
-        mupow[threadIdx.x] = p;
+        for (int k = 0; k < e; k++) p *= mu;
+        mupow[e] = p;
     }
     __syncthreads();
     const int m = Nfs - 2;
@@ -346,13 +350,16 @@ __global__ void k_fs_coeffs(IntegratorDev I, int Nfs, double loga0, double loga)
 
 // ------------------------------------------------------------------ history splines
 // Forward/back substitution of every history row against the shared factorisation,
-// warp per row.
+// warp per row (warp-parallel affine scans when the row fits in shared memory).
 __global__ void k_dtot_coeffs(IntegratorDev I, int nk, int Na, int staged) {
     extern __shared__ __align__(16) double sdc[];
     const int warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
     double* sy = staged ? sdc + (size_t)warp * 2 * I.ld : nullptr;
     double* sc = staged ? sy + I.ld : nullptr;
-    for (int ik = blockIdx.x * nw + warp; ik < nk; ik += gridDim.x * nw) dtot_row_coeffs_warp(I, ik, Na, sy, sc);
+    for (int ik = blockIdx.x * nw + warp; ik < nk; ik += gridDim.x * nw) {
+        if (staged) dtot_row_coeffs_scan(I, ik, Na, sy, sc);
+        else dtot_row_coeffs_warp(I, ik, Na, nullptr, nullptr);
+    }
 }
 
 // ------------------------------------------------------------------ node table
@@ -588,23 +595,34 @@ size_t dnu_qag_smem(int ld, int wpb) {
            wpb * (sizeof(QagList) + 2 * sizeof(double) * ld) + wpb * sizeof(uint64_t);
 }
 
-void launch_delta_nu_combined(const IntegratorDev& I, int nk, int Na, double a, double loga, double loga0,
-                              double TimeTransfer, int start_row, int nspec, const int* spec_ids,
-                              int warps_per_block, cudaStream_t st, int qag_split) {
+// The part of a call that does not depend on the current delta_cdm: the scalars and the
+// knot factorisation, the fslength table, the node table.  Can run concurrently with
+// the binning pass (write_knot = 1 also stores the provisional knot, log a).
+void launch_integrator_prepare(const IntegratorDev& I, int Na, double a, double loga, double loga0,
+                               double TimeTransfer, int start_row, int write_knot, bool scalars_only,
+                               cudaStream_t st) {
     static const GL4 gl = gl4_host();
-    k_scalars<<<1, 256, 0, st>>>(I, Na, a, loga, loga0, TimeTransfer, start_row);
-    if (nk <= 0) return;  // scalars only
+    k_scalars<<<1, 256, 0, st>>>(I, Na, a, loga, loga0, TimeTransfer, start_row, write_knot);
+    if (scalars_only) return;
     // the fslength table (always built: it also gives fslength(log a0, log a))
     const int Nfs = 16 * (Na > 1 ? Na : 1);
     if (loga > loga0) {
         const long long threads = 4LL * Nfs;
         k_fs_segments<<<(unsigned)((threads + 255) / 256), 256, 0, st>>>(I, Nfs, loga0, loga, gl);
         k_fs_finish<<<1, 1024, 0, st>>>(I, Nfs);
-        if (Nfs > 2) k_fs_coeffs<<<(Nfs - 2 + 127) / 128, 128, 0, st>>>(I, Nfs, loga0, loga);
+        if (Nfs > 2) k_fs_coeffs<<<(Nfs - 2 + 31) / 32, 32, 0, st>>>(I, Nfs, loga0, loga);
     } else {
         cudaMemsetAsync(&I.sc->fsl_A0a, 0, sizeof(double), st);
         cudaMemsetAsync(&I.sc->Nfs, 0, sizeof(int), st);
     }
+    if (loga > loga0 && Na > 1 && I.nc_slots > 0)
+        k_nc_build<<<(I.nc_slots * 61 + 63) / 64, 64, 0, st>>>(I, Na);
+}
+
+// The rest, after the provisional history row: spline coefficients of the rows, the
+// integrals, the species sum.
+void launch_integrator_rest(const IntegratorDev& I, int nk, int Na, int nspec, const int* spec_ids,
+                            int warps_per_block, cudaStream_t st, int qag_split) {
     if (Na > 2) {
         static bool dc_attr = false;
         if (!dc_attr) {
@@ -615,8 +633,6 @@ void launch_delta_nu_combined(const IntegratorDev& I, int nk, int Na, double a, 
         const int staged = smem <= 200 * 1024;
         k_dtot_coeffs<<<(nk + 3) / 4, 128, staged ? smem : 0, st>>>(I, nk, Na, staged);
     }
-    if (loga > loga0 && Na > 1 && I.nc_slots > 0)
-        k_nc_build<<<(I.nc_slots * 61 + 127) / 128, 128, 0, st>>>(I, Na);
     const int wpb = warps_per_block < 1 ? 1 : (warps_per_block > 4 ? 4 : warps_per_block);
     const size_t smem = dnu_qag_smem(I.ld, wpb);
     static bool attr_set = false;
@@ -651,6 +667,14 @@ void launch_delta_nu_combined(const IntegratorDev& I, int nk, int Na, double a, 
         }
     }
     k_combine<<<(nk + 255) / 256, 256, 0, st>>>(I, nk);
+}
+
+void launch_delta_nu_combined(const IntegratorDev& I, int nk, int Na, double a, double loga, double loga0,
+                              double TimeTransfer, int start_row, int nspec, const int* spec_ids,
+                              int warps_per_block, cudaStream_t st, int qag_split) {
+    launch_integrator_prepare(I, Na, a, loga, loga0, TimeTransfer, start_row, 0, nk <= 0, st);
+    if (nk <= 0) return;  // scalars only
+    launch_integrator_rest(I, nk, Na, nspec, spec_ids, warps_per_block, st, qag_split);
 }
 
 // ------------------------------------------------------------------ end of an update

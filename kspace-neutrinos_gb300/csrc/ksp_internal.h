@@ -150,6 +150,83 @@ __device__ __forceinline__ void dtot_row_coeffs_warp(const IntegratorDev& I, int
     __syncwarp();
 }
 
+// The same solve with all 32 lanes: both substitutions are linear recurrences
+// z_u = r_u - f_u z_{u-1} and c_u = (z_u - o_u c_{u+1}) / d_u, i.e. chains of affine
+// maps; each lane composes the maps of its stretch of rows, a warp scan composes the
+// stretches, and each lane then replays its stretch from the value entering it.  The
+// results equal the sequential sweep's up to rounding.  sy, sc: ld doubles of shared
+// memory each (staged rows).
+__device__ __forceinline__ void dtot_row_coeffs_scan(const IntegratorDev& I, int ik, int Na, double* sy,
+                                                     double* sc) {
+    const int lane = threadIdx.x & 31;
+    const double* y = I.dtot + (size_t)ik * I.ld;
+    double* c = I.coef + (size_t)ik * I.ld;
+    for (int k = lane; k < Na; k += 32) sy[k] = y[k];
+    __syncwarp();
+    const int m = Na - 2;  // unknowns c[1..m]
+    const double* ih = I.knot_invh;
+    const double* x = I.scalefact;
+    const int per = (m + 31) / 32;
+    const int u0 = min(m, lane * per), u1 = min(m, u0 + per);
+    // forward: z_u = r_u - fac_u z_{u-1} (fac_0 = 0)
+    double A = 1.0, B = 0.0;
+    for (int u = u0; u < u1; u++) {
+        const double r = 3.0 * ((sy[u + 2] - sy[u + 1]) * ih[u + 1] - (sy[u + 1] - sy[u]) * ih[u]);
+        const double f = u > 0 ? I.knot_fac[u] : 0.0;
+        B = r - f * B;
+        A = -f * A;
+        sc[u + 1] = r;  // keep r_u
+    }
+    // exclusive scan of the maps z -> A z + B over the lanes (left to right)
+    double pa = A, pb = B;
+#pragma unroll
+    for (int d = 1; d < 32; d <<= 1) {
+        const double qa = __shfl_up_sync(0xffffffffu, pa, d), qb = __shfl_up_sync(0xffffffffu, pb, d);
+        if (lane >= d) {  // (mine) after (theirs)
+            pb = pa * qb + pb;
+            pa = pa * qa;
+        }
+    }
+    double zin = __shfl_up_sync(0xffffffffu, pb, 1);  // z entering this stretch (z_{-1} = 0)
+    if (lane == 0) zin = 0.0;
+    for (int u = u0; u < u1; u++) {
+        const double f = u > 0 ? I.knot_fac[u] : 0.0;
+        zin = sc[u + 1] - f * zin;
+        sc[u + 1] = zin;  // z_u
+    }
+    __syncwarp();
+    // backward: c_u = (z_u - off_u c_{u+1}) * invdiag_u, c_{m} (= c[m+1]) = 0
+    A = 1.0;
+    B = 0.0;
+    for (int u = u1 - 1; u >= u0; u--) {
+        const double off = u < m - 1 ? x[u + 2] - x[u + 1] : 0.0;
+        const double iv = I.knot_invdiag[u];
+        B = (sc[u + 1] - off * B) * iv;
+        A = -off * iv * A;
+    }
+    pa = A;
+    pb = B;
+#pragma unroll
+    for (int d = 1; d < 32; d <<= 1) {  // right to left
+        const double qa = __shfl_down_sync(0xffffffffu, pa, d), qb = __shfl_down_sync(0xffffffffu, pb, d);
+        if (lane + d < 32) {
+            pb = pa * qb + pb;
+            pa = pa * qa;
+        }
+    }
+    double cin = __shfl_down_sync(0xffffffffu, pb, 1);  // c entering from the right
+    if (lane == 31) cin = 0.0;
+    __syncwarp();
+    for (int u = u1 - 1; u >= u0; u--) {
+        const double off = u < m - 1 ? x[u + 2] - x[u + 1] : 0.0;
+        cin = (sc[u + 1] - off * cin) * I.knot_invdiag[u];
+        sc[u + 1] = cin;
+    }
+    __syncwarp();
+    for (int k = lane; k < Na; k += 32) c[k] = (k == 0 || k == Na - 1) ? 0.0 : sc[k];
+    __syncwarp();
+}
+
 // The delta_nu integrand of one (species, bin) with the instance's node table; knots,
 // row and rc may be staged copies (shared memory) of the instance's arrays.
 __device__ __forceinline__ DnuIntegrandC dnu_integrand(const IntegratorDev& I, const StepScalars& S, double k,
@@ -192,6 +269,13 @@ void launch_delta_tot_init(const IntegratorDev& I, int nk, const double* wavenum
 void launch_delta_nu_combined(const IntegratorDev& I, int nk, int Na, double a, double loga, double loga0,
                               double TimeTransfer, int start_row, int nspec, const int* spec_ids,
                               int warps_per_block, cudaStream_t st, int qag_split = 0);
+// the same in two parts: what does not depend on delta_cdm (may overlap the binning
+// pass; write_knot stores the provisional knot log a), and the rest
+void launch_integrator_prepare(const IntegratorDev& I, int Na, double a, double loga, double loga0,
+                               double TimeTransfer, int start_row, int write_knot, bool scalars_only,
+                               cudaStream_t st);
+void launch_integrator_rest(const IntegratorDev& I, int nk, int Na, int nspec, const int* spec_ids,
+                            int warps_per_block, cudaStream_t st, int qag_split);
 size_t dnu_qag_smem(int ld, int wpb);
 // end of get_delta_nu_update (delta_tot_table.c:226-248) + interface_common.c:134-146:
 // delta_nu_last, committed row, NaN check, clamp, ratio/log k/kspace_prefac, grid table

@@ -29,6 +29,37 @@ __device__ __forceinline__ double specialJ_fit_tab(double x) {
     return v;
 }
 
+// J and dJ/dx together (the adjoint): the derivative of the piece's polynomial, times
+// du/dx; outside the table the formula and its derivative.
+__device__ __forceinline__ void specialJ_fit_tab_d(double x, double& J, double& Jd) {
+    if (x <= 0.) { J = 1.; Jd = 0.; return; }
+    const long long bits = __double_as_longlong(x);
+    const int e = (int)((bits >> 52) & 0x7ff) - 1023;
+    if (e < KSP_JFIT_E0 || e >= KSP_JFIT_E1) {
+        const double x2 = x * x, x4 = x2 * x2, x8 = x4 * x4;
+        const double p = e < KSP_JFIT_E0 ? 0.0 : exp(4.1811 * log(x));
+        const double N = 1. + 0.0168 * x2 + 0.0407 * x4;
+        const double D = 1. + 2.1734 * x2 + 1.6787 * p + 0.1467 * x8;
+        const double dN = 0.0336 * x + 0.1628 * x2 * x;
+        const double dD = 4.3468 * x + 1.6787 * 4.1811 * p / x + 1.1736 * x4 * x2 * x;
+        J = N / D;
+        Jd = (dN * D - N * dD) / (D * D);
+        return;
+    }
+    const int sub = (int)((bits >> (52 - KSP_JFIT_SUB_BITS)) & ((1 << KSP_JFIT_SUB_BITS) - 1));
+    const double* p = g_jfit + (((e - KSP_JFIT_E0) << KSP_JFIT_SUB_BITS) | sub) * KSP_JFIT_STRIDE;
+    const double ih = __ldg(p + 1);
+    const double u = (x - __ldg(p)) * ih;
+    double v = __ldg(p + 2 + KSP_JFIT_DEG), dv = 0.0;
+#pragma unroll
+    for (int j = KSP_JFIT_DEG - 1; j >= 0; j--) {
+        dv = fma(dv, u, v);
+        v = fma(v, u, __ldg(p + 2 + j));
+    }
+    J = v;
+    Jd = dv * ih;
+}
+
 // specialJ (delta_tot_table.c:442-463) with the tabulated fit
 __device__ __forceinline__ double specialJ_tab(double x, double qc, double nufrac_low) {
     return qc > 0 ? specialJ(x, qc, nufrac_low) : specialJ_fit_tab(x);
