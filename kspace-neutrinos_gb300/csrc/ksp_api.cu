@@ -375,7 +375,7 @@ extern "C" int kspace_gpu_alloc_table(kspace_ctx* c, int nk_alloc, double TimeTr
     CK(dalloc(&I.nc_fsl, kNcNodes));
     CK(dalloc(&I.nc_dx, kNcNodes));
     CK(dalloc(&I.nc_j, kNcNodes));
-    I.nc_slots = (1 << c->nc_levels) - 1;
+    I.nc_slots = c->nc_levels > 0 ? 1 + 2 * c->nc_levels : 0;
     I.fs_cap = 16 * (int)ld + 16;
     CK(dalloc(&I.fs_x, I.fs_cap));
     CK(dalloc(&I.fs_y, I.fs_cap));

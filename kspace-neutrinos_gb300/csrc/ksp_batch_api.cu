@@ -49,7 +49,7 @@ struct kspace_batch {
     int total_bins = 0, ldmax = 0;
     // tuning
     int wpb = 4, blocks_per_sm = 2, use_graph = 1;
-    int nc_slots = 63;  // node-table slots per instance (6 levels)
+    int nc_slots = 17;  // node-table slots per instance (8 levels of the right spine)
     bool eager_done = false;
     cudaGraph_t graph = nullptr;
     cudaGraphExec_t exec = nullptr;
@@ -109,7 +109,8 @@ extern "C" int kspace_gpu_batch_create(kspace_batch** out, kspace_ctx* const* ct
     b->last_status.assign(M, 0);
     if (const char* e = getenv("KSPACE_GPU_NC_LEVELS")) {
         const int l = atoi(e);
-        b->nc_slots = (1 << (l < 0 ? 0 : (l > kNcMaxLevels ? kNcMaxLevels : l))) - 1;
+        const int lv = l < 0 ? 0 : (l > kNcMaxLevels ? kNcMaxLevels : l);
+        b->nc_slots = lv > 0 ? 1 + 2 * lv : 0;
     }
     batch_set_attributes();
     *out = b;

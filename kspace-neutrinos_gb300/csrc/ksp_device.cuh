@@ -423,17 +423,23 @@ __device__ QagResult qag_warp(const F& f, const Gk61Nodes& N, QagList& L, double
     return R;
 }
 // ------------------------------------------------------------------ cached QAG
-// QAG only ever bisects, so its intervals are the dyadic subintervals of [a, b]; those
-// of the first kNcLevels levels are numbered in heap order (root 0, children of s:
-// 2s+1, 2s+2).  A functor with node(slot, j, x) may serve the 61 nodes of such an
-// interval from a table built once; x is passed for the others (slot -1).
-constexpr int kNcMaxLevels = 6;
-constexpr int kNcMaxSlots = (1 << kNcMaxLevels) - 1;  // 63 intervals
-constexpr int kNcNodes = kNcMaxSlots * 61;               // capacity of a node table
+// QAG only ever bisects, so its intervals are dyadic subintervals of [a, b].  For the
+// delta_nu integral it refines toward the upper end (log a, where J -> 1 and the newest
+// history rows are): at every depth the intervals it evaluates are the two children of
+// the rightmost interval of the depth above.  Those are numbered: slot 0 = [a, b]; at
+// depth d >= 1, slot 2d-1 the left and slot 2d the right child of the depth-(d-1)
+// rightmost interval.  A functor with node(slot, j, x) may serve the 61 nodes of such an
+// interval from a table built once; the others pass slot -1.
+constexpr int kNcMaxLevels = 12;
+constexpr int kNcMaxSlots = 1 + 2 * kNcMaxLevels;  // 25 intervals
+constexpr int kNcNodes = kNcMaxSlots * 61;         // capacity of a node table
 
-// child slot of s (right = 0, 1) in a table of nslots = 2^levels - 1 slots
+// child slot of s (right = 0, 1) in a table of nslots = 1 + 2 levels slots
 __device__ __forceinline__ int nc_child(int s, int right, int nslots) {
-    return (s >= 0 && 2 * s + 2 < nslots) ? 2 * s + 1 + right : -1;
+    if (s < 0 || (s > 0 && (s & 1))) return -1;  // only the rightmost intervals have cached children
+    const int d = s / 2 + 1;                      // depth of the children
+    const int c = 2 * d - 1 + right;
+    return c < nslots ? c : -1;
 }
 
 // gk61_warp with interval slots (same arithmetic)
@@ -844,11 +850,13 @@ struct DnuIntegrandC {
 // Slot of the dyadic interval [a, b] of [lo, hi] in a node table of nslots slots (-1: not
 // one of them), by the bisections QAG performs.
 __device__ __forceinline__ int nc_slot_of(double a, double b, double lo, double hi, int nslots) {
-    int s = 0;
-    while (s < nslots) {
-        if (lo == a && hi == b) return s;
+    if (nslots <= 0) return -1;
+    if (a == lo && b == hi) return 0;
+    for (int d = 1; 2 * d < nslots + 1; d++) {
         const double m = 0.5 * (lo + hi);
-        if (a >= m) { lo = m; s = 2 * s + 2; } else { hi = m; s = 2 * s + 1; }
+        if (a == lo && b == m) return 2 * d - 1;
+        if (a == m && b == hi) return 2 * d;
+        lo = m;
     }
     return -1;
 }
@@ -872,15 +880,11 @@ __device__ __forceinline__ void warp_seg_sum4(int key, double& a, double& b, dou
 
 // End points of cache slot s of [a, b], by the bisections QAG performs (b1 = (a+b)/2).
 __device__ __forceinline__ void nc_interval(int s, double a, double b, double* lo, double* hi) {
-    int lvl = 0;
-    while ((2 << lvl) - 1 <= s) lvl++;
-    const int p = s + 1 - (1 << lvl);
-    for (int i = lvl - 1; i >= 0; i--) {
-        const double m = 0.5 * (a + b);
-        if ((p >> i) & 1) a = m; else b = m;
-    }
-    *lo = a;
-    *hi = b;
+    if (s == 0) { *lo = a; *hi = b; return; }
+    const int d = (s + 1) / 2;
+    for (int k = 1; k < d; k++) a = 0.5 * (a + b);  // the rightmost interval of depth k
+    const double m = 0.5 * (a + b);
+    if (s & 1) { *lo = a; *hi = m; } else { *lo = m; *hi = b; }
 }
 #endif  // __CUDACC__
 

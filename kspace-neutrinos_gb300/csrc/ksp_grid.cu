@@ -150,18 +150,35 @@ k_bin_power_tma(const __grid_constant__ CUtensorMap tmap, GridArgs g, const int*
             const unsigned char* rp = stage0 + (size_t)st * ROWS * 128 + (size_t)r * 128;
             ModeCursor c;
             c.init(g, s_w1, s_rowbase, s_zbase, r * 16 + q * MPT);
+            if (c.z + MPT <= g.nz && c.kxy2 != 0) {
+                // the common case: all MPT modes in one column, none of them k = 0; k^2 and
+                // z follow from the first mode
+                const int z0 = c.z;
+                int k2 = c.kxy2 + z0 * z0;
 #pragma unroll
-            for (int u = q * (MPT / 2); u < (q + 1) * (MPT / 2); u++) {
-                const float4 v = *reinterpret_cast<const float4*>(rp + ((u ^ (r & 7)) << 4));
-                {
-                    const int k2 = c.kxy2 + c.z * c.z;
-                    if (k2 != 0) acc.add(k2, mode_power2w(v.x, v.y, c, s_w1, s_wt), g, s_thr, s_H, s_L);
-                    c.next(g, s_w1);
+                for (int u = 0; u < MPT / 2; u++) {
+                    const float4 v = *reinterpret_cast<const float4*>(rp + (((q * (MPT / 2) + u) ^ (r & 7)) << 4));
+                    c.z = z0 + 2 * u;
+                    acc.add(k2, mode_power2w(v.x, v.y, c, s_w1, s_wt), g, s_thr, s_H, s_L);
+                    k2 += 2 * c.z + 1;
+                    c.z++;
+                    acc.add(k2, mode_power2w(v.z, v.w, c, s_w1, s_wt), g, s_thr, s_H, s_L);
+                    k2 += 2 * c.z + 1;
                 }
-                {
-                    const int k2 = c.kxy2 + c.z * c.z;
-                    if (k2 != 0) acc.add(k2, mode_power2w(v.z, v.w, c, s_w1, s_wt), g, s_thr, s_H, s_L);
-                    c.next(g, s_w1);
+            } else {
+#pragma unroll
+                for (int u = q * (MPT / 2); u < (q + 1) * (MPT / 2); u++) {
+                    const float4 v = *reinterpret_cast<const float4*>(rp + ((u ^ (r & 7)) << 4));
+                    {
+                        const int k2 = c.kxy2 + c.z * c.z;
+                        if (k2 != 0) acc.add(k2, mode_power2w(v.x, v.y, c, s_w1, s_wt), g, s_thr, s_H, s_L);
+                        c.next(g, s_w1);
+                    }
+                    {
+                        const int k2 = c.kxy2 + c.z * c.z;
+                        if (k2 != 0) acc.add(k2, mode_power2w(v.z, v.w, c, s_w1, s_wt), g, s_thr, s_H, s_L);
+                        c.next(g, s_w1);
+                    }
                 }
             }
             acc.flush(s_H, s_L);

@@ -46,7 +46,7 @@ struct IntegratorDev {
     double* nc_fsl;
     double* nc_dx;
     int* nc_j;
-    int nc_slots;                    // slots of the node table in use (2^levels - 1, 0 = none)
+    int nc_slots;                    // slots of the node table in use (1 + 2 levels, 0 = none)
     double* fs_x;                    // [fs_cap]
     double* fs_y;                    // [fs_cap]
     double* fs_c;                    // [fs_cap]
