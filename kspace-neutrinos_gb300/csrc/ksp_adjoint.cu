@@ -345,6 +345,59 @@ __device__ __forceinline__ DnuNode dnu_node(const Background* B, double k, doubl
     return o;
 }
 
+// The 61 nodes of one interval [a_i, b_i] of the final subdivision, by one warp (lane
+// order = ascending x): each node's weight w g J times the spline weights of its
+// history segment goes to ybar / cbar (cotangents of the delta_tot row values and of
+// its spline second derivatives), and its mass derivative to mder (per lane).
+__device__ __forceinline__ void adj_interval(const DnuIntegrandC& fi, const Gk61Nodes& N, const double* knots,
+                                             const double* row, const double* rc, int Na, double qc, double a_i,
+                                             double b_i, double loga0, double loga, int nc_slots, double ckm,
+                                             double* ybar, double* cbar, double& mder, int lane) {
+    const double c = __dmul_rn(0.5, __dadd_rn(a_i, b_i));
+    const double h = __dmul_rn(0.5, __dsub_rn(b_i, a_i));
+    const int slot = nc_slot_of(a_i, b_i, loga0, loga, nc_slots);
+    // nodes in ascending x (lane order): the history segments grow with the
+    // lane, so a segmented warp sum per segment replaces atomic updates
+    for (int m = 0; m < 2; m++) {
+        const int sidx = lane + 32 * m;
+        double ya = 0.0, yb = 0.0, ca = 0.0, cb = 0.0;
+        int key = -1;
+        if (sidx < 61) {
+            const int jn = sidx < 30 ? sidx : (sidx == 30 ? 60 : 90 - sidx);
+            const double xn = __dadd_rn(c, __dmul_rn(h, N.x[jn]));
+            const NodeTerms t = fi.terms(slot, jn, xn);
+            double J, Jd;
+            if (qc > 0) {
+                J = specialJ(t.fsl * fi.k_over_m, qc, fi.nfl);
+                Jd = 0.0;
+            } else {
+                specialJ_fit_tab_d(t.fsl * fi.k_over_m, J, Jd);
+            }
+            const double hh = knots[t.j + 1] - knots[t.j];
+            const double dx = t.dx;
+            const double wt = N.wk[jn] * h;
+            const double u = wt * t.g * J;
+            const double tt = dx / hh;
+            ya = u * (1 - tt);
+            yb = u * tt;
+            if (Na > 2) {
+                ca = u * (dx * (-2 * hh / 3) + dx * dx - dx * dx * dx / (3 * hh));
+                cb = u * (dx * (-hh / 3) + dx * dx * dx / (3 * hh));
+            }
+            key = t.j;
+            mder += ckm * wt * t.g * Jd * t.fsl * dnu_S(t, row, rc, Na, fi.ks);
+        }
+        bool tail;
+        warp_seg_sum4(key, ya, yb, ca, cb, tail);
+        // each run's last lane adds its run; left ends first, then right ends
+        // (two runs may share a knot), so no two lanes touch one entry at once
+        if (tail && key >= 0) { ybar[key] += ya; cbar[key] += ca; }
+        __syncwarp();
+        if (tail && key >= 0) { ybar[key + 1] += yb; cbar[key + 1] += cb; }
+        __syncwarp();
+    }
+}
+
 // Shared memory per CTA: Gk61Nodes | knots[ld] | per warp: QagList, row[ld], coef[ld], ybar[ld], cbar[ld] | bars
 __global__ void __launch_bounds__(128) k_dnu_adj(IntegratorDev I, DnuAdjArgs A, int nk, int Na, int nspec,
                                                  int4 spec_ids) {
@@ -429,76 +482,23 @@ __global__ void __launch_bounds__(128) k_dnu_adj(IntegratorDev I, DnuAdjArgs A, 
             }
             const DnuIntegrandC fi = dnu_integrand(I, S, k, mnubykT, qc, knots, row, rc, Na);
             const double ckm = -sbar * S.prefac * fi.k_over_m / mnu;  // d(J's argument)/dm per fsl
-            for (int q = 0; q < nint; q++) {
-                const double a_i = iv ? iv[2 * q] : L.a[q];
-                const double b_i = iv ? iv[2 * q + 1] : L.b[q];
-                const double c = __dmul_rn(0.5, __dadd_rn(a_i, b_i));
-                const double h = __dmul_rn(0.5, __dsub_rn(b_i, a_i));
-                const int slot = nc_slot_of(a_i, b_i, S.loga0, S.loga, I.nc_slots);
-                // nodes in ascending x (lane order): the history segments grow with the
-                // lane, so a segmented warp sum per segment replaces atomic updates
-                for (int m = 0; m < 2; m++) {
-                    const int sidx = lane + 32 * m;
-                    double ya = 0.0, yb = 0.0, ca = 0.0, cb = 0.0;
-                    int key = -1;
-                    if (sidx < 61) {
-                        const int jn = sidx < 30 ? sidx : (sidx == 30 ? 60 : 90 - sidx);
-                        const double xn = __dadd_rn(c, __dmul_rn(h, N.x[jn]));
-                        const NodeTerms t = fi.terms(slot, jn, xn);
-                        double J, Jd;
-                        if (qc > 0) {
-                            J = specialJ(t.fsl * fi.k_over_m, qc, fi.nfl);
-                            Jd = 0.0;
-                        } else {
-                            specialJ_fit_tab_d(t.fsl * fi.k_over_m, J, Jd);
-                        }
-                        const double hh = knots[t.j + 1] - knots[t.j];
-                        const double dx = t.dx;
-                        const double wt = N.wk[jn] * h;
-                        const double u = wt * t.g * J;
-                        const double tt = dx / hh;
-                        ya = u * (1 - tt);
-                        yb = u * tt;
-                        if (Na > 2) {
-                            ca = u * (dx * (-2 * hh / 3) + dx * dx - dx * dx * dx / (3 * hh));
-                            cb = u * (dx * (-hh / 3) + dx * dx * dx / (3 * hh));
-                        }
-                        key = t.j;
-                        mder += ckm * wt * t.g * Jd * t.fsl * dnu_S(t, row, rc, Na, fi.ks);
-                    }
-                    bool tail;
-                    warp_seg_sum4(key, ya, yb, ca, cb, tail);
-                    // each run's last lane adds its run; left ends first, then right ends
-                    // (two runs may share a knot), so no two lanes touch one entry at once
-                    if (tail && key >= 0) { ybar[key] += ya; cbar[key] += ca; }
-                    __syncwarp();
-                    if (tail && key >= 0) { ybar[key + 1] += yb; cbar[key + 1] += cb; }
-                    __syncwarp();
-                }
-            }
+            for (int q = 0; q < nint; q++)
+                adj_interval(fi, N, knots, row, rc, Na, qc, iv ? iv[2 * q] : L.a[q], iv ? iv[2 * q + 1] : L.b[q],
+                             S.loga0, S.loga, I.nc_slots, ckm, ybar, cbar, mder, lane);
             __syncwarp();
-            if (lane == 0 && Na > 2) {
-                // z = A^-1 cbar_int with the shared factorisation; ybar += rhs^T z
+            if (Na > 2) {
+                // z = A^-1 cbar_int with the shared factorisation (A is symmetric, so the
+                // solve of the forward pass applies); then ybar += rhs^T z, gathered per
+                // entry in the order the scatter over rows would add them
                 const int m = Na - 2;
-                double prev = 0;
-                for (int u = 0; u < m; u++) {
-                    double r = cbar[u + 1];
-                    if (u > 0) r -= I.knot_fac[u] * prev;
-                    prev = r;
-                    cbar[u + 1] = r;
-                }
-                double next = cbar[m] * I.knot_invdiag[m - 1];
-                cbar[m] = next;
-                for (int u = m - 1; u-- > 0;) {
-                    next = (cbar[u + 1] - (knots[u + 2] - knots[u + 1]) * next) * I.knot_invdiag[u];
-                    cbar[u + 1] = next;
-                }
-                for (int u = 0; u < m; u++) {
-                    const double z = cbar[u + 1];
-                    const double ih0 = I.knot_invh[u], ih1 = I.knot_invh[u + 1];
-                    ybar[u] += 3 * z * ih0;
-                    ybar[u + 1] -= 3 * z * (ih0 + ih1);
-                    ybar[u + 2] += 3 * z * ih1;
+                spline_solve_scan(I, m, cbar);
+                const double* ih = I.knot_invh;
+                for (int j = lane; j < Na; j += 32) {
+                    double v = ybar[j];
+                    if (j >= 2 && j <= m + 1) v += 3 * cbar[j - 1] * ih[j - 1];
+                    if (j >= 1 && j <= m) v -= 3 * cbar[j] * (ih[j - 1] + ih[j]);
+                    if (j < m) v += 3 * cbar[j + 1] * ih[j];
+                    ybar[j] = v;
                 }
             }
             __syncwarp();
@@ -567,6 +567,147 @@ __global__ void k_adj_grid_plain(GridArgs g, const int* __restrict__ thresh, con
 }
 
 // ------------------------------------------------------------------ launchers
+// Few tasks (fewer than four per SM): a block of NW warps per task.  The final
+// subdivision is recomputed with the block-cooperative QAG (the same decisions and
+// sums as the forward pass's block kernel) or read back; its intervals are dealt out
+// to the warps, each warp scatters into its own copy of the row cotangents, and the
+// copies are summed before the transposed spline solve.
+// Shared memory: Gk61Nodes | knots, row, coef [ld] | QagList | QagBlockSmem | per warp
+// ybar[ld], cbar[ld] | mbarrier
+size_t dnu_adj_blk_smem(int ld, int nw) {
+    return ((sizeof(Gk61Nodes) + 15) & ~size_t(15)) + 3 * sizeof(double) * ld + ((sizeof(QagList) + 15) & ~size_t(15)) +
+           ((sizeof(QagBlockSmem) + 15) & ~size_t(15)) + (size_t)nw * 2 * sizeof(double) * ld + 16;
+}
+
+__global__ void __launch_bounds__(128) k_dnu_adj_blk(IntegratorDev I, DnuAdjArgs A, int nk, int Na, int nspec,
+                                                     int4 spec_ids) {
+    extern __shared__ __align__(16) unsigned char sm[];
+    __shared__ double s_red[4];
+    Gk61Nodes& N = *reinterpret_cast<Gk61Nodes*>(sm);
+    size_t off = (sizeof(Gk61Nodes) + 15) & ~size_t(15);
+    double* knots = reinterpret_cast<double*>(sm + off);
+    double* row = knots + I.ld;
+    double* rc = row + I.ld;
+    off += 3 * sizeof(double) * I.ld;
+    QagList& L = *reinterpret_cast<QagList*>(sm + off);
+    off += (sizeof(QagList) + 15) & ~size_t(15);
+    QagBlockSmem& sh = *reinterpret_cast<QagBlockSmem*>(sm + off);
+    off += (sizeof(QagBlockSmem) + 15) & ~size_t(15);
+    const int tid = threadIdx.x, nw = blockDim.x >> 5, warp = tid >> 5, lane = tid & 31;
+    double* wy = reinterpret_cast<double*>(sm + off);  // [nw][ld]
+    double* wc = wy + (size_t)nw * I.ld;                // [nw][ld]
+    off += (size_t)nw * 2 * sizeof(double) * I.ld;
+    uint64_t* bar = reinterpret_cast<uint64_t*>(sm + off);
+    gk61_fill(N, tid, blockDim.x);
+    for (int i = tid; i < Na; i += blockDim.x) knots[i] = I.scalefact[i];
+    if (tid == 0) asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_u32a(bar)) : "memory");
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    __syncthreads();
+    const Background* B = I.B;
+    const StepScalars& S = *I.sc;
+    const unsigned row_bytes = (unsigned)(((Na + 1) & ~1) * sizeof(double));
+    unsigned phase = 0;
+    for (int task = blockIdx.x; task < nspec * nk; task += gridDim.x) {
+        const int si = task / nk, ik = task % nk;
+        const int mi = si == 0 ? spec_ids.x : (si == 1 ? spec_ids.y : spec_ids.z);
+        const double mnu = B->mnu_J[mi];
+        const double mnubykT = mnu / B->kBtnu;
+        const double k = I.wavenum[ik];
+        const double sbar = A.dnu_bar[ik] * S.omeganu[mi] / S.Omega_nu_tot;
+        if (sbar == 0.0) continue;  // block-uniform
+        double mder = 0.0;
+        // initial-condition piece (delta_tot_table.c:525-535)
+        if (tid == 0 && mnubykT > 0) {
+            const double x0 = k * S.fsl_A0a / mnubykT;
+            mder += sbar * specialJ_fit_deriv(x0) * (-x0 / mnu) * I.nu_init[ik] * (1. + S.deriv_prefac * S.fsl_A0a);
+        }
+        const bool integrate = !S.skip_integral && Na > 1 && mnubykT > 0;
+        if (integrate) {
+            __syncthreads();  // the previous task's readers of row / rc / wy / wc are done
+            if (tid == 0) {
+                asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+                asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32a(bar)),
+                             "r"(Na > 2 ? 2 * row_bytes : row_bytes)
+                             : "memory");
+                asm volatile(
+                    "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+                        smem_u32a(row)),
+                    "l"(I.dtot + (size_t)ik * I.ld), "r"(row_bytes), "r"(smem_u32a(bar))
+                    : "memory");
+                if (Na > 2)
+                    asm volatile(
+                        "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+                            smem_u32a(rc)),
+                        "l"(I.coef + (size_t)ik * I.ld), "r"(row_bytes), "r"(smem_u32a(bar))
+                        : "memory");
+            }
+            for (int i = tid; i < nw * I.ld; i += blockDim.x) {
+                wy[i] = 0.0;
+                wc[i] = 0.0;
+            }
+            const bool got = __syncthreads_and(mbar_wait_bounded_a(bar, phase));  // block-uniform
+            phase ^= 1;
+            if (!got) {
+                if (tid == 0) atomicOr(I.status, kStTimeout);
+                mbar_wait_bounded_a(bar, phase ^ 1);
+                return;
+            }
+            const double qc = S.partnu_now > 0 ? B->vcrit * mnubykT : 0.0;
+            int nint;
+            const double* iv = nullptr;
+            if (!A.recompute && A.ivals) {
+                nint = A.nivals[(size_t)mi * I.nk_alloc + ik];
+                iv = A.ivals + ((size_t)mi * I.nk_alloc + ik) * kQagLimit * 2;
+            } else {
+                const DnuIntegrandC f = dnu_integrand(I, S, k, mnubykT, qc, knots, row, rc, Na);
+                const QagResult r = qag_block_c(f, N, L, S.loga0, S.loga, 0.0, S.relerr, kQagLimit, sh);
+                nint = r.nint;
+            }
+            __syncthreads();
+            const DnuIntegrandC fi = dnu_integrand(I, S, k, mnubykT, qc, knots, row, rc, Na);
+            const double ckm = -sbar * S.prefac * fi.k_over_m / mnu;
+            double* yb = wy + (size_t)warp * I.ld;
+            double* cb = wc + (size_t)warp * I.ld;
+            for (int q = warp; q < nint; q += nw)
+                adj_interval(fi, N, knots, row, rc, Na, qc, iv ? iv[2 * q] : L.a[q], iv ? iv[2 * q + 1] : L.b[q],
+                             S.loga0, S.loga, I.nc_slots, ckm, yb, cb, mder, lane);
+            __syncthreads();
+            for (int j = tid; j < Na; j += blockDim.x) {
+                double y = wy[j], c = wc[j];
+                for (int w = 1; w < nw; w++) {
+                    y += wy[(size_t)w * I.ld + j];
+                    c += wc[(size_t)w * I.ld + j];
+                }
+                wy[j] = y;
+                wc[j] = c;
+            }
+            __syncthreads();
+            const int m = Na - 2;
+            if (warp == 0 && Na > 2) spline_solve_scan(I, m, wc);
+            __syncthreads();
+            const double* ih = I.knot_invh;
+            for (int j = tid; j < Na; j += blockDim.x) {  // column Na-1: the provisional row
+                double v = wy[j];
+                if (Na > 2) {
+                    if (j >= 2 && j <= m + 1) v += 3 * wc[j - 1] * ih[j - 1];
+                    if (j >= 1 && j <= m) v -= 3 * wc[j] * (ih[j - 1] + ih[j]);
+                    if (j < m) v += 3 * wc[j + 1] * ih[j];
+                }
+                atomicAdd(&A.Dbar[(size_t)ik * I.ld + j], S.prefac * sbar * v);
+            }
+        }
+        mder = warp_sum_to0(mder);
+        if (lane == 0) s_red[warp] = mder;
+        __syncthreads();
+        if (tid == 0) {
+            double t = 0.0;
+            for (int w = 0; w < nw; w++) t += s_red[w];
+            if (t != 0.0) atomicAdd(&A.mbar[mi], t);
+        }
+        __syncthreads();
+    }
+}
+
 size_t dnu_adj_smem(int ld, int wpb) {
     return ((sizeof(Gk61Nodes) + 15) & ~size_t(15)) + sizeof(double) * ld +
            wpb * (sizeof(QagList) + 4 * sizeof(double) * ld) + wpb * sizeof(uint64_t);
@@ -634,6 +775,17 @@ void launch_dnu_adj(const IntegratorDev& I, const double* dnu_bar, double* Dbar,
     }
     const int ntask = nspec * nk;
     if (ntask <= 0) return;
+    const size_t bsmem = dnu_adj_blk_smem(I.ld, 4);
+    if (ntask < 4 * sm_count_a() && bsmem <= 227 * 1024) {
+        static bool blk_attr = false;
+        if (!blk_attr) {
+            cudaFuncSetAttribute(k_dnu_adj_blk, cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024);
+            blk_attr = true;
+        }
+        k_dnu_adj_blk<<<ntask, 128, bsmem, st>>>(I, A, nk, Na, nspec,
+                                                 make_int4(spec_ids[0], spec_ids[1], spec_ids[2], 0));
+        return;
+    }
     k_dnu_adj<<<(ntask + wpb - 1) / wpb, 32 * wpb, smem, st>>>(I, A, nk, Na, nspec,
                                                                make_int4(spec_ids[0], spec_ids[1], spec_ids[2], 0));
 }

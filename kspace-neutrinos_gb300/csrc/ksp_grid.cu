@@ -490,7 +490,7 @@ static PFN_encodeTiled get_encode() {
     return fn;
 }
 
-static bool make_map(CUtensorMap* map, const void* grid, long long nrows16, int rows) {
+bool make_grid_tmap(CUtensorMap* map, const void* grid, long long nrows16, int rows) {
     PFN_encodeTiled enc = get_encode();
     if (!enc || nrows16 <= 0) return false;
     if ((reinterpret_cast<uintptr_t>(grid) & 15) != 0) return false;
@@ -519,7 +519,7 @@ static int run_bin_tma(const GridGeom& g, const GridArgs& a, const float* grid, 
                        unsigned* status, cudaStream_t st) {
     constexpr int NT = ROWS * (16 / MPT);
     CUtensorMap map;
-    if (!make_map(&map, grid, a.nrows16, ROWS)) return -1;
+    if (!make_grid_tmap(&map, grid, a.nrows16, ROWS)) return -1;
     const SmemPlan P = plan_smem(ROWS, STAGES, g.nrbins, 2 * a.nz, NT / 32);
     if (P.total > 220 * 1024) return -1;
     auto kern = k_bin_power_tma<ROWS, STAGES, MPT>;
@@ -550,7 +550,11 @@ static int bin_variant(const GridGeom& g, const GridArgs& a, const float* grid, 
 int launch_bin_power(const GridGeom& g, const float* grid, double* bin_sum, double* F0sq, unsigned* status, int tma,
                      int rows_per_cta, int stages, cudaStream_t st) {
     const GridArgs a = make_grid_args(g, 0, 0.f);
-    if (tma && a.nrows16 > 0) {
+    if (tma >= 3) {
+        const int r = launch_bin_stream(g, a, grid, bin_sum, F0sq, status, rows_per_cta / 32, stages, tma == 3, st);
+        if (r == 0) return 0;
+        if (r == -2) return -2;
+    } else if (tma && a.nrows16 > 0) {
         const int r = bin_variant(g, a, grid, bin_sum, F0sq, status, rows_per_cta, stages, tma == 2 ? 8 : 16, st);
         if (r == 0) return 0;
         if (r == -2) return -2;
@@ -570,7 +574,7 @@ static int run_corr_tma(const GridGeom& g, const GridArgs& a, float* grid, CorrT
                         cudaStream_t st) {
     constexpr int NT = ROWS * (16 / MPT);
     CUtensorMap map;
-    if (!make_map(&map, grid, a.nrows16, ROWS)) return -1;
+    if (!make_grid_tmap(&map, grid, a.nrows16, ROWS)) return -1;
     const SmemPlan P = plan_smem(ROWS, STAGES, g.nrbins, 3 * a.nk + g.nrbins);
     if (P.total > 220 * 1024) return -1;
     auto kern = k_correct_tma<ROWS, STAGES, MPT>;
@@ -599,7 +603,11 @@ static int corr_variant(const GridGeom& g, const GridArgs& a, float* grid, CorrT
 int launch_apply_correction(const GridGeom& g, float* grid, CorrTable corr, float lnscale, unsigned* status, int tma,
                             int rows_per_cta, int stages, cudaStream_t st) {
     const GridArgs a = make_grid_args(g, corr.nk, lnscale);
-    if (tma && a.nrows16 > 0) {
+    if (tma >= 3) {
+        const int r = launch_correct_stream(a, grid, corr, status, rows_per_cta / 32, stages, st);
+        if (r == 0) return 0;
+        if (r == -2) return -2;
+    } else if (tma && a.nrows16 > 0) {
         const int r = corr_variant(g, a, grid, corr, status, rows_per_cta, stages, tma == 2 ? 8 : 16, st);
         if (r == 0) return 0;
         if (r == -2) return -2;

@@ -2,11 +2,24 @@
 // correction K3 and their adjoints): mode coordinates, the exact log bin of integer
 // k^2, the CIC window factor and the correction interpolation.
 #pragma once
+#include <cuda.h>
 #include <cuda_runtime.h>
 #include <stdint.h>
 #include "ksp_internal.h"
 
 namespace ksp {
+
+// 2-D tensor map of a slab viewed as [nrows16][16 modes] complex64 (128-byte rows,
+// 128-byte swizzle), box of `rows` rows; false if the driver entry point is missing or
+// the grid pointer is not 16-byte aligned (ksp_grid.cu)
+bool make_grid_tmap(CUtensorMap* map, const void* grid, long long nrows16, int rows);
+
+struct GridArgs;
+// warp-pipelined K1 / K3 (ksp_stream.cu): 0 launched, -1 not applicable, -2 launch error
+int launch_bin_stream(const struct GridGeom& g, const GridArgs& a, const float* grid, double* bin_sum, double* F0sq,
+                      unsigned* status, int warps, int stages, bool exact, cudaStream_t st);
+int launch_correct_stream(const GridArgs& a, float* grid, struct CorrTable corr, unsigned* status, int warps,
+                          int stages, cudaStream_t st);
 
 // n / d for n < 2^31: m = floor(2^s/d)+1 with s = 31 + ceil(log2 d)
 struct FastDiv {

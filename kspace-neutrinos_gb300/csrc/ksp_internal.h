@@ -156,33 +156,25 @@ __device__ __forceinline__ void dtot_row_coeffs_warp(const IntegratorDev& I, int
 // stretches, and each lane then replays its stretch from the value entering it.  The
 // results equal the sequential sweep's up to rounding.  sy, sc: ld doubles of shared
 // memory each (staged rows).
-__device__ __forceinline__ void dtot_row_coeffs_scan(const IntegratorDev& I, int ik, int Na, double* sy,
-                                                     double* sc) {
+// Solve the natural-spline system of the knots (factorised by k_scalars) for the
+// right-hand side sc[1..m], m = Na - 2, in place, with all 32 lanes of a warp.
+__device__ __forceinline__ void spline_solve_scan(const IntegratorDev& I, int m, double* sc) {
     const int lane = threadIdx.x & 31;
-    const double* y = I.dtot + (size_t)ik * I.ld;
-    double* c = I.coef + (size_t)ik * I.ld;
-    for (int k = lane; k < Na; k += 32) sy[k] = y[k];
-    __syncwarp();
-    const int m = Na - 2;  // unknowns c[1..m]
-    const double* ih = I.knot_invh;
     const double* x = I.scalefact;
     const int per = (m + 31) / 32;
     const int u0 = min(m, lane * per), u1 = min(m, u0 + per);
     // forward: z_u = r_u - fac_u z_{u-1} (fac_0 = 0)
     double A = 1.0, B = 0.0;
     for (int u = u0; u < u1; u++) {
-        const double r = 3.0 * ((sy[u + 2] - sy[u + 1]) * ih[u + 1] - (sy[u + 1] - sy[u]) * ih[u]);
         const double f = u > 0 ? I.knot_fac[u] : 0.0;
-        B = r - f * B;
+        B = sc[u + 1] - f * B;
         A = -f * A;
-        sc[u + 1] = r;  // keep r_u
     }
-    // exclusive scan of the maps z -> A z + B over the lanes (left to right)
     double pa = A, pb = B;
 #pragma unroll
-    for (int d = 1; d < 32; d <<= 1) {
+    for (int d = 1; d < 32; d <<= 1) {  // inclusive scan of the maps, left to right
         const double qa = __shfl_up_sync(0xffffffffu, pa, d), qb = __shfl_up_sync(0xffffffffu, pb, d);
-        if (lane >= d) {  // (mine) after (theirs)
+        if (lane >= d) {
             pb = pa * qb + pb;
             pa = pa * qa;
         }
@@ -192,10 +184,10 @@ __device__ __forceinline__ void dtot_row_coeffs_scan(const IntegratorDev& I, int
     for (int u = u0; u < u1; u++) {
         const double f = u > 0 ? I.knot_fac[u] : 0.0;
         zin = sc[u + 1] - f * zin;
-        sc[u + 1] = zin;  // z_u
+        sc[u + 1] = zin;
     }
     __syncwarp();
-    // backward: c_u = (z_u - off_u c_{u+1}) * invdiag_u, c_{m} (= c[m+1]) = 0
+    // backward: c_u = (z_u - off_u c_{u+1}) * invdiag_u, c_m = 0
     A = 1.0;
     B = 0.0;
     for (int u = u1 - 1; u >= u0; u--) {
@@ -223,6 +215,27 @@ __device__ __forceinline__ void dtot_row_coeffs_scan(const IntegratorDev& I, int
         sc[u + 1] = cin;
     }
     __syncwarp();
+}
+
+// The same solve with all 32 lanes: both substitutions are linear recurrences
+// z_u = r_u - f_u z_{u-1} and c_u = (z_u - o_u c_{u+1}) / d_u, i.e. chains of affine
+// maps; each lane composes the maps of its stretch of rows, a warp scan composes the
+// stretches, and each lane then replays its stretch from the value entering it.  The
+// results equal the sequential sweep's up to rounding.  sy, sc: ld doubles of shared
+// memory each (staged rows).
+__device__ __forceinline__ void dtot_row_coeffs_scan(const IntegratorDev& I, int ik, int Na, double* sy,
+                                                     double* sc) {
+    const int lane = threadIdx.x & 31;
+    const double* y = I.dtot + (size_t)ik * I.ld;
+    double* c = I.coef + (size_t)ik * I.ld;
+    for (int k = lane; k < Na; k += 32) sy[k] = y[k];
+    __syncwarp();
+    const int m = Na - 2;  // unknowns c[1..m]
+    const double* ih = I.knot_invh;
+    for (int u = lane; u < m; u += 32)
+        sc[u + 1] = 3.0 * ((sy[u + 2] - sy[u + 1]) * ih[u + 1] - (sy[u + 1] - sy[u]) * ih[u]);
+    __syncwarp();
+    spline_solve_scan(I, m, sc);
     for (int k = lane; k < Na; k += 32) c[k] = (k == 0 || k == Na - 1) ? 0.0 : sc[k];
     __syncwarp();
 }

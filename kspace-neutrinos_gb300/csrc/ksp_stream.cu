@@ -1,0 +1,650 @@
+// ksp_stream.cu -- warp-pipelined streaming passes over the half-complex grid: the
+// binning pass (K1, powerspectrum.c:56-89) and the correction multiply (K3,
+// interface_gadget.c:163-188).
+//
+// Each warp is a pipeline of its own: it owns a ring of STAGES shared-memory tiles of
+// 32 rows x 16 modes (4 KB, 128-byte swizzle), its lane 0 keeps the ring full with 2-D
+// TMA loads (and, for K3, writes each corrected tile back with a TMA store), and no
+// barrier spans more than the warp.  A lane handles the 16 consecutive modes of one
+// row.  Along such a run k^2 grows with z, so the bin (K1) or the interpolation
+// segment (K3) can only step forward: each mode compares its integer k^2 with the next
+// threshold, and a crossing is a few predicated moves, not a divergent branch.  A run
+// starting below ksafe -- the k^2 under which some threshold gap is narrower than one
+// k^2 step (2z + 1 <= 2 sqrt(k^2) + 1), so that a step could cross two thresholds --
+// and a run that crosses the end of a grid row go to a warp-cooperative path instead,
+// one mode per lane (low k and row ends: a few percent of the runs).
+//
+// K1 per mode: |F|^2 and the window factor inv = (w1x w1y w1z)^2 rounded in float as
+// the reference forms them; the reference then multiplies |F|^2 inv^2 in double.  The
+// exact variant carries that product and the run sums as float pairs (TwoSum), so
+// the bin sums agree with the reference's double sums to ~1e-14; the lean variant
+// rounds the product to float and sums a run (at most 16 modes) in plain FP32.  Both
+// hand each closed run to the CTA's float-pair totals (compensated atomics) and the
+// CTA totals to the global FP64 sums once.
+#include <cuda.h>
+#include <cuda_runtime.h>
+#include <stdint.h>
+#include "ksp_internal.h"
+#include "ksp_gridutil.cuh"
+#include "ksp_ptx.cuh"
+
+namespace ksp {
+namespace {
+
+constexpr int kRowsPerWarp = 32;                // 16-mode rows per warp tile
+constexpr int kTileBytes = kRowsPerWarp * 128;  // 4 KB
+constexpr int kSpillSlots = 16;                 // bins a lane can close within one run
+constexpr unsigned kFull = 0xffffffffu;
+constexpr float kHalfLn2 = 0.34657359027997264f;
+
+struct StreamPlan {
+    size_t stage_off, bar_off, spill_off, hist_off, thr_off, tab_off, total;
+};
+
+// K1 shared memory (from a 1024-byte aligned base): stage rings | mbarriers | per-warp
+// spill slots | float-pair bin totals | bin thresholds | {w1[z], multiplicity(z)}
+__host__ __device__ inline StreamPlan plan_bin_stream(int warps, int stages, int nrbins, int nz, bool exact) {
+    StreamPlan p{};
+    size_t o = 0;
+    p.stage_off = o;
+    o += (size_t)warps * stages * kTileBytes;
+    p.bar_off = o;
+    o += sizeof(uint64_t) * (size_t)warps * stages;
+    o = (o + 15) & ~size_t(15);
+    p.spill_off = o;
+    o += (size_t)warps * kSpillSlots * 32 * (exact ? 8 : 4);
+    p.hist_off = o;
+    o += sizeof(float) * 2 * (size_t)nrbins;
+    p.thr_off = o;
+    o += sizeof(int) * (size_t)(nrbins + 1);
+    o = (o + 15) & ~size_t(15);
+    p.tab_off = o;
+    o += sizeof(float2) * (size_t)(nz + (nz >> 4) + 1);
+    p.total = o + 1024;  // alignment slack
+    return p;
+}
+
+// The z-window table is read at z, z+1, ..., z+15 by every lane at once, lanes 16 z
+// apart: one padding entry after every 16 (entry z at z + z/16) spreads a warp's reads
+// over all banks.
+__device__ __forceinline__ int wpad(int z) { return z + (z >> 4); }
+
+// K3 shared memory: stage rings | mbarriers | segments {x0, slope, value, next k^2} | k^2 thresholds
+__host__ __device__ inline StreamPlan plan_corr_stream(int warps, int stages, int nk) {
+    StreamPlan p{};
+    size_t o = 0;
+    p.stage_off = o;
+    o += (size_t)warps * stages * kTileBytes;
+    p.bar_off = o;
+    o += sizeof(uint64_t) * (size_t)warps * stages;
+    o = (o + 15) & ~size_t(15);
+    p.tab_off = o;
+    o += sizeof(float4) * (size_t)(nk + 1);
+    p.thr_off = o;
+    o += sizeof(int) * (size_t)(nk + 1);
+    p.total = o + 1024;
+    return p;
+}
+
+template <bool EXACT> struct SpillOf { typedef float type; };
+template <> struct SpillOf<true> { typedef float2 type; };
+
+// w |F|^2 inv^2 of one mode; w = {w1[z], multiplicity}, iwxy = w1x * w1y (float)
+template <bool EXACT>
+__device__ __forceinline__ void mode_value(float re, float im, float iwxy, float2 w, float& hi, float& lo) {
+    const float t = __fmul_rn(iwxy, w.x);
+    const float inv = __fmul_rn(t, t);
+    const float F2 = __fmul_rn(__fadd_rn(__fmul_rn(re, re), __fmul_rn(im, im)), w.y);
+    const float f_hi = __fmul_rn(inv, inv);
+    hi = __fmul_rn(F2, f_hi);
+    if (EXACT) {
+        const float f_lo = fmaf(inv, inv, -f_hi);
+        lo = fmaf(F2, f_lo, fmaf(F2, f_hi, -hi));
+    } else {
+        lo = 0.f;
+    }
+}
+
+// one mode of a fast run: close the current bin if k^2 reached the next threshold,
+// then add the mode to the (new) current bin
+template <bool EXACT>
+__device__ __forceinline__ void bin_step(float re, float im, float iwxy, float2 w, int& k2, int& d, int& tnext,
+                                         const int*& tq, typename SpillOf<EXACT>::type*& sp, float& h, float& l) {
+    float phi, plo;
+    mode_value<EXACT>(re, im, iwxy, w, phi, plo);
+    const bool c = k2 >= tnext;
+    if (c) {
+        if constexpr (EXACT) *sp = make_float2(h, l);
+        else *sp = h;
+        sp += 32;
+        ++tq;
+        tnext = *tq;
+    }
+    const float h0 = c ? 0.f : h;
+    if constexpr (EXACT) {
+        const float l0 = c ? 0.f : l;
+        const float s = __fadd_rn(h0, phi);
+        const float bb = __fsub_rn(s, h0);
+        const float e = __fadd_rn(__fsub_rn(h0, __fsub_rn(s, bb)), __fsub_rn(phi, bb));
+        h = s;
+        l = __fadd_rn(l0, __fadd_rn(e, plo));
+    } else {
+        h = __fadd_rn(h0, phi);
+    }
+    k2 += d;
+    d += 2;
+}
+
+__device__ __forceinline__ void add_pair(float* H, float* L, int b, float hi, float lo) {
+    if (hi != 0.f || lo != 0.f) pair_atomic_add(H, L, b, hi, lo);
+}
+
+// Segmented sums of float pairs over the lanes of a warp: each run of equal key (in
+// lane order) is summed, with error-free additions, onto its last lane (tail).
+__device__ __forceinline__ void warp_seg_pair(int key, float& h, float& l, bool& tail) {
+    const int lane = threadIdx.x & 31;
+    const int up = __shfl_up_sync(kFull, key, 1);
+    const unsigned heads = __ballot_sync(kFull, lane == 0 || up != key);
+    const int my_head = 31 - __clz(heads & (0xffffffffu >> (31 - lane)));
+#pragma unroll
+    for (int dd = 1; dd < 32; dd <<= 1) {
+        const float oh = __shfl_up_sync(kFull, h, dd), ol = __shfl_up_sync(kFull, l, dd);
+        if (lane - dd >= my_head) pair_add(h, l, oh, ol);
+    }
+    tail = lane == 31 || ((heads >> (lane + 1)) & 1u);
+}
+
+template <int WARPS, int STAGES, bool EXACT>
+__global__ void __launch_bounds__(WARPS * 32)
+    k_bin_stream(const __grid_constant__ CUtensorMap tmap, GridArgs g, const int* __restrict__ thresh,
+                 const float* __restrict__ w1g, const float* __restrict__ grid, double* bin_sum, double* F0sq,
+                 unsigned* status, long long ntiles, int adv_r, int adv_z) {
+    typedef typename SpillOf<EXACT>::type Spill;
+    extern __shared__ unsigned char sm_raw[];
+    __shared__ int s_gap;
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    const StreamPlan P = plan_bin_stream(WARPS, STAGES, g.nrbins, g.nz, EXACT);
+    unsigned char* base = sm_raw + ((1024 - (ptx::smem_u32(sm_raw) & 1023)) & 1023);
+    unsigned char* my_stage = base + P.stage_off + (size_t)warp * STAGES * kTileBytes;
+    uint64_t* my_bar = reinterpret_cast<uint64_t*>(base + P.bar_off) + warp * STAGES;
+    Spill* my_spill = reinterpret_cast<Spill*>(base + P.spill_off) + (size_t)warp * kSpillSlots * 32 + lane;
+    float* s_H = reinterpret_cast<float*>(base + P.hist_off);
+    float* s_L = s_H + g.nrbins;
+    int* s_thr = reinterpret_cast<int*>(base + P.thr_off);
+    float2* s_wt = reinterpret_cast<float2*>(base + P.tab_off);
+    for (int i = tid; i < 2 * g.nrbins; i += blockDim.x) s_H[i] = 0.f;
+    for (int i = tid; i <= g.nrbins; i += blockDim.x) s_thr[i] = thresh[i];
+    for (int i = tid; i < g.nz; i += blockDim.x)
+        s_wt[wpad(i)] = make_float2(w1g[i], (i == 0 || i == g.half) ? 1.f : 2.f);
+    if (tid == 0) s_gap = -1;
+    if (lane == 0) {
+        for (int s = 0; s < STAGES; s++) ptx::mbar_init(&my_bar[s], 1);
+        ptx::mbar_init_fence();
+    }
+    __syncthreads();
+    // ksafe: the lower threshold of the highest reachable gap narrower than a k^2 step
+    const int k2max = 3 * g.half * g.half;
+    for (int b = tid; b < g.nrbins - 1; b += blockDim.x) {
+        const int t0 = s_thr[b], t1 = s_thr[b + 1];
+        if (t1 <= k2max && (float)(t1 - t0) < 2.f * sqrtf((float)t0) + 3.f) atomicMax(&s_gap, b);
+    }
+    __syncthreads();
+    const int ksafe = s_gap >= 0 ? s_thr[s_gap] : 1;
+
+    const int gw = blockIdx.x * WARPS + warp;
+    const long long TW = (long long)gridDim.x * WARPS;
+    const long long my_n = gw < ntiles ? (ntiles - 1 - gw) / TW + 1 : 0;
+    if (lane == 0)
+        for (int s = 0; s < STAGES && s < my_n; s++) {
+            ptx::mbar_expect_tx(&my_bar[s], kTileBytes);
+            ptx::tma_load_2d(my_stage + s * kTileBytes, &tmap, &my_bar[s], 0, (int)((gw + s * TW) * kRowsPerWarp));
+        }
+    // first mode of the warp's current tile: grid row rb of the slab, z zb
+    const uint32_t mb = (uint32_t)gw * (kRowsPerWarp * 16);
+    int rb = (int)fdiv(mb, g.fd_nz);
+    int zb = (int)(mb - (uint32_t)rb * (uint32_t)g.nz);
+    bool ok = true;
+    long long k = 0;
+    int s = 0;
+    unsigned phase = 0;
+    for (; k < my_n; k++) {
+        const bool got = ptx::mbar_wait_bounded(&my_bar[s], phase);
+        if (!__all_sync(kFull, got)) {
+            ok = false;
+            break;
+        }
+        const unsigned char* tb = my_stage + s * kTileBytes;
+        const bool valid = (gw + k * TW) * kRowsPerWarp + lane < g.nrows16;
+        // this lane's run: 16 modes from z of grid row pr
+        const uint32_t o = (uint32_t)(zb + 16 * lane);
+        const uint32_t dr = fdiv(o, g.fd_nz);
+        const int z = (int)(o - dr * (uint32_t)g.nz);
+        const int pr = rb + (int)dr;
+        const int il = (int)fdiv((uint32_t)pr, g.fd_N);
+        const int kx = kval(g.slab0 + il, g.N), ky = kval(pr - il * g.N, g.N);
+        int k2 = kx * kx + ky * ky + z * z;
+        const bool fast = valid && z + 15 < g.nz && k2 >= ksafe;
+        if (fast) {
+            const float iwxy = __fmul_rn(s_wt[wpad(kx < 0 ? -kx : kx)].x, s_wt[wpad(ky < 0 ? -ky : ky)].x);
+            const float2* wz = s_wt + wpad(z);
+            const int cut = 16 - (z & 15);  // modes from z + cut on sit past one more padding entry
+            const int b = bin_of(k2, g.c1, s_thr, g.nrbins);
+            const int* tq = s_thr + b + 1;
+            int tnext = *tq;
+            Spill* sp = my_spill;
+            float h = 0.f, l = 0.f;
+            int d = 2 * z + 1;
+            const unsigned char* rp = tb + lane * 128;
+#pragma unroll
+            for (int u = 0; u < 8; u++) {
+                const float4 v = *reinterpret_cast<const float4*>(rp + ((u ^ (lane & 7)) << 4));
+                bin_step<EXACT>(v.x, v.y, iwxy, wz[2 * u + (2 * u >= cut)], k2, d, tnext, tq, sp, h, l);
+                bin_step<EXACT>(v.z, v.w, iwxy, wz[2 * u + 1 + (2 * u + 1 >= cut)], k2, d, tnext, tq, sp, h, l);
+            }
+            const int nsp = (int)(sp - my_spill) >> 5;
+            for (int q = 0; q < nsp; q++) {
+                const Spill v = my_spill[32 * q];
+                if constexpr (EXACT) add_pair(s_H, s_L, b + q, v.x, v.y);
+                else add_pair(s_H, s_L, b + q, v, 0.f);
+            }
+            add_pair(s_H, s_L, b + nsp, h, l);
+        }
+        // runs off the fast path: two at a time, one mode per lane
+        unsigned slow = __ballot_sync(kFull, valid && !fast);
+        while (slow) {
+            const int L0 = __ffs(slow) - 1;
+            slow &= slow - 1;
+            int L1 = -1;
+            if (slow) {
+                L1 = __ffs(slow) - 1;
+                slow &= slow - 1;
+            }
+            const int L = lane < 16 ? L0 : L1;
+            const int zL = __shfl_sync(kFull, z, L < 0 ? 0 : L);
+            const int pL = __shfl_sync(kFull, pr, L < 0 ? 0 : L);
+            int key = -1;
+            float phi = 0.f, plo = 0.f;
+            if (L >= 0) {
+                const int i = lane & 15;
+                int zz = zL + i, pp = pL;
+                while (zz >= g.nz) {
+                    zz -= g.nz;
+                    pp++;
+                }
+                const int il2 = (int)fdiv((uint32_t)pp, g.fd_N);
+                const int kx2 = kval(g.slab0 + il2, g.N), ky2 = kval(pp - il2 * g.N, g.N);
+                const int k2m = kx2 * kx2 + ky2 * ky2 + zz * zz;
+                if (k2m != 0) {
+                    const float2 v = *reinterpret_cast<const float2*>(tb + L * 128 + (((i >> 1) ^ (L & 7)) << 4) +
+                                                                      (i & 1) * 8);
+                    const float iw =
+                        __fmul_rn(s_wt[wpad(kx2 < 0 ? -kx2 : kx2)].x, s_wt[wpad(ky2 < 0 ? -ky2 : ky2)].x);
+                    mode_value<EXACT>(v.x, v.y, iw, s_wt[wpad(zz)], phi, plo);
+                    key = bin_of(k2m, g.c1, s_thr, g.nrbins);
+                }
+            }
+            // consecutive modes mostly share a bin: one shared-memory update per run
+            bool tail;
+            warp_seg_pair(key, phi, plo, tail);
+            if (tail && key >= 0) add_pair(s_H, s_L, key, phi, plo);
+        }
+        __syncwarp();
+        if (lane == 0 && k + STAGES < my_n) {
+            ptx::mbar_expect_tx(&my_bar[s], kTileBytes);
+            ptx::tma_load_2d(my_stage + s * kTileBytes, &tmap, &my_bar[s], 0,
+                             (int)((gw + (k + STAGES) * TW) * kRowsPerWarp));
+        }
+        if (++s == STAGES) {
+            s = 0;
+            phase ^= 1;
+        }
+        zb += adv_z;
+        rb += adv_r;
+        if (zb >= g.nz) {
+            zb -= g.nz;
+            rb++;
+        }
+    }
+    if (!ok && lane == 0) {
+        // wait (bounded) for this warp's loads still in flight, then leave the tiles
+        atomicOr(status, kStTimeout);
+        for (long long kk = k; kk < my_n && kk < k + STAGES; kk++) {
+            ptx::mbar_wait_bounded(&my_bar[s], phase);
+            if (++s == STAGES) {
+                s = 0;
+                phase ^= 1;
+            }
+        }
+    }
+    __syncthreads();
+    if (blockIdx.x == 0 && tid == 0) {
+        // the modes after the last full 16-mode row
+        for (long long m = g.nrows16 * 16; m < g.nmodes; m++) {
+            const long long rr = m / g.nz;
+            const int zz = (int)(m - rr * g.nz);
+            const int il2 = (int)(rr / g.N);
+            const int kx2 = kval(g.slab0 + il2, g.N), ky2 = kval((int)(rr - (long long)il2 * g.N), g.N);
+            const int k2m = kx2 * kx2 + ky2 * ky2 + zz * zz;
+            if (k2m == 0) continue;
+            const float iw = __fmul_rn(s_wt[wpad(kx2 < 0 ? -kx2 : kx2)].x, s_wt[wpad(ky2 < 0 ? -ky2 : ky2)].x);
+            float phi, plo;
+            mode_value<EXACT>(grid[2 * m], grid[2 * m + 1], iw, s_wt[wpad(zz)], phi, plo);
+            add_pair(s_H, s_L, bin_of(k2m, g.c1, s_thr, g.nrbins), phi, plo);
+        }
+        if (g.slab0 == 0 && g.nmodes > 0) {
+            const float re = grid[0], im = grid[1];
+            *F0sq = (double)__fadd_rn(__fmul_rn(re, re), __fmul_rn(im, im));
+        }
+    }
+    __syncthreads();
+    for (int b = tid; b < g.nrbins; b += blockDim.x) {
+        const double v = (double)s_H[b] + (double)s_L[b];
+        if (v != 0.0) atomicAdd(bin_sum + b, v);
+    }
+}
+
+// ------------------------------------------------------------------ K3
+// one mode of a fast run: step to the next segment if k^2 reached its start, then
+// multiply by 1 + (value + slope (log k - x0))
+__device__ __forceinline__ void corr_step(float& re, float& im, int& k2, int& d, int& tnext, const float4*& sq,
+                                          float4& cs, float lnscale) {
+    if (k2 >= tnext) {
+        ++sq;
+        cs = *sq;
+        tnext = __float_as_int(cs.w);
+    }
+    const float x = fmaf(__log2f((float)k2), kHalfLn2, lnscale);
+    const float f = fmaf(x - cs.x, cs.y, cs.z);
+    re = fmaf(re, f, re);
+    im = fmaf(im, f, im);
+    k2 += d;
+    d += 2;
+}
+
+// segment of k^2: the number of node thresholds at or below it
+__device__ __forceinline__ int seg_of(int k2, const int* k2t, int nk) {
+    int lo = 0, hi = nk;
+    while (lo < hi) {
+        const int mid = (lo + hi) >> 1;
+        if (k2t[mid] <= k2) lo = mid + 1;
+        else hi = mid;
+    }
+    return lo;
+}
+
+template <int WARPS, int STAGES>
+__global__ void __launch_bounds__(WARPS * 32)
+    k_correct_stream(const __grid_constant__ CUtensorMap tmap, GridArgs g, CorrTable corr, float* grid,
+                     unsigned* status, long long ntiles, int adv_r, int adv_z) {
+    extern __shared__ unsigned char sm_raw[];
+    __shared__ int s_gap;
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    const int nk = g.nk;
+    const StreamPlan P = plan_corr_stream(WARPS, STAGES, nk);
+    unsigned char* base = sm_raw + ((1024 - (ptx::smem_u32(sm_raw) & 1023)) & 1023);
+    unsigned char* my_stage = base + P.stage_off + (size_t)warp * STAGES * kTileBytes;
+    uint64_t* my_bar = reinterpret_cast<uint64_t*>(base + P.bar_off) + warp * STAGES;
+    float4* s_seg = reinterpret_cast<float4*>(base + P.tab_off);
+    int* s_k2t = reinterpret_cast<int*>(base + P.thr_off);
+    // segment s covers k^2 in [k2t[s-1], k2t[s]): s = 0 below the first node (value of
+    // node 0), 1..nk-1 the linear pieces between nodes, nk from the last node on (its
+    // value) -- the clamped interpolation of delta_pow.c:19-37 in log k.  k2t[j]: the
+    // first integer k^2 whose log k reaches node j.
+    for (int j = tid; j < nk; j += blockDim.x) {
+        const float e = expf(2.f * (corr.xf[j] - g.lnscale));
+        int t = e >= 1.0e9f ? 1000000000 : (int)ceilf(e);
+        s_k2t[j] = t < 1 ? 1 : t;
+    }
+    if (tid == 0) {
+        s_k2t[nk] = 0x7fffffff;
+        s_gap = -1;
+    }
+    if (lane == 0) {
+        for (int s = 0; s < STAGES; s++) ptx::mbar_init(&my_bar[s], 1);
+        ptx::mbar_init_fence();
+    }
+    __syncthreads();
+    for (int s = tid; s <= nk; s += blockDim.x) {
+        float4 v;
+        if (s == 0) v = make_float4(0.f, 0.f, corr.rn[0], 0.f);
+        else if (s == nk) v = make_float4(0.f, 0.f, corr.rn[nk - 1], 0.f);
+        else v = make_float4(corr.xf[s - 1], corr.sn[s - 1], corr.rn[s - 1], 0.f);
+        v.w = __int_as_float(s_k2t[s]);
+        s_seg[s] = v;
+    }
+    const int k2max = 3 * g.half * g.half;
+    for (int j = tid; j < nk - 1; j += blockDim.x) {
+        const int t0 = s_k2t[j], t1 = s_k2t[j + 1];
+        if (t1 <= k2max && (float)(t1 - t0) < 2.f * sqrtf((float)t0) + 3.f) atomicMax(&s_gap, j);
+    }
+    __syncthreads();
+    const int ksafe = s_gap >= 0 ? s_k2t[s_gap] : 1;
+    const float xwarn = corr.xf[0] - 0.69314718f;
+
+    const int gw = blockIdx.x * WARPS + warp;
+    const long long TW = (long long)gridDim.x * WARPS;
+    const long long my_n = gw < ntiles ? (ntiles - 1 - gw) / TW + 1 : 0;
+    if (lane == 0)
+        for (int s = 0; s < STAGES - 1 && s < my_n; s++) {
+            ptx::mbar_expect_tx(&my_bar[s], kTileBytes);
+            ptx::tma_load_2d(my_stage + s * kTileBytes, &tmap, &my_bar[s], 0, (int)((gw + s * TW) * kRowsPerWarp));
+        }
+    const uint32_t mb = (uint32_t)gw * (kRowsPerWarp * 16);
+    int rb = (int)fdiv(mb, g.fd_nz);
+    int zb = (int)(mb - (uint32_t)rb * (uint32_t)g.nz);
+    unsigned flags = 0;
+    bool ok = true;
+    long long k = 0;
+    int s = 0, s2 = STAGES - 1;  // stage of tile k, and of tile k + STAGES - 1
+    unsigned phase = 0;
+    for (; k < my_n; k++) {
+        const long long tile = gw + k * TW;
+        const bool got = ptx::mbar_wait_bounded(&my_bar[s], phase);
+        if (!__all_sync(kFull, got)) {
+            ok = false;
+            break;
+        }
+        unsigned char* tb = my_stage + s * kTileBytes;
+        const bool valid = tile * kRowsPerWarp + lane < g.nrows16;
+        const uint32_t o = (uint32_t)(zb + 16 * lane);
+        const uint32_t dr = fdiv(o, g.fd_nz);
+        const int z = (int)(o - dr * (uint32_t)g.nz);
+        const int pr = rb + (int)dr;
+        const int il = (int)fdiv((uint32_t)pr, g.fd_N);
+        const int kx = kval(g.slab0 + il, g.N), ky = kval(pr - il * g.N, g.N);
+        int k2 = kx * kx + ky * ky + z * z;
+        const bool fast = valid && z + 15 < g.nz && k2 >= ksafe;
+        if (fast) {
+            const float4* sq = s_seg + seg_of(k2, s_k2t, nk);
+            // log k grows along the run: only its first mode can be far below node 0
+            if (sq == s_seg && fmaf(__log2f((float)k2), kHalfLn2, g.lnscale) < xwarn) flags |= kStKWarn;
+            float4 cs = *sq;
+            int tnext = __float_as_int(cs.w);
+            int d = 2 * z + 1;
+            unsigned char* rp = tb + lane * 128;
+#pragma unroll
+            for (int u = 0; u < 8; u++) {
+                float4* vp = reinterpret_cast<float4*>(rp + ((u ^ (lane & 7)) << 4));
+                float4 v = *vp;
+                corr_step(v.x, v.y, k2, d, tnext, sq, cs, g.lnscale);
+                corr_step(v.z, v.w, k2, d, tnext, sq, cs, g.lnscale);
+                *vp = v;
+            }
+        }
+        unsigned slow = __ballot_sync(kFull, valid && !fast);
+        while (slow) {
+            const int L0 = __ffs(slow) - 1;
+            slow &= slow - 1;
+            int L1 = -1;
+            if (slow) {
+                L1 = __ffs(slow) - 1;
+                slow &= slow - 1;
+            }
+            const int L = lane < 16 ? L0 : L1;
+            const int zL = __shfl_sync(kFull, z, L < 0 ? 0 : L);
+            const int pL = __shfl_sync(kFull, pr, L < 0 ? 0 : L);
+            if (L >= 0) {
+                const int i = lane & 15;
+                int zz = zL + i, pp = pL;
+                while (zz >= g.nz) {
+                    zz -= g.nz;
+                    pp++;
+                }
+                const int il2 = (int)fdiv((uint32_t)pp, g.fd_N);
+                const int kx2 = kval(g.slab0 + il2, g.N), ky2 = kval(pp - il2 * g.N, g.N);
+                const int k2m = kx2 * kx2 + ky2 * ky2 + zz * zz;
+                if (k2m != 0) {
+                    float2* vp = reinterpret_cast<float2*>(tb + L * 128 + (((i >> 1) ^ (L & 7)) << 4) + (i & 1) * 8);
+                    const float x = fmaf(__log2f((float)k2m), kHalfLn2, g.lnscale);
+                    const int sg = seg_of(k2m, s_k2t, nk);
+                    const float4 cs = s_seg[sg];
+                    if (x < xwarn) flags |= kStKWarn;
+                    const float f = fmaf(x - cs.x, cs.y, cs.z);
+                    float2 v = *vp;
+                    v.x = fmaf(v.x, f, v.x);
+                    v.y = fmaf(v.y, f, v.y);
+                    *vp = v;
+                }
+            }
+        }
+        ptx::fence_async_smem();
+        __syncwarp();
+        if (lane == 0) {
+            ptx::tma_store_2d(&tmap, tb, 0, (int)(tile * kRowsPerWarp));
+            ptx::bulk_commit();
+            if (k + STAGES - 1 < my_n) {
+                ptx::bulk_wait_read_le1();  // the store from stage s2 (one tile ago) has read it
+                ptx::mbar_expect_tx(&my_bar[s2], kTileBytes);
+                ptx::tma_load_2d(my_stage + s2 * kTileBytes, &tmap, &my_bar[s2], 0,
+                                 (int)((gw + (k + STAGES - 1) * TW) * kRowsPerWarp));
+            }
+        }
+        if (++s == STAGES) {
+            s = 0;
+            phase ^= 1;
+        }
+        if (++s2 == STAGES) s2 = 0;
+        zb += adv_z;
+        rb += adv_r;
+        if (zb >= g.nz) {
+            zb -= g.nz;
+            rb++;
+        }
+    }
+    if (lane == 0) {
+        if (!ok) {
+            atomicOr(status, kStTimeout);
+            for (long long kk = k; kk < my_n && kk < k + STAGES - 1; kk++) {
+                ptx::mbar_wait_bounded(&my_bar[s], phase);
+                if (++s == STAGES) {
+                    s = 0;
+                    phase ^= 1;
+                }
+            }
+        }
+        ptx::bulk_wait_all();
+    }
+    if (blockIdx.x == 0 && tid == 0) {
+        // the modes after the last full 16-mode row
+        for (long long m = g.nrows16 * 16; m < g.nmodes; m++) {
+            const long long rr = m / g.nz;
+            const int zz = (int)(m - rr * g.nz);
+            const int il2 = (int)(rr / g.N);
+            const int kx2 = kval(g.slab0 + il2, g.N), ky2 = kval((int)(rr - (long long)il2 * g.N), g.N);
+            const int k2m = kx2 * kx2 + ky2 * ky2 + zz * zz;
+            if (k2m == 0) continue;
+            const float x = fmaf(__log2f((float)k2m), kHalfLn2, g.lnscale);
+            const float4 cs = s_seg[seg_of(k2m, s_k2t, nk)];
+            if (x < xwarn) flags |= kStKWarn;
+            const float f = fmaf(x - cs.x, cs.y, cs.z);
+            grid[2 * m] = fmaf(grid[2 * m], f, grid[2 * m]);
+            grid[2 * m + 1] = fmaf(grid[2 * m + 1], f, grid[2 * m + 1]);
+        }
+    }
+    if (flags) atomicOr(status, flags);
+}
+
+int sm_count_s() {
+    static int n = 0;
+    if (!n) {
+        int dev = 0;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev);
+        if (n <= 0) n = 1;
+    }
+    return n;
+}
+
+// grid size and the per-iteration advance of a warp's tile start (TW tiles)
+template <typename K>
+bool stream_grid(K kern, int warps, size_t smem, long long ntiles, int nz, int& grid_n, int& adv_r, int& adv_z) {
+    cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    int per_sm = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, warps * 32, smem) != cudaSuccess || per_sm < 1)
+        return false;
+    long long n = (long long)sm_count_s() * per_sm;
+    const long long need = (ntiles + warps - 1) / warps;
+    if (n > need) n = need > 0 ? need : 1;
+    grid_n = (int)n;
+    const long long adv = n * warps * kRowsPerWarp * 16;
+    adv_r = (int)(adv / nz);
+    adv_z = (int)(adv % nz);
+    return true;
+}
+
+template <int WARPS, int STAGES, bool EXACT>
+int run_bin_stream(const GridGeom& g, const GridArgs& a, const float* grid, double* bin_sum, double* F0sq,
+                   unsigned* status, cudaStream_t st) {
+    CUtensorMap map;
+    if (!make_grid_tmap(&map, grid, a.nrows16, kRowsPerWarp)) return -1;
+    const StreamPlan P = plan_bin_stream(WARPS, STAGES, g.nrbins, a.nz, EXACT);
+    if (P.total > 220 * 1024) return -1;
+    auto kern = k_bin_stream<WARPS, STAGES, EXACT>;
+    const long long ntiles = (a.nrows16 + kRowsPerWarp - 1) / kRowsPerWarp;
+    int grid_n = 1, adv_r = 0, adv_z = 0;
+    if (!stream_grid(kern, WARPS, P.total, ntiles, a.nz, grid_n, adv_r, adv_z)) return -1;
+    kern<<<grid_n, WARPS * 32, P.total, st>>>(map, a, g.thresh, g.w1, grid, bin_sum, F0sq, status, ntiles, adv_r,
+                                              adv_z);
+    return cudaPeekAtLastError() == cudaSuccess ? 0 : -2;
+}
+
+template <int WARPS, int STAGES>
+int run_corr_stream(const GridArgs& a, float* grid, CorrTable corr, unsigned* status, cudaStream_t st) {
+    CUtensorMap map;
+    if (!make_grid_tmap(&map, grid, a.nrows16, kRowsPerWarp)) return -1;
+    const StreamPlan P = plan_corr_stream(WARPS, STAGES, a.nk);
+    if (P.total > 220 * 1024) return -1;
+    auto kern = k_correct_stream<WARPS, STAGES>;
+    const long long ntiles = (a.nrows16 + kRowsPerWarp - 1) / kRowsPerWarp;
+    int grid_n = 1, adv_r = 0, adv_z = 0;
+    if (!stream_grid(kern, WARPS, P.total, ntiles, a.nz, grid_n, adv_r, adv_z)) return -1;
+    kern<<<grid_n, WARPS * 32, P.total, st>>>(map, a, corr, grid, status, ntiles, adv_r, adv_z);
+    return cudaPeekAtLastError() == cudaSuccess ? 0 : -2;
+}
+
+}  // namespace
+
+int launch_bin_stream(const GridGeom& g, const GridArgs& a, const float* grid, double* bin_sum, double* F0sq,
+                      unsigned* status, int warps, int stages, bool exact, cudaStream_t st) {
+    if (a.nrows16 <= 0 || a.N >= 32768) return -1;
+#define KSP_BS(W, S)                                                                              \
+    if (warps == W && stages == S)                                                                \
+        return exact ? run_bin_stream<W, S, true>(g, a, grid, bin_sum, F0sq, status, st)          \
+                     : run_bin_stream<W, S, false>(g, a, grid, bin_sum, F0sq, status, st);
+    KSP_BS(4, 2) KSP_BS(4, 3) KSP_BS(4, 4) KSP_BS(8, 2) KSP_BS(8, 3) KSP_BS(8, 4)
+#undef KSP_BS
+    return exact ? run_bin_stream<8, 2, true>(g, a, grid, bin_sum, F0sq, status, st)
+                 : run_bin_stream<8, 2, false>(g, a, grid, bin_sum, F0sq, status, st);
+}
+
+int launch_correct_stream(const GridArgs& a, float* grid, CorrTable corr, unsigned* status, int warps, int stages,
+                          cudaStream_t st) {
+    if (a.nrows16 <= 0 || a.nk < 2 || a.N >= 32768) return -1;
+#define KSP_CS(W, S) \
+    if (warps == W && stages == S) return run_corr_stream<W, S>(a, grid, corr, status, st);
+    KSP_CS(4, 2) KSP_CS(4, 3) KSP_CS(4, 4) KSP_CS(8, 2) KSP_CS(8, 3) KSP_CS(8, 4)
+#undef KSP_CS
+    return run_corr_stream<8, 2>(a, grid, corr, status, st);
+}
+
+}  // namespace ksp

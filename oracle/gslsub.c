@@ -266,18 +266,31 @@ void gslsub_qag_counters(long long *calls, long long *intervals)
 /* rule applications by depth in the bisection tree of [a, b] (diagnostics) */
 static long long g_depth_rules[32];
 static double g_depth_a, g_depth_w;
+static long long g_slot_rules[255];
 static void count_rule(double lo, double hi)
 {
     const double r = g_depth_w / (hi - lo);
     int d = 0;
     while (d < 31 && r > 1.5 * (double)(1LL << d)) d++;
     g_depth_rules[d]++;
+    if (d < 8) {
+        const int p = (int)floor((lo - g_depth_a) / (hi - lo) + 0.5);
+        const int s = (1 << d) - 1 + p;
+        if (s >= 0 && s < 255) g_slot_rules[s]++;
+    }
 }
 void gslsub_depth_rules(long long *out32, int reset)
 {
     for (int i = 0; i < 32; i++) {
         out32[i] = g_depth_rules[i];
         if (reset) g_depth_rules[i] = 0;
+    }
+}
+void gslsub_slot_rules(long long *out255, int reset)
+{
+    for (int i = 0; i < 255; i++) {
+        out255[i] = g_slot_rules[i];
+        if (reset) g_slot_rules[i] = 0;
     }
 }
 void gslsub_reset_counters(void) { g_total_qag_calls = 0; g_total_qag_intervals = 0; }

@@ -1,0 +1,111 @@
+"""The warp-pipelined grid passes -- the default binning (K1) and correction (K3)
+kernels -- over their tile shapes and both binning variants, against the oracle:
+whole grids and slab ranges, grid sizes whose 16-mode rows straddle grid rows or
+leave a partial last tile, and low-k regions that take the cooperative path.
+
+Bars: mode counts bit-exact; the exact binning variant within 1e-12 of the oracle's
+double sums (it carries the reference's double product and sums as float pairs); the
+lean variant (FP32 run sums) within the 1e-6 bar for P(k); the corrected grid within
+1e-6 relative."""
+import math
+
+import numpy as np
+import pytest
+
+import cases
+import workloads as W
+
+pytestmark = pytest.mark.gpu
+
+L_BOX = 512.0
+SHAPES = [(256, 2), (256, 3), (128, 2), (128, 4)]  # rows per CTA (32 per warp), stages per warp
+TOL_EXACT = 1e-12
+TOL_LEAN = 1e-6
+
+
+def _instance(gpu, nb):
+    k = gpu.KspaceNeutrinos()
+    k.init_omega_nu((0.1, 0.1, 0.1), 0.01, 0.7)
+    k.alloc_table(max(nb, 16), 0.01, 1.0, 0.3, cases.UT, cases.UL)
+    return k
+
+
+@pytest.mark.parametrize("N,nb", [(16, 15), (64, 48), (96, 80), (128, 128), (256, 200)])
+def test_binning_stream_variants(gpu, oracle, N, nb):
+    import torch
+    g = W.make_grid(N, seed=100 + N)
+    nk_o, p_o, c_o, _ = oracle.total_powerspectrum(g, N, nb)
+    k = _instance(gpu, nb)
+    gd = torch.as_tensor(g).cuda()
+    worst = {3: 0.0, 4: 0.0}
+    for rows, stages in SHAPES:
+        for tma, tol in ((3, TOL_EXACT), (4, TOL_LEAN)):
+            k.set_tuning(tma=tma, rows=rows, stages=stages)
+            nk_g, p_g, c_g, _ = k.total_powerspectrum(N, gd, nb)
+            assert nk_g == nk_o
+            assert np.array_equal(c_g, c_o)
+            err = cases.rel_err(p_g, p_o)
+            worst[tma] = max(worst[tma], err)
+            assert err < tol, (rows, stages, tma, err)
+    # the CTA-tiled kernel of the same pass agrees too
+    k.set_tuning(tma=1, rows=128, stages=2)
+    _, p_1, _, _ = k.total_powerspectrum(N, gd, nb)
+    assert cases.rel_err(p_1, p_o) < TOL_EXACT
+    k.close()
+    print("N=%d worst P error: exact %.2e lean %.2e" % (N, worst[3], worst[4]))
+
+
+@pytest.mark.parametrize("N,nb,cuts", [(96, 64, (0, 37, 96)), (128, 100, (0, 1, 64, 127, 128))])
+def test_binning_stream_slabs(gpu, oracle, N, nb, cuts):
+    """Per-slab bin sums through the allocation-free entry point (the same kernel)."""
+    import torch
+    lib = gpu.load_library()
+    g = W.make_grid(N, seed=7 + N)
+    for s0, s1 in zip(cuts[:-1], cuts[1:]):
+        gs = np.ascontiguousarray(g[s0:s1])
+        po, _, _, fo = oracle.total_powerspectrum(gs, N, nb, startslab=s0, nslab=s1 - s0, partial=True)
+        gd = torch.as_tensor(gs).cuda()
+        sums = np.full(nb + 1, np.nan)
+        st = lib.kspace_gpu_bin_power_noalloc(N, gd.data_ptr(), nb, s0, s1 - s0, sums.ctypes.data, None)
+        assert st == 0, st
+        assert np.array_equal(sums[:nb] == 0, po == 0)
+        m = po != 0
+        assert cases.rel_err(sums[:nb][m], po[m]) < TOL_EXACT, (s0, s1)
+        if s0 == 0:
+            assert sums[nb] == fo
+
+
+def _table(N, nb):
+    count, keff = W.geometry(N, nb)
+    kph = keff[count > 0] * 2 * math.pi / L_BOX
+    ratio = 0.4 / (1.0 + (kph / 0.05) ** 2) + 0.01 * np.sin(7 * np.log(kph))
+    return np.log(kph), ratio, 0.37
+
+
+@pytest.mark.parametrize("N,nb", [(16, 15), (64, 48), (96, 80), (128, 100)])
+def test_correction_stream_variants(gpu, oracle, N, nb):
+    import torch
+    logk, ratio, norm = _table(N, nb)
+    g = W.make_grid(N, seed=300 + N)
+    go = g.copy()
+    assert oracle.apply_correction(go, N, 0, N, L_BOX, logk, ratio, norm) == 0
+    k = _instance(gpu, nb)
+    for tma, (rows, stages) in [(3, s) for s in SHAPES] + [(1, (128, 2))]:
+        k.set_tuning(tma=tma, rows=rows, stages=stages)
+        gd = torch.as_tensor(g).cuda()
+        k.apply_delta_pow(L_BOX, gd, N, nb, logk, ratio, norm)
+        gg = gd.cpu().numpy()
+        rel = np.abs(gg - go) / np.maximum(np.abs(go), 1e-30)
+        assert rel.max() < 1e-6, (tma, rows, stages, rel.max())
+    # slab ranges
+    k.set_tuning(tma=3, rows=256, stages=2)
+    cuts = (0, 5, N // 2, N)
+    for s0, s1 in zip(cuts[:-1], cuts[1:]):
+        gs = np.ascontiguousarray(g[s0:s1])
+        gos = gs.copy()
+        assert oracle.apply_correction(gos, N, s0, s1 - s0, L_BOX, logk, ratio, norm) == 0
+        gd = torch.as_tensor(gs).cuda()
+        k.apply_delta_pow(L_BOX, gd, N, nb, logk, ratio, norm, slabstart_y=s0, nslab_y=s1 - s0)
+        rel = np.abs(gd.cpu().numpy() - gos) / np.maximum(np.abs(gos), 1e-30)
+        assert rel.max() < 1e-6, (s0, s1, rel.max())
+    k.close()
