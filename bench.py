@@ -205,8 +205,9 @@ def run_gb300(args, cfg):
     k1_ms, k2_ms, k3_ms = stage[0] / args.steps, stage[1] / args.steps, stage[2] / args.steps
     k1_gbs = bytes_grid / (k1_ms * 1e-3) / 1e9 if k1_ms > 0 else None
     k3_gbs = 2 * bytes_grid / (k3_ms * 1e-3) / 1e9 if k3_ms > 0 else None
-    tma = int(os.environ.get("KSPACE_GPU_TMA", "3"))
-    k1_name, k3_name = ("k_bin_stream", "k_correct_stream") if tma >= 3 else ("k_bin_power_tma", "k_correct_tma")
+    tma = int(os.environ.get("KSPACE_GPU_TMA", "5"))
+    k1_name = "k_bin_rows" if tma >= 5 else ("k_bin_stream" if tma >= 3 else "k_bin_power_tma")
+    k3_name = "k_correct_stream" if tma >= 3 else "k_correct_tma"
     if k3_ms >= k1_ms:
         dom = {"kernel": k3_name + " (grid multiply)", "bytes": 2 * bytes_grid, "ms": k3_ms, "gbs": k3_gbs}
     else:

@@ -61,9 +61,14 @@ const char *kspace_gpu_error_string(int status);
 int kspace_gpu_set_stream(kspace_ctx *ctx, void *cuda_stream);
 /* Multi-rank slab decomposition: reduction of the per-bin sums (NULL = one rank). */
 int kspace_gpu_set_allreduce(kspace_ctx *ctx, kspace_allreduce_fn fn, void *user);
-/* Kernel variant selection: tma (1 = TMA tile engine with a thread per 16-mode row,
- * 2 = two threads per row, 0 = plain loads), rows per CTA (128/256), pipeline stages
- * (2/3/4), warps per block of the integrator (1..4).  Values < 0 (rows, stages,
+/* Kernel variant selection for the grid passes.  tma: 5 (default) = binning over
+ * row-aligned runs of 17 modes (whole grid rows per bulk copy) with the reference's float
+ * roundings and float-pair sums, 6 = the same with FP32 run sums; 3 / 4 = warp-pipelined
+ * binning over 16-mode TMA rows (exact / FP32 run sums); 1 = CTA-tiled TMA engine with a
+ * thread per 16-mode row, 2 = two threads per row; 0 = plain loads.  The correction pass
+ * is warp-pipelined for tma >= 3.  rows_per_cta: 32 x warps per CTA for tma >= 3
+ * (128/256); stages: per warp (or tile group) for tma >= 3 (2/3/4), per CTA otherwise;
+ * qag_warps: warps per block of the integrator (1..4).  Values < 0 (rows, stages,
  * qag_warps: <= 0) keep the current setting. */
 int kspace_gpu_set_tuning(kspace_ctx *ctx, int tma, int rows_per_cta, int stages, int qag_warps);
 

@@ -385,7 +385,7 @@ __device__ __forceinline__ void adj_interval(const DnuIntegrandC& fi, const Gk61
                 cb = u * (dx * (-hh / 3) + dx * dx * dx / (3 * hh));
             }
             key = t.j;
-            mder += ckm * wt * t.g * Jd * t.fsl * dnu_S(t, row, rc, Na, fi.ks);
+            mder += ckm * wt * t.g * Jd * t.fsl * dnu_S_poly(t, row, rc, fi.sb, fi.sd, Na, fi.ks);
         }
         bool tail;
         warp_seg_sum4(key, ya, yb, ca, cb, tail);
@@ -398,7 +398,8 @@ __device__ __forceinline__ void adj_interval(const DnuIntegrandC& fi, const Gk61
     }
 }
 
-// Shared memory per CTA: Gk61Nodes | knots[ld] | per warp: QagList, row[ld], coef[ld], ybar[ld], cbar[ld] | bars
+// Shared memory per CTA: Gk61Nodes | knots[ld] | per warp: QagList, row[ld], coef[ld], ybar[ld], cbar[ld],
+// seg_poly [2 ld] | bars
 __global__ void __launch_bounds__(128) k_dnu_adj(IntegratorDev I, DnuAdjArgs A, int nk, int Na, int nspec,
                                                  int4 spec_ids) {
     extern __shared__ __align__(16) unsigned char sm[];
@@ -407,13 +408,15 @@ __global__ void __launch_bounds__(128) k_dnu_adj(IntegratorDev I, DnuAdjArgs A, 
     double* knots = reinterpret_cast<double*>(sm + off);
     off += sizeof(double) * I.ld;
     const int nw = blockDim.x >> 5, warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    const size_t per_warp = sizeof(QagList) + 4 * sizeof(double) * I.ld;
+    const size_t per_warp = sizeof(QagList) + 6 * sizeof(double) * I.ld;
     unsigned char* wbase = sm + off + warp * per_warp;
     QagList& L = *reinterpret_cast<QagList*>(wbase);
     double* row = reinterpret_cast<double*>(wbase + sizeof(QagList));
     double* rc = row + I.ld;
     double* ybar = rc + I.ld;
     double* cbar = ybar + I.ld;
+    double* sb = cbar + I.ld;
+    double* sd = sb + I.ld;
     uint64_t* bars = reinterpret_cast<uint64_t*>(sm + off + nw * per_warp);
     uint64_t* mybar = bars + warp;
     gk61_fill(N, threadIdx.x, blockDim.x);
@@ -467,6 +470,9 @@ __global__ void __launch_bounds__(128) k_dnu_adj(IntegratorDev I, DnuAdjArgs A, 
                 mbar_wait_bounded_a(mybar, phase ^ 1);
                 return;
             }
+            const KnotSeg ks{I.knot_invh, I.knot_h3, I.knot_ih3};
+            if (Na > 2) seg_poly(row, rc, Na, ks, sb, sd, lane, 32);
+            __syncwarp();
             const double qc = S.partnu_now > 0 ? B->vcrit * mnubykT : 0.0;
             const double fs_inv = (S.Nfs - 1.) / (S.loga - S.loga0);
             // the final subdivision of the forward QAG: stored, or recomputed (same decisions)
@@ -476,11 +482,11 @@ __global__ void __launch_bounds__(128) k_dnu_adj(IntegratorDev I, DnuAdjArgs A, 
                 nint = A.nivals[(size_t)mi * I.nk_alloc + ik];
                 iv = A.ivals + ((size_t)mi * I.nk_alloc + ik) * kQagLimit * 2;
             } else {
-                const DnuIntegrandC f = dnu_integrand(I, S, k, mnubykT, qc, knots, row, rc, Na);
+                const DnuIntegrandC f = dnu_integrand(I, S, k, mnubykT, qc, knots, row, rc, sb, sd, Na);
                 QagResult r = qag_warp_c(f, N, L, S.loga0, S.loga, 0.0, S.relerr, kQagLimit);
                 nint = r.nint;
             }
-            const DnuIntegrandC fi = dnu_integrand(I, S, k, mnubykT, qc, knots, row, rc, Na);
+            const DnuIntegrandC fi = dnu_integrand(I, S, k, mnubykT, qc, knots, row, rc, sb, sd, Na);
             const double ckm = -sbar * S.prefac * fi.k_over_m / mnu;  // d(J's argument)/dm per fsl
             for (int q = 0; q < nint; q++)
                 adj_interval(fi, N, knots, row, rc, Na, qc, iv ? iv[2 * q] : L.a[q], iv ? iv[2 * q + 1] : L.b[q],
@@ -572,10 +578,10 @@ __global__ void k_adj_grid_plain(GridArgs g, const int* __restrict__ thresh, con
 // sums as the forward pass's block kernel) or read back; its intervals are dealt out
 // to the warps, each warp scatters into its own copy of the row cotangents, and the
 // copies are summed before the transposed spline solve.
-// Shared memory: Gk61Nodes | knots, row, coef [ld] | QagList | QagBlockSmem | per warp
+// Shared memory: Gk61Nodes | knots, row, coef, seg_poly [5 ld] | QagList | QagBlockSmem | per warp
 // ybar[ld], cbar[ld] | mbarrier
 size_t dnu_adj_blk_smem(int ld, int nw) {
-    return ((sizeof(Gk61Nodes) + 15) & ~size_t(15)) + 3 * sizeof(double) * ld + ((sizeof(QagList) + 15) & ~size_t(15)) +
+    return ((sizeof(Gk61Nodes) + 15) & ~size_t(15)) + 5 * sizeof(double) * ld + ((sizeof(QagList) + 15) & ~size_t(15)) +
            ((sizeof(QagBlockSmem) + 15) & ~size_t(15)) + (size_t)nw * 2 * sizeof(double) * ld + 16;
 }
 
@@ -588,7 +594,9 @@ __global__ void __launch_bounds__(128) k_dnu_adj_blk(IntegratorDev I, DnuAdjArgs
     double* knots = reinterpret_cast<double*>(sm + off);
     double* row = knots + I.ld;
     double* rc = row + I.ld;
-    off += 3 * sizeof(double) * I.ld;
+    double* sb = rc + I.ld;
+    double* sd = sb + I.ld;
+    off += 5 * sizeof(double) * I.ld;
     QagList& L = *reinterpret_cast<QagList*>(sm + off);
     off += (sizeof(QagList) + 15) & ~size_t(15);
     QagBlockSmem& sh = *reinterpret_cast<QagBlockSmem*>(sm + off);
@@ -652,6 +660,9 @@ __global__ void __launch_bounds__(128) k_dnu_adj_blk(IntegratorDev I, DnuAdjArgs
                 mbar_wait_bounded_a(bar, phase ^ 1);
                 return;
             }
+            const KnotSeg ks{I.knot_invh, I.knot_h3, I.knot_ih3};
+            if (Na > 2) seg_poly(row, rc, Na, ks, sb, sd, tid, blockDim.x);
+            __syncthreads();
             const double qc = S.partnu_now > 0 ? B->vcrit * mnubykT : 0.0;
             int nint;
             const double* iv = nullptr;
@@ -659,12 +670,12 @@ __global__ void __launch_bounds__(128) k_dnu_adj_blk(IntegratorDev I, DnuAdjArgs
                 nint = A.nivals[(size_t)mi * I.nk_alloc + ik];
                 iv = A.ivals + ((size_t)mi * I.nk_alloc + ik) * kQagLimit * 2;
             } else {
-                const DnuIntegrandC f = dnu_integrand(I, S, k, mnubykT, qc, knots, row, rc, Na);
+                const DnuIntegrandC f = dnu_integrand(I, S, k, mnubykT, qc, knots, row, rc, sb, sd, Na);
                 const QagResult r = qag_block_c(f, N, L, S.loga0, S.loga, 0.0, S.relerr, kQagLimit, sh);
                 nint = r.nint;
             }
             __syncthreads();
-            const DnuIntegrandC fi = dnu_integrand(I, S, k, mnubykT, qc, knots, row, rc, Na);
+            const DnuIntegrandC fi = dnu_integrand(I, S, k, mnubykT, qc, knots, row, rc, sb, sd, Na);
             const double ckm = -sbar * S.prefac * fi.k_over_m / mnu;
             double* yb = wy + (size_t)warp * I.ld;
             double* cb = wc + (size_t)warp * I.ld;
@@ -710,7 +721,7 @@ __global__ void __launch_bounds__(128) k_dnu_adj_blk(IntegratorDev I, DnuAdjArgs
 
 size_t dnu_adj_smem(int ld, int wpb) {
     return ((sizeof(Gk61Nodes) + 15) & ~size_t(15)) + sizeof(double) * ld +
-           wpb * (sizeof(QagList) + 4 * sizeof(double) * ld) + wpb * sizeof(uint64_t);
+           wpb * (sizeof(QagList) + 6 * sizeof(double) * ld) + wpb * sizeof(uint64_t);
 }
 
 static int sm_count_a() {
@@ -767,6 +778,7 @@ void launch_dnu_adj(const IntegratorDev& I, const double* dnu_bar, double* Dbar,
                     cudaStream_t st) {
     DnuAdjArgs A{dnu_bar, Dbar, mbar, ivals, nivals, recompute};
     wpb = wpb < 1 ? 1 : (wpb > 4 ? 4 : wpb);
+    while (wpb > 1 && dnu_adj_smem(I.ld, wpb) > 227 * 1024) wpb--;
     const size_t smem = dnu_adj_smem(I.ld, wpb);
     static bool attr = false;
     if (!attr) {

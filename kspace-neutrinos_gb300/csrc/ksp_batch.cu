@@ -93,7 +93,8 @@ __global__ void kb_prologue(BatchDev b) {
 // ------------------------------------------------------------------ fslength table
 struct GL4b { double x[2], w[2]; };
 
-// 4 lanes per segment, as k_fs_segments
+// 4 lanes per segment over the segments of all instances (flat, so that instances of
+// any length balance), as k_fs_segments
 __global__ void kb_fs_segments(BatchDev b, GL4b gl) {
     const int total = b.hdr->total_segs;
     const long long stride = (long long)gridDim.x * blockDim.x;  // a multiple of 4
@@ -118,7 +119,7 @@ __global__ void kb_fs_segments(BatchDev b, GL4b gl) {
                 const int j = q & 1;
                 const double x = (q < 2) ? c - h * gl.x[j] : c + h * gl.x[j];
                 const double ax = exp(x);
-                v = gl.w[j] * h * (1. / ax / (ax * hubble(*b.insts[i].B, ax)));
+                v = gl.w[j] * h * (1. / (ax * (ax * hubble(*b.insts[i].B, ax, x))));
             }
             if (q == 0) b.insts[i].fs_x[seg] = xa;
         }
@@ -179,39 +180,15 @@ __global__ void __launch_bounds__(1024) kb_fs_finish(BatchDev b) {
     }
 }
 
-// thread per (instance, unknown): closed-form inverse of tridiag(1,4,1), as k_fs_coeffs
+// warp per instance: the fslength table's spline coefficients, as k_fs_coeffs
 __global__ void kb_fs_coeffs(BatchDev b) {
-    __shared__ double mupow[82];
-    for (int e = threadIdx.x; e < 82; e += blockDim.x) {  // any block size
-        const double mu = 2.0 - sqrt(3.0);
-        double p = 1.0;
-        for (int k = 0; k < e; k++) p *= mu;
-        mupow[e] = p;
-    }
-    __syncthreads();
-    const int total = b.hdr->total_fsc;
-    for (int g = blockIdx.x * blockDim.x + threadIdx.x; g < total; g += gridDim.x * blockDim.x) {
-        const int i = owner_of(b.fsc_off, b.M, g);
-        const int u = g - __ldg(b.fsc_off + i);
+    const int nw = blockDim.x >> 5;
+    for (int i = blockIdx.x * nw + (threadIdx.x >> 5); i < b.M; i += gridDim.x * nw) {
         const BatchCall& P = b.calls[i];
+        const int Nfs = P.nfs;
+        if (!P.active || P.commit_row == -2 || Nfs <= 2) continue;  // uniform over the warp
         const IntegratorDev& I = b.insts[i];
-        const int Nfs = P.nfs, m = Nfs - 2;
-        const double h = (P.loga - P.loga0) / (Nfs - 1.);
-        const double scale = 3.0 / (h * h) / (2.0 * sqrt(3.0));
-        const double D = (2 * (m + 1) < 82) ? 1.0 - mupow[2 * (m + 1)] : 1.0;
-        const double* y = I.fs_y;
-        double acc = 0;
-        const int vlo = max(0, u - 40), vhi = min(m - 1, u + 40);
-        for (int v = vlo; v <= vhi; v++) {
-            const int d = v > u ? v - u : u - v;
-            const int lo1 = min(u, v) + 1, hi1 = max(u, v) + 1;
-            const double A = (2 * lo1 < 82) ? 1.0 - mupow[2 * lo1] : 1.0;
-            const int e2 = 2 * (m + 1 - hi1);
-            const double Bf = (e2 < 82) ? 1.0 - mupow[e2] : 1.0;
-            const double r = y[v + 2] - 2.0 * y[v + 1] + y[v];
-            acc += ((d & 1) ? -mupow[d] : mupow[d]) * A * Bf * r;
-        }
-        I.fs_c[u + 1] = acc * scale / D;
+        uniform_spline_warp(I.fs_y, I.fs_c, Nfs, (P.loga - P.loga0) / (Nfs - 1.));
     }
 }
 
@@ -284,22 +261,25 @@ __global__ void kb_nc_build(BatchDev b) {
 }
 
 size_t batch_qag_smem(int ldmax, int wpb) {
-    return ((sizeof(Gk61Nodes) + 15) & ~size_t(15)) + wpb * (sizeof(QagList) + 3 * sizeof(double) * ldmax) +
+    return ((sizeof(Gk61Nodes) + 15) & ~size_t(15)) + wpb * (sizeof(QagList) + 5 * sizeof(double) * ldmax) +
            wpb * sizeof(uint64_t);
 }
 
-// Shared memory: Gk61Nodes | per warp: QagList, knots[ldmax], row[ldmax], coef[ldmax] | mbarriers
+// Shared memory: Gk61Nodes | per warp: QagList, knots[ldmax], row[ldmax], coef[ldmax], seg_poly [2 ldmax] |
+// mbarriers
 __global__ void __launch_bounds__(128) kb_dnu_qag(BatchDev b) {
     extern __shared__ __align__(16) unsigned char sm[];
     Gk61Nodes& N = *reinterpret_cast<Gk61Nodes*>(sm);
     const size_t off = (sizeof(Gk61Nodes) + 15) & ~size_t(15);
     const int nw = blockDim.x >> 5, warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    const size_t per_warp = sizeof(QagList) + 3 * sizeof(double) * b.ldmax;
+    const size_t per_warp = sizeof(QagList) + 5 * sizeof(double) * b.ldmax;
     unsigned char* wbase = sm + off + warp * per_warp;
     QagList& L = *reinterpret_cast<QagList*>(wbase);
     double* knots = reinterpret_cast<double*>(wbase + sizeof(QagList));
     double* row = knots + b.ldmax;
     double* rc = row + b.ldmax;
+    double* sb = rc + b.ldmax;
+    double* sd = sb + b.ldmax;
     uint64_t* mybar = reinterpret_cast<uint64_t*>(sm + off + nw * per_warp) + warp;
     gk61_fill(N, threadIdx.x, blockDim.x);
     if (lane == 0) ptx::mbar_init(mybar, 1);
@@ -344,8 +324,11 @@ __global__ void __launch_bounds__(128) kb_dnu_qag(BatchDev b) {
                 ptx::mbar_wait_bounded(mybar, phase ^ 1);  // the copies still in flight
                 return;
             }
+            const KnotSeg ks{I.knot_invh, I.knot_h3, I.knot_ih3};
+            if (Na > 2) seg_poly(row, rc, Na, ks, sb, sd, lane, 32);
+            __syncwarp();
             const double qc = S.partnu_now > 0 ? B->vcrit * mnubykT : 0.0;
-            const DnuIntegrandC f = dnu_integrand(I, S, k, mnubykT, qc, knots, row, rc, Na);
+            const DnuIntegrandC f = dnu_integrand(I, S, k, mnubykT, qc, knots, row, rc, sb, sd, Na);
             const QagResult r = qag_warp_c(f, N, L, S.loga0, S.loga, 0.0, S.relerr, kQagLimit);
             val += S.prefac * r.result;
             if (!r.ok && lane == 0) atomicOr(I.status, kStGsl);

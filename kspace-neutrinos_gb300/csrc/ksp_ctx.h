@@ -33,7 +33,7 @@ struct kspace_ctx {
     cudaStream_t stream = nullptr, own_stream = nullptr;
     kspace_allreduce_fn ar_fn = nullptr;
     void* ar_user = nullptr;
-    int tma = 3, rows = 256, stages = 2, qag_warps = 1;
+    int tma = 5, rows = 256, stages = 2, qag_warps = 1;
     int nc_levels = 8;  // depths of QAG's rightmost bisections kept in the integrand node table
     int qag_split = 0;  // warps per (species, bin) integral: 1, 2, 4; 0 = by the task count
     // background

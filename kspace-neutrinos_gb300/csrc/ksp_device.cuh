@@ -136,12 +136,13 @@ KSP_HD double rel_rho_nu(double a, double kT, double conv) {
 }
 
 // omega_nu_single.c:171-202
-KSP_HD double rho_nu(const RhoTable& T, double a, double kT, double conv) {
+// loga_in: log(a) when the caller has it (NaN: computed here)
+KSP_HD double rho_nu(const RhoTable& T, double a, double kT, double conv, double loga_in = NAN) {
     const double amnu = a * T.mnu;
     const double kTamnu2 = (kT * kT / amnu / amnu);
     if (kNuSw * kNuSw * kTamnu2 < 1) return non_rel_rho_nu(a, kT, amnu, kTamnu2, conv);
     if (amnu < 1e-6 * kT) return rel_rho_nu(a, kT, conv);
-    const double loga = log(a);
+    const double loga = loga_in == loga_in ? loga_in : log(a);
     if (!T.has_table || loga < T.loga[0]) {
         if (amnu < 1e-4 * kT) return rel_rho_nu(a, kT, conv);
         return non_rel_rho_nu(a, kT, amnu, kTamnu2, conv);
@@ -163,10 +164,10 @@ KSP_HD double particle_nu_fraction(const Background& B, double a, int i) {
 }
 
 // omega_nu_single.c:55-65
-KSP_HD double omega_nu(const Background& B, double a) {
+KSP_HD double omega_nu(const Background& B, double a, double loga = NAN) {
     double rhonu = 0;
     for (int mi = 0; mi < kNuSpecies; mi++)
-        if (B.deg[mi] > 0) rhonu += B.deg[mi] * rho_nu(B.tab[mi], a, B.kBtnu, B.conv);
+        if (B.deg[mi] > 0) rhonu += B.deg[mi] * rho_nu(B.tab[mi], a, B.kBtnu, B.conv, loga);
     return rhonu / B.rhocrit;
 }
 
@@ -189,11 +190,11 @@ KSP_HD double omega_nu_single(const Background& B, double a, int i) {
 
 // delta_tot_table_test.c:33-45 (+ curvature, gadget-2/0003 patch:38); Omega_g as
 // omega_nu_single.c:77-81.
-KSP_HD double hubble(const Background& B, double a) {
+KSP_HD double hubble(const Background& B, double a, double loga = NAN) {
     const double a3 = a * a * a;
     double om = B.Omega_nonu_H / a3 + B.OmegaLambda;
     if (B.OmegaK != 0.0) om += B.OmegaK / (a * a);
-    om += omega_nu(B, a);
+    om += omega_nu(B, a, loga);
     if (B.radiation) om += B.omegag0 / (a3 * a);
     return B.hubble * sqrt(om);
 }
@@ -442,40 +443,50 @@ __device__ __forceinline__ int nc_child(int s, int right, int nslots) {
     return c < nslots ? c : -1;
 }
 
-// gk61_warp with interval slots (same arithmetic)
-template <class F>
-__device__ __forceinline__ void gk61_warp_c(const F& f, const Gk61Nodes& N, int nint, const double* a,
-                                            const double* b, const int* slot, GkOut* out) {
+// The GK61 sums of one or two intervals from the node values of a warp (lane holds the
+// values of slots lane, lane+32, lane+64, lane+96; slot s is node s%61 of interval s/61),
+// and the rule's outputs, identical on every lane.  The six sums (Kronrod, Gauss and
+// |f| sums of both intervals) are reduced together by a butterfly that halves the set of
+// values each lane carries at every step (9 additions per lane instead of 30), then
+// resasc's two sums likewise (5 instead of 10); the results are broadcast.
+__device__ __forceinline__ void gk61_lane_sums(const Gk61Nodes& N, const double* fv, int nslots, int nint,
+                                               const double* h, GkOut* out) {
     const int lane = threadIdx.x & 31;
-    double c[2], h[2];
-    for (int t = 0; t < 2; t++) {
-        c[t] = __dmul_rn(0.5, __dadd_rn(a[t], b[t]));
-        h[t] = __dmul_rn(0.5, __dsub_rn(b[t], a[t]));
-    }
-    double fv[4];
-    double rk[2] = {0, 0}, rg[2] = {0, 0}, ra[2] = {0, 0};
-    const int nslots = 61 * nint;
+    double v[8] = {0, 0, 0, 0, 0, 0, 0, 0};  // rk0 rg0 ra0 - rk1 rg1 ra1 -
 #pragma unroll
     for (int m = 0; m < 4; m++) {
         const int s = lane + 32 * m;
-        fv[m] = 0.0;
         if (s < nslots) {
             const int t = s >= 61 ? 1 : 0;
             const int j = s - 61 * t;
-            const double x = __dadd_rn(c[t], __dmul_rn(h[t], N.x[j]));
-            const double v = f.node(slot[t], j, x);
-            fv[m] = v;
-            if (t == 0) { rk[0] += N.wk[j] * v; rg[0] += N.wg[j] * v; ra[0] += N.wk[j] * fabs(v); }
-            else { rk[1] += N.wk[j] * v; rg[1] += N.wg[j] * v; ra[1] += N.wk[j] * fabs(v); }
+            const double x = fv[m];
+            if (t == 0) { v[0] += N.wk[j] * x; v[1] += N.wg[j] * x; v[2] += N.wk[j] * fabs(x); }
+            else { v[4] += N.wk[j] * x; v[5] += N.wg[j] * x; v[6] += N.wk[j] * fabs(x); }
         }
     }
-    double mean[2];
-    for (int t = 0; t < nint; t++) {
-        rk[t] = bcast0(warp_sum_to0(rk[t]));
-        rg[t] = bcast0(warp_sum_to0(rg[t]));
-        ra[t] = bcast0(warp_sum_to0(ra[t]));
-        mean[t] = 0.5 * rk[t];
+    // value q ends in lanes with bits (4, 3, 2) = (q >> 2, (q >> 1) & 1, q & 1)
+    const int b4 = (lane >> 4) & 1, b3 = (lane >> 3) & 1, b2 = (lane >> 2) & 1;
+    double w[4];
+#pragma unroll
+    for (int k = 0; k < 4; k++) {
+        const double keep = b4 ? v[4 + k] : v[k], give = b4 ? v[k] : v[4 + k];
+        w[k] = keep + __shfl_xor_sync(0xffffffffu, give, 16);
     }
+    double x2[2];
+#pragma unroll
+    for (int k = 0; k < 2; k++) {
+        const double keep = b3 ? w[2 + k] : w[k], give = b3 ? w[k] : w[2 + k];
+        x2[k] = keep + __shfl_xor_sync(0xffffffffu, give, 8);
+    }
+    double y;
+    {
+        const double keep = b2 ? x2[1] : x2[0], give = b2 ? x2[0] : x2[1];
+        y = keep + __shfl_xor_sync(0xffffffffu, give, 4);
+    }
+    y += __shfl_xor_sync(0xffffffffu, y, 2);
+    y += __shfl_xor_sync(0xffffffffu, y, 1);
+    const double rk0 = __shfl_sync(0xffffffffu, y, 0), rk1 = __shfl_sync(0xffffffffu, y, 16);
+    const double mean[2] = {0.5 * rk0, 0.5 * rk1};
     double rs[2] = {0, 0};
 #pragma unroll
     for (int m = 0; m < 4; m++) {
@@ -487,14 +498,46 @@ __device__ __forceinline__ void gk61_warp_c(const F& f, const Gk61Nodes& N, int 
             if (t == 0) rs[0] += d; else rs[1] += d;
         }
     }
+    double z = (b4 ? rs[1] : rs[0]) + __shfl_xor_sync(0xffffffffu, b4 ? rs[0] : rs[1], 16);
+#pragma unroll
+    for (int o = 8; o > 0; o >>= 1) z += __shfl_xor_sync(0xffffffffu, z, o);
+    const double rk[2] = {rk0, rk1};
+    const double rg[2] = {__shfl_sync(0xffffffffu, y, 4), __shfl_sync(0xffffffffu, y, 20)};
+    const double ra[2] = {__shfl_sync(0xffffffffu, y, 8), __shfl_sync(0xffffffffu, y, 24)};
+    const double rsum[2] = {__shfl_sync(0xffffffffu, z, 0), __shfl_sync(0xffffffffu, z, 16)};
     for (int t = 0; t < nint; t++) {
-        rs[t] = bcast0(warp_sum_to0(rs[t]));
         const double err = (rk[t] - rg[t]) * h[t];
         out[t].result = rk[t] * h[t];
         out[t].resabs = ra[t] * fabs(h[t]);
-        out[t].resasc = rs[t] * fabs(h[t]);
+        out[t].resasc = rsum[t] * fabs(h[t]);
         out[t].abserr = rescale_error(err, out[t].resabs, out[t].resasc);
     }
+}
+
+// gk61_warp with interval slots (same arithmetic)
+template <class F>
+__device__ __forceinline__ void gk61_warp_c(const F& f, const Gk61Nodes& N, int nint, const double* a,
+                                            const double* b, const int* slot, GkOut* out) {
+    const int lane = threadIdx.x & 31;
+    double c[2], h[2];
+    for (int t = 0; t < 2; t++) {
+        c[t] = __dmul_rn(0.5, __dadd_rn(a[t], b[t]));
+        h[t] = __dmul_rn(0.5, __dsub_rn(b[t], a[t]));
+    }
+    double fv[4];
+    const int nslots = 61 * nint;
+#pragma unroll
+    for (int m = 0; m < 4; m++) {
+        const int s = lane + 32 * m;
+        fv[m] = 0.0;
+        if (s < nslots) {
+            const int t = s >= 61 ? 1 : 0;
+            const int j = s - 61 * t;
+            const double x = __dadd_rn(c[t], __dmul_rn(h[t], N.x[j]));
+            fv[m] = f.node(slot[t], j, x);
+        }
+    }
+    gk61_lane_sums(N, fv, nslots, nint, h, out);
 }
 
 // qag_warp with interval slots (same decisions)
@@ -602,53 +645,16 @@ __device__ __forceinline__ void gk61_block_c(const F& f, const Gk61Nodes& N, int
         sh.fv[s] = f.node(slot[t], j, x);
     }
     __syncthreads();
-    if (tid < 32) {
+    if (tid < 32) {  // warp 0: the sums exactly as gk61_warp_c forms them
         double fv[4];
-        double rk[2] = {0, 0}, rg[2] = {0, 0}, ra[2] = {0, 0};
 #pragma unroll
         for (int m = 0; m < 4; m++) {
             const int s = lane + 32 * m;
-            fv[m] = 0.0;
-            if (s < nslots) {
-                const int t = s >= 61 ? 1 : 0;
-                const int j = s - 61 * t;
-                const double v = sh.fv[s];
-                fv[m] = v;
-                if (t == 0) { rk[0] += N.wk[j] * v; rg[0] += N.wg[j] * v; ra[0] += N.wk[j] * fabs(v); }
-                else { rk[1] += N.wk[j] * v; rg[1] += N.wg[j] * v; ra[1] += N.wk[j] * fabs(v); }
-            }
+            fv[m] = s < nslots ? sh.fv[s] : 0.0;
         }
-        double mean[2];
-        for (int t = 0; t < nint; t++) {
-            rk[t] = bcast0(warp_sum_to0(rk[t]));
-            rg[t] = bcast0(warp_sum_to0(rg[t]));
-            ra[t] = bcast0(warp_sum_to0(ra[t]));
-            mean[t] = 0.5 * rk[t];
-        }
-        double rs[2] = {0, 0};
-#pragma unroll
-        for (int m = 0; m < 4; m++) {
-            const int s = lane + 32 * m;
-            if (s < nslots) {
-                const int t = s >= 61 ? 1 : 0;
-                const int j = s - 61 * t;
-                const double d = N.wk[j] * fabs(fv[m] - mean[t]);
-                if (t == 0) rs[0] += d; else rs[1] += d;
-            }
-        }
-        for (int t = 0; t < nint; t++) rs[t] = bcast0(warp_sum_to0(rs[t]));
-        if (lane < nint) {  // the intervals' estimates on separate lanes
-            const int t = lane;
-            const double rkt = t ? rk[1] : rk[0], rgt = t ? rg[1] : rg[0], rat = t ? ra[1] : ra[0];
-            const double rst = t ? rs[1] : rs[0], ht = t ? h[1] : h[0];
-            const double err = (rkt - rgt) * ht;
-            GkOut o;
-            o.result = rkt * ht;
-            o.resabs = rat * fabs(ht);
-            o.resasc = rst * fabs(ht);
-            o.abserr = rescale_error(err, o.resabs, o.resasc);
-            sh.out[t] = o;
-        }
+        GkOut o[2];
+        gk61_lane_sums(N, fv, nslots, nint, h, o);
+        if (lane < nint) sh.out[lane] = o[lane];
     }
     __syncthreads();
     for (int t = 0; t < nint; t++) out[t] = sh.out[t];
@@ -792,13 +798,32 @@ __device__ __forceinline__ double dnu_S(const NodeTerms& t, const double* ky, co
     return y0 + t.dx * ((y1 - y0) * __ldg(ks.ih + j));
 }
 
+// The node-independent part of dnu_S per segment of a history row, computed once per
+// (row, call) into sb / sd by threads t, t+nt, ...: the same expressions as dnu_S, so
+// that dnu_S_poly returns the same values with three FMAs per node.
+__device__ __forceinline__ void seg_poly(const double* ky, const double* kc, int na, const KnotSeg& ks, double* sb,
+                                         double* sd, int t, int nt) {
+    for (int j = t; j < na - 1; j += nt) {
+        const double y0 = ky[j], y1 = ky[j + 1], c0 = kc[j], c1 = kc[j + 1];
+        sb[j] = (y1 - y0) * __ldg(ks.ih + j) - (c1 + 2.0 * c0) * __ldg(ks.h3 + j);
+        sd[j] = (c1 - c0) * __ldg(ks.ih3 + j);
+    }
+}
+__device__ __forceinline__ double dnu_S_poly(const NodeTerms& t, const double* ky, const double* kc,
+                                             const double* sb, const double* sd, int na, const KnotSeg& ks) {
+    const int j = t.j;
+    if (na > 2) return ky[j] + t.dx * (sb[j] + t.dx * (kc[j] + t.dx * sd[j]));
+    return ky[j] + t.dx * ((ky[j + 1] - ky[j]) * __ldg(ks.ih + j));
+}
+
 // The per-bin rest: J and the history row's natural spline (or linear for 2 knots) at
 // the node.  Same for the cached and uncached paths.
 // k_over_m = k / (m / kT): J's argument is fslength * k_over_m (one division per bin
 // instead of one per node).
 __device__ __forceinline__ double dnu_combine(const NodeTerms& t, double k_over_m, double qc, double nfl,
-                                              const double* ky, const double* kc, int na, const KnotSeg& ks) {
-    const double S = dnu_S(t, ky, kc, na, ks);
+                                              const double* ky, const double* kc, const double* sb,
+                                              const double* sd, int na, const KnotSeg& ks) {
+    const double S = dnu_S_poly(t, ky, kc, sb, sd, na, ks);
     const double J = specialJ_tab(t.fsl * k_over_m, qc, nfl);
     return t.g * J * S;
 }
@@ -818,6 +843,7 @@ struct DnuIntegrandC {
     double k_over_m, qc, nfl;
     const double* fs_x; const double* fs_y; const double* fs_c; int nfs; double fs_x0, fs_inv;
     const double* kx; const double* ky; const double* kc; int na;
+    const double* sb; const double* sd;  // seg_poly of (ky, kc)
     KnotSeg ks;
     NodeCache nc;
     __device__ double node(int slot, int jn, double x) const {
@@ -831,7 +857,7 @@ struct DnuIntegrandC {
         } else {
             t = dnu_node_terms(B, fs_x, fs_y, fs_c, nfs, fs_x0, fs_inv, kx, na, x);
         }
-        return dnu_combine(t, k_over_m, qc, nfl, ky, kc, na, ks);
+        return dnu_combine(t, k_over_m, qc, nfl, ky, kc, sb, sd, na, ks);
     }
     __device__ NodeTerms terms(int slot, int jn, double x) const {
         if (slot >= 0) {

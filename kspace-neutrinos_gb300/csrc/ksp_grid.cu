@@ -550,7 +550,11 @@ static int bin_variant(const GridGeom& g, const GridArgs& a, const float* grid, 
 int launch_bin_power(const GridGeom& g, const float* grid, double* bin_sum, double* F0sq, unsigned* status, int tma,
                      int rows_per_cta, int stages, cudaStream_t st) {
     const GridArgs a = make_grid_args(g, 0, 0.f);
-    if (tma >= 3) {
+    if (tma >= 5) {
+        const int r = launch_bin_rows(g, a, grid, bin_sum, F0sq, status, rows_per_cta / 32, stages, tma == 5, st);
+        if (r == 0) return 0;
+        if (r == -2) return -2;
+    } else if (tma >= 3) {
         const int r = launch_bin_stream(g, a, grid, bin_sum, F0sq, status, rows_per_cta / 32, stages, tma == 3, st);
         if (r == 0) return 0;
         if (r == -2) return -2;

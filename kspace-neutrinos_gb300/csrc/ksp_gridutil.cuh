@@ -20,6 +20,9 @@ int launch_bin_stream(const struct GridGeom& g, const GridArgs& a, const float* 
                       unsigned* status, int warps, int stages, bool exact, cudaStream_t st);
 int launch_correct_stream(const GridArgs& a, float* grid, struct CorrTable corr, unsigned* status, int warps,
                           int stages, cudaStream_t st);
+// K1 over row-aligned runs of 17 modes (ksp_stream.cu): same return codes
+int launch_bin_rows(const struct GridGeom& g, const GridArgs& a, const float* grid, double* bin_sum, double* F0sq,
+                    unsigned* status, int warps, int stages, bool exact, cudaStream_t st);
 
 // n / d for n < 2^31: m = floor(2^s/d)+1 with s = 31 + ceil(log2 d)
 struct FastDiv {

@@ -238,7 +238,7 @@ struct FslIntegrand {  // delta_tot_table.c:378-383
     const Background* B;
     __device__ double operator()(double loga) const {
         const double a = exp(loga);
-        return 1. / a / (a * hubble(*B, a));
+        return 1. / (a * (a * hubble(*B, a, loga)));
     }
 };
 
@@ -317,7 +317,9 @@ __global__ void k_fs_finish(IntegratorDev I, int Nfs) {
 // unknown.  The system is tridiag(1,4,1) c = 3 D^2 y / h^2 with known inverse: for
 // mu = 2 - sqrt(3) and 1-based i <= j,
 //   (T^-1)_{ij} = (-1)^{i+j} mu^{j-i} (1-mu^{2i}) (1-mu^{2(m+1-j)}) / (2 sqrt3 (1-mu^{2(m+1)})).
-// Terms with |i-j| > 40 are below 1e-22 relative and dropped.
+// Terms with |i-j| > 40 are below 1e-22 relative and dropped.  (Fully parallel: a single
+// table is solved faster this way than by one warp's substitution, whose loads are
+// serial; the batch path, with thousands of tables, uses uniform_spline_warp.)
 __global__ void k_fs_coeffs(IntegratorDev I, int Nfs, double loga0, double loga) {
     __shared__ double mupow[82];
     for (int e = threadIdx.x; e < 82; e += blockDim.x) {  // any block size
@@ -386,7 +388,8 @@ __global__ void k_nc_build(IntegratorDev I, int Na) {
 }
 
 // ------------------------------------------------------------------ delta_nu integral
-// Shared memory per CTA: Gk61Nodes | knots[ld] | per warp: QagList, row[ld], coef[ld] | mbarriers
+// Shared memory per CTA: Gk61Nodes | knots[ld] | per warp: QagList, row[ld], coef[ld], seg_poly [2 ld] |
+// mbarriers
 __global__ void __launch_bounds__(128) k_dnu_qag(IntegratorDev I, int nk, int Na, int nspec, int4 spec_ids) {
     extern __shared__ __align__(16) unsigned char sm[];
     Gk61Nodes& N = *reinterpret_cast<Gk61Nodes*>(sm);
@@ -394,11 +397,13 @@ __global__ void __launch_bounds__(128) k_dnu_qag(IntegratorDev I, int nk, int Na
     double* knots = reinterpret_cast<double*>(sm + off);
     off += sizeof(double) * I.ld;
     const int nw = blockDim.x >> 5, warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    const size_t per_warp = sizeof(QagList) + 2 * sizeof(double) * I.ld;
+    const size_t per_warp = sizeof(QagList) + 4 * sizeof(double) * I.ld;
     unsigned char* wbase = sm + off + warp * per_warp;
     QagList& L = *reinterpret_cast<QagList*>(wbase);
     double* row = reinterpret_cast<double*>(wbase + sizeof(QagList));
     double* rc = row + I.ld;
+    double* sb = rc + I.ld;
+    double* sd = sb + I.ld;
     uint64_t* bars = reinterpret_cast<uint64_t*>(sm + off + nw * per_warp);
     uint64_t* mybar = bars + warp;
 
@@ -443,8 +448,11 @@ __global__ void __launch_bounds__(128) k_dnu_qag(IntegratorDev I, int nk, int Na
                 mbar_wait_bounded(mybar, phase ^ 1);
                 return;
             }
+            const KnotSeg ks{I.knot_invh, I.knot_h3, I.knot_ih3};
+            if (Na > 2) seg_poly(row, rc, Na, ks, sb, sd, lane, 32);
+            __syncwarp();
             const double qc = S.partnu_now > 0 ? B->vcrit * mnubykT : 0.0;
-            const DnuIntegrandC f = dnu_integrand(I, S, k, mnubykT, qc, knots, row, rc, Na);
+            const DnuIntegrandC f = dnu_integrand(I, S, k, mnubykT, qc, knots, row, rc, sb, sd, Na);
             QagResult r = qag_warp_c(f, N, L, S.loga0, S.loga, 0.0, S.relerr, kQagLimit);
             val += S.prefac * r.result;
             if (I.ivals) {  // keep the final subdivision for the adjoint
@@ -482,6 +490,9 @@ __global__ void __launch_bounds__(128) k_dnu_qag_blk(IntegratorDev I, int nk, in
     off += sizeof(double) * I.ld;
     double* rc = reinterpret_cast<double*>(sm + off);
     off += sizeof(double) * I.ld;
+    double* sb = reinterpret_cast<double*>(sm + off);
+    double* sd = sb + I.ld;
+    off += 2 * sizeof(double) * I.ld;
     QagList& L = *reinterpret_cast<QagList*>(sm + off);
     off += (sizeof(QagList) + 15) & ~size_t(15);
     QagBlockSmem& sh = *reinterpret_cast<QagBlockSmem*>(sm + off);
@@ -524,8 +535,11 @@ __global__ void __launch_bounds__(128) k_dnu_qag_blk(IntegratorDev I, int nk, in
                 mbar_wait_bounded(bar, phase ^ 1);
                 return;
             }
+            const KnotSeg ks{I.knot_invh, I.knot_h3, I.knot_ih3};
+            if (Na > 2) seg_poly(row, rc, Na, ks, sb, sd, tid, blockDim.x);
+            __syncthreads();
             const double qc = S.partnu_now > 0 ? B->vcrit * mnubykT : 0.0;
-            const DnuIntegrandC f = dnu_integrand(I, S, k, mnubykT, qc, knots, row, rc, Na);
+            const DnuIntegrandC f = dnu_integrand(I, S, k, mnubykT, qc, knots, row, rc, sb, sd, Na);
             const QagResult r = qag_block_c(f, N, L, S.loga0, S.loga, 0.0, S.relerr, kQagLimit, sh);
             val += S.prefac * r.result;
             if (I.ivals) {  // keep the final subdivision for the adjoint
@@ -549,7 +563,7 @@ __global__ void __launch_bounds__(128) k_dnu_qag_blk(IntegratorDev I, int nk, in
 }
 
 size_t dnu_qag_blk_smem(int ld) {
-    return ((sizeof(Gk61Nodes) + 15) & ~size_t(15)) + 3 * sizeof(double) * ld + ((sizeof(QagList) + 15) & ~size_t(15)) +
+    return ((sizeof(Gk61Nodes) + 15) & ~size_t(15)) + 5 * sizeof(double) * ld + ((sizeof(QagList) + 15) & ~size_t(15)) +
            ((sizeof(QagBlockSmem) + 15) & ~size_t(15)) + sizeof(uint64_t);
 }
 
@@ -592,7 +606,7 @@ static GL4 gl4_host() {
 
 size_t dnu_qag_smem(int ld, int wpb) {
     return ((sizeof(Gk61Nodes) + 15) & ~size_t(15)) + sizeof(double) * ld +
-           wpb * (sizeof(QagList) + 2 * sizeof(double) * ld) + wpb * sizeof(uint64_t);
+           wpb * (sizeof(QagList) + 4 * sizeof(double) * ld) + wpb * sizeof(uint64_t);
 }
 
 // The part of a call that does not depend on the current delta_cdm: the scalars and the
@@ -633,7 +647,8 @@ void launch_integrator_rest(const IntegratorDev& I, int nk, int Na, int nspec, c
         const int staged = smem <= 200 * 1024;
         k_dtot_coeffs<<<(nk + 3) / 4, 128, staged ? smem : 0, st>>>(I, nk, Na, staged);
     }
-    const int wpb = warps_per_block < 1 ? 1 : (warps_per_block > 4 ? 4 : warps_per_block);
+    int wpb = warps_per_block < 1 ? 1 : (warps_per_block > 4 ? 4 : warps_per_block);
+    while (wpb > 1 && dnu_qag_smem(I.ld, wpb) > 227 * 1024) wpb--;
     const size_t smem = dnu_qag_smem(I.ld, wpb);
     static bool attr_set = false;
     if (!attr_set) {

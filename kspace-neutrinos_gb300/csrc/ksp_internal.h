@@ -150,6 +150,91 @@ __device__ __forceinline__ void dtot_row_coeffs_warp(const IntegratorDev& I, int
     __syncwarp();
 }
 
+// Natural-spline second derivatives c[0..n-1] of a table y on uniform spacing h, by
+// one warp: tridiag(1,4,1) c[1..n-2] = 3/h^2 (y[u+2] - 2 y[u+1] + y[u]), c[0] = c[n-1]
+// = 0.  Gaussian elimination has pivots d_0 = 4, d_u = 4 - 1/d_{u-1}; they reach
+// 2 + sqrt(3) to double precision by u = 40, and d_u = d_40 is used from there on.
+// Forward and back substitution are chains of affine maps, composed per lane over a
+// stretch of rows, then across lanes by a warp scan, then replayed (as
+// spline_solve_scan).  c holds the forward pass's results in between.
+struct UniformPivots {
+    double inv[41];  // 1 / d_u, u = 0..40
+    constexpr UniformPivots() : inv() {
+        double d = 4.0;
+        for (int u = 0; u <= 40; u++) {
+            if (u > 0) d = 4.0 - 1.0 / d;
+            inv[u] = 1.0 / d;
+        }
+    }
+};
+static __constant__ UniformPivots kUniformPivots{};
+__device__ __forceinline__ double uniform_inv_pivot(int u) { return kUniformPivots.inv[u < 40 ? u : 40]; }
+__device__ __forceinline__ void uniform_spline_warp(const double* y, double* c, int n, double h) {
+    const int lane = threadIdx.x & 31;
+    const int m = n - 2;
+    if (m >= 1) {
+        const double s3 = 3.0 / (h * h);
+        const int per = (m + 31) / 32;
+        const int u0 = min(m, lane * per), u1 = min(m, u0 + per);
+        // forward: z_u = r_u - z_{u-1} / d_{u-1}
+        double A = 1.0, B = 0.0;
+        for (int u = u0; u < u1; u++) {
+            const double f = u > 0 ? uniform_inv_pivot(u - 1) : 0.0;
+            B = s3 * (y[u + 2] - 2.0 * y[u + 1] + y[u]) - f * B;
+            A = -f * A;
+        }
+        double pa = A, pb = B;
+#pragma unroll
+        for (int d = 1; d < 32; d <<= 1) {
+            const double qa = __shfl_up_sync(0xffffffffu, pa, d), qb = __shfl_up_sync(0xffffffffu, pb, d);
+            if (lane >= d) {
+                pb = pa * qb + pb;
+                pa = pa * qa;
+            }
+        }
+        double zin = __shfl_up_sync(0xffffffffu, pb, 1);
+        if (lane == 0) zin = 0.0;
+        for (int u = u0; u < u1; u++) {
+            const double f = u > 0 ? uniform_inv_pivot(u - 1) : 0.0;
+            zin = s3 * (y[u + 2] - 2.0 * y[u + 1] + y[u]) - f * zin;
+            c[u + 1] = zin;
+        }
+        __syncwarp();
+        // back: x_u = (z_u - x_{u+1}) / d_u, x_m = 0
+        A = 1.0;
+        B = 0.0;
+        for (int u = u1 - 1; u >= u0; u--) {
+            const double iv = uniform_inv_pivot(u);
+            const double off = u < m - 1 ? 1.0 : 0.0;
+            B = (c[u + 1] - off * B) * iv;
+            A = -off * iv * A;
+        }
+        pa = A;
+        pb = B;
+#pragma unroll
+        for (int d = 1; d < 32; d <<= 1) {
+            const double qa = __shfl_down_sync(0xffffffffu, pa, d), qb = __shfl_down_sync(0xffffffffu, pb, d);
+            if (lane + d < 32) {
+                pb = pa * qb + pb;
+                pa = pa * qa;
+            }
+        }
+        double cin = __shfl_down_sync(0xffffffffu, pb, 1);
+        if (lane == 31) cin = 0.0;
+        __syncwarp();
+        for (int u = u1 - 1; u >= u0; u--) {
+            const double off = u < m - 1 ? 1.0 : 0.0;
+            cin = (c[u + 1] - off * cin) * uniform_inv_pivot(u);
+            c[u + 1] = cin;
+        }
+    }
+    if (lane == 0) {
+        c[0] = 0.0;
+        c[n - 1] = 0.0;
+    }
+    __syncwarp();
+}
+
 // The same solve with all 32 lanes: both substitutions are linear recurrences
 // z_u = r_u - f_u z_{u-1} and c_u = (z_u - o_u c_{u+1}) / d_u, i.e. chains of affine
 // maps; each lane composes the maps of its stretch of rows, a warp scan composes the
@@ -242,14 +327,17 @@ __device__ __forceinline__ void dtot_row_coeffs_scan(const IntegratorDev& I, int
 
 // The delta_nu integrand of one (species, bin) with the instance's node table; knots,
 // row and rc may be staged copies (shared memory) of the instance's arrays.
+// sb, sd: seg_poly of (row, rc), filled by the caller
 __device__ __forceinline__ DnuIntegrandC dnu_integrand(const IntegratorDev& I, const StepScalars& S, double k,
                                                        double mnubykT, double qc, const double* knots,
-                                                       const double* row, const double* rc, int Na) {
+                                                       const double* row, const double* rc, const double* sb,
+                                                       const double* sd, int Na) {
     DnuIntegrandC f;
     f.B = I.B; f.k_over_m = k / mnubykT; f.qc = qc; f.nfl = I.B->nufrac_low[0];
     f.fs_x = I.fs_x; f.fs_y = I.fs_y; f.fs_c = I.fs_c; f.nfs = S.Nfs; f.fs_x0 = S.loga0;
     f.fs_inv = (S.Nfs - 1.) / (S.loga - S.loga0);
     f.kx = knots; f.ky = row; f.kc = rc; f.na = Na;
+    f.sb = sb; f.sd = sd;
     f.ks = KnotSeg{I.knot_invh, I.knot_h3, I.knot_ih3};
     f.nc = NodeCache{I.nc_g, I.nc_fsl, I.nc_dx, I.nc_j, I.nc_slots};
     return f;

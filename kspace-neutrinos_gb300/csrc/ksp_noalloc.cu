@@ -121,7 +121,7 @@ extern "C" int kspace_gpu_bin_power_noalloc(int dims, const void* grid, int nrbi
     g.cmap = nullptr;
     g.bin_c1 = (float)(bpu * 0.5 * log(2.0));
     if (g.nmodes > 0 &&
-        launch_bin_power(g, reinterpret_cast<const float*>(grid), S->sums, S->sums + nrbins, &S->status, 3, 256, 2,
+        launch_bin_power(g, reinterpret_cast<const float*>(grid), S->sums, S->sums + nrbins, &S->status, 5, 256, 2,
                          st) < 0)
         return KSPACE_ERR_CUDA;
     unsigned status = 0;

@@ -135,6 +135,36 @@ __device__ __forceinline__ void bin_step(float re, float im, float iwxy, float2 
     d += 2;
 }
 
+// The same step without a branch: the running sum of the current bin is stored to the
+// lane's current slot every mode, and a crossing just moves on to the next slot and the
+// next threshold.  After a run, slots 0..n hold the sums of bins b..b+n.
+template <bool EXACT>
+__device__ __forceinline__ void bin_step_slots(float re, float im, float iwxy, float2 w, int& k2, int& d,
+                                               int& tnext, const int*& tq, typename SpillOf<EXACT>::type*& sp,
+                                               float& h, float& l) {
+    float phi, plo;
+    mode_value<EXACT>(re, im, iwxy, w, phi, plo);
+    const bool c = k2 >= tnext;
+    sp += c ? 32 : 0;
+    tq += c ? 1 : 0;
+    tnext = *tq;
+    const float h0 = c ? 0.f : h;
+    if constexpr (EXACT) {
+        const float l0 = c ? 0.f : l;
+        const float s = __fadd_rn(h0, phi);
+        const float bb = __fsub_rn(s, h0);
+        const float e = __fadd_rn(__fsub_rn(h0, __fsub_rn(s, bb)), __fsub_rn(phi, bb));
+        h = s;
+        l = __fadd_rn(l0, __fadd_rn(e, plo));
+        *sp = make_float2(h, l);
+    } else {
+        h = __fadd_rn(h0, phi);
+        *sp = h;
+    }
+    k2 += d;
+    d += 2;
+}
+
 __device__ __forceinline__ void add_pair(float* H, float* L, int b, float hi, float lo) {
     if (hi != 0.f || lo != 0.f) pair_atomic_add(H, L, b, hi, lo);
 }
@@ -564,6 +594,241 @@ __global__ void __launch_bounds__(WARPS * 32)
     if (flags) atomicOr(status, flags);
 }
 
+// ------------------------------------------------------------------ K1, row-aligned runs
+// A tile is an even number of whole grid rows (one 1-D bulk copy: 16-byte aligned
+// because rows come in pairs), split into runs of 17 modes that never cross a row end;
+// the 136-byte stride between lanes' runs makes the 8-byte shared reads of data and
+// window table conflict-free.  Rows shorter than a multiple of 17 leave a short last
+// run, masked per mode.  Tiles of few rows (small N) hold several row pairs; long rows
+// (N >= 1024) give a tile to a group of warps that share its stage ring.
+constexpr int kRun = 17;
+
+struct RowTiling {
+    int R;            // runs per grid row: ceil(nz / 17)
+    int trows;        // grid rows per tile (even)
+    int wg;           // warps per tile group
+    int tile_bytes;   // trows * nz * 8
+    int stage_bytes;  // tile + read-past slack, 128-byte multiple
+};
+
+inline RowTiling make_row_tiling(int nz) {
+    RowTiling t;
+    t.R = (nz + kRun - 1) / kRun;
+    int pairs = 32 / (2 * t.R);
+    if (pairs < 1) pairs = 1;
+    t.trows = 2 * pairs;
+    t.wg = (t.trows * t.R + 31) / 32;
+    t.tile_bytes = t.trows * nz * 8;
+    t.stage_bytes = (t.tile_bytes + kRun * 8 + 127) & ~127;
+    return t;
+}
+
+// stage rings (per group) | mbarriers | per-warp spill slots | float-pair bin totals |
+// thresholds | {w1[z], multiplicity} for z < nz + 17 (zero past nz)
+__host__ __device__ inline StreamPlan plan_bin_rows(int warps, int stages, int nrbins, int nz, bool exact,
+                                                   const RowTiling& T) {
+    StreamPlan p{};
+    const int groups = warps / T.wg;
+    size_t o = 0;
+    p.stage_off = o;
+    o += (size_t)groups * stages * T.stage_bytes;
+    p.bar_off = o;
+    o += sizeof(uint64_t) * (size_t)groups * stages;
+    o = (o + 15) & ~size_t(15);
+    p.spill_off = o;
+    o += (size_t)warps * kRun * 32 * (exact ? 8 : 4);  // a slot per bin of a run: at most kRun
+    p.hist_off = o;
+    o += sizeof(float) * 2 * (size_t)nrbins;
+    p.thr_off = o;
+    o += sizeof(int) * (size_t)(nrbins + 1);
+    o = (o + 15) & ~size_t(15);
+    p.tab_off = o;
+    o += sizeof(float2) * (size_t)(nz + kRun);
+    p.total = o + 128;  // alignment slack
+    return p;
+}
+
+__device__ __forceinline__ void named_sync(int id, int nthreads) {
+    asm volatile("bar.sync %0, %1;" ::"r"(id), "r"(nthreads) : "memory");
+}
+__device__ __forceinline__ bool named_and(int id, int nthreads, bool v) {
+    uint32_t out;
+    asm volatile(
+        "{\n .reg .pred p, q;\n setp.ne.u32 p, %1, 0;\n bar.red.and.pred q, %2, %3, p;\n selp.u32 %0, 1, 0, q;\n}\n"
+        : "=r"(out)
+        : "r"((uint32_t)v), "r"(id), "r"(nthreads)
+        : "memory");
+    return out != 0;
+}
+
+template <int WARPS, int STAGES, bool EXACT>
+__global__ void __launch_bounds__(WARPS * 32)
+    k_bin_rows(GridArgs g, RowTiling T, const int* __restrict__ thresh, const float* __restrict__ w1g,
+               const float* __restrict__ grid, double* bin_sum, double* F0sq, unsigned* status, long long ntiles,
+               long long nrows) {
+    typedef typename SpillOf<EXACT>::type Spill;
+    extern __shared__ unsigned char sm_raw[];
+    __shared__ int s_gap;
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    const StreamPlan P = plan_bin_rows(WARPS, STAGES, g.nrbins, g.nz, EXACT, T);
+    unsigned char* base = sm_raw + ((128 - (ptx::smem_u32(sm_raw) & 127)) & 127);
+    const int groups = WARPS / T.wg;
+    const int grp = warp / T.wg, wig = warp - grp * T.wg;
+    unsigned char* gstage = base + P.stage_off + (size_t)grp * STAGES * T.stage_bytes;
+    uint64_t* gbar = reinterpret_cast<uint64_t*>(base + P.bar_off) + grp * STAGES;
+    Spill* my_spill = reinterpret_cast<Spill*>(base + P.spill_off) + (size_t)warp * kRun * 32 + lane;
+    float* s_H = reinterpret_cast<float*>(base + P.hist_off);
+    float* s_L = s_H + g.nrbins;
+    int* s_thr = reinterpret_cast<int*>(base + P.thr_off);
+    float2* s_wt = reinterpret_cast<float2*>(base + P.tab_off);
+    for (int i = tid; i < 2 * g.nrbins; i += blockDim.x) s_H[i] = 0.f;
+    for (int i = tid; i < g.nrbins; i += blockDim.x) s_thr[i] = thresh[i];
+    for (int i = tid; i < g.nz + kRun; i += blockDim.x)
+        s_wt[i] = i < g.nz ? make_float2(w1g[i], (i == 0 || i == g.half) ? 1.f : 2.f) : make_float2(0.f, 0.f);
+    const bool leader = wig == 0 && lane == 0;
+    // Modes past a row end (the short last run of a row) are read from the next row or
+    // from the slack after the tile and weighted by the zero table entries past nz; the
+    // slack starts zeroed, so nothing read there is ever uninitialised.
+    {
+        uint4* st4 = reinterpret_cast<uint4*>(base + P.stage_off);
+        for (int i = tid; i < groups * STAGES * T.stage_bytes / 16; i += blockDim.x) st4[i] = make_uint4(0, 0, 0, 0);
+        ptx::fence_async_smem();
+    }
+    if (tid == 0) {
+        s_thr[g.nrbins] = 0x7fffffff;  // never crossed, also by the zero-weight modes past a row end
+        s_gap = -1;
+    }
+    if (leader) {
+        for (int s = 0; s < STAGES; s++) ptx::mbar_init(&gbar[s], 1);
+        ptx::mbar_init_fence();
+    }
+    __syncthreads();
+    const int k2max = 3 * g.half * g.half;
+    for (int b = tid; b < g.nrbins - 1; b += blockDim.x) {
+        const int t0 = s_thr[b], t1 = s_thr[b + 1];
+        if (t1 <= k2max && (float)(t1 - t0) < 2.f * sqrtf((float)t0) + 3.f) atomicMax(&s_gap, b);
+    }
+    __syncthreads();
+    const int ksafe = s_gap >= 0 ? s_thr[s_gap] : 1;
+
+    // this lane's run within every tile
+    const int run = wig * 32 + lane;
+    const bool lane_ok = run < T.trows * T.R;
+    const int row_t = lane_ok ? run / T.R : 0;
+    const int z0 = (run - row_t * T.R) * kRun;
+    const int len = g.nz - z0 < kRun ? g.nz - z0 : kRun;
+    const unsigned lane_off = (unsigned)(row_t * g.nz + z0) * 8u;
+    const float2* wz = s_wt + z0;
+    const int gsz = T.wg * 32;
+
+    const long long gg = (long long)blockIdx.x * groups + grp, TG = (long long)gridDim.x * groups;
+    const long long my_n = gg < ntiles ? (ntiles - 1 - gg) / TG + 1 : 0;
+    const unsigned char* gsrc = reinterpret_cast<const unsigned char*>(grid);
+    if (leader)
+        for (int s = 0; s < STAGES && s < my_n; s++) {
+            const long long t = gg + s * TG;
+            const long long r0 = t * T.trows;
+            const unsigned bytes = (unsigned)((nrows - r0 < T.trows ? nrows - r0 : T.trows) * g.nz * 8);
+            ptx::mbar_expect_tx(&gbar[s], bytes);
+            ptx::bulk_g2s(gstage + s * T.stage_bytes, gsrc + r0 * g.nz * 8, bytes, &gbar[s]);
+        }
+    bool ok = true;
+    long long k = 0;
+    int s = 0;
+    unsigned phase = 0;
+    for (; k < my_n; k++) {
+        const bool got = ptx::mbar_wait_bounded(&gbar[s], phase);
+        const bool all = T.wg == 1 ? __all_sync(kFull, got) : named_and(1 + grp, gsz, got);
+        if (!all) {
+            ok = false;
+            break;
+        }
+        const unsigned char* tb = gstage + s * T.stage_bytes;
+        const long long pr64 = (gg + k * TG) * T.trows + row_t;
+        const bool valid = lane_ok && pr64 < nrows;
+        const int pr = (int)(valid ? pr64 : 0);
+        const int il = (int)fdiv((uint32_t)pr, g.fd_N);
+        const int kx = kval(g.slab0 + il, g.N), ky = kval(pr - il * g.N, g.N);
+        const int kxy2 = kx * kx + ky * ky;
+        int k2 = kxy2 + z0 * z0;
+        const float iwxy = __fmul_rn(s_wt[kx < 0 ? -kx : kx].x, s_wt[ky < 0 ? -ky : ky].x);
+        const bool fast = valid && k2 >= ksafe;
+        if (fast) {
+            const int b = bin_of(k2, g.c1, s_thr, g.nrbins);
+            const int* tq = s_thr + b + 1;
+            int tnext = *tq;
+            Spill* sp = my_spill;
+            float h = 0.f, l = 0.f;
+            int d = 2 * z0 + 1;
+            const float2* vp = reinterpret_cast<const float2*>(tb + lane_off);
+#pragma unroll
+            for (int i = 0; i < kRun; i++) {
+                const float2 v = vp[i];  // past the row end: weight 0 (table entries past nz)
+                bin_step_slots<EXACT>(v.x, v.y, iwxy, wz[i], k2, d, tnext, tq, sp, h, l);
+            }
+            const int nsp = (int)(sp - my_spill) >> 5;
+            for (int q = 0; q <= nsp; q++) {
+                const Spill v = my_spill[32 * q];
+                if constexpr (EXACT) add_pair(s_H, s_L, b + q, v.x, v.y);
+                else add_pair(s_H, s_L, b + q, v, 0.f);
+            }
+        }
+        // runs below ksafe (and the k = 0 mode): one run at a time, a mode per lane
+        unsigned slow = __ballot_sync(kFull, valid && !fast);
+        while (slow) {
+            const int L = __ffs(slow) - 1;
+            slow &= slow - 1;
+            const int zL = __shfl_sync(kFull, z0, L), lenL = __shfl_sync(kFull, len, L);
+            const int kxyL = __shfl_sync(kFull, kxy2, L);
+            const float iwL = __shfl_sync(kFull, iwxy, L);
+            const unsigned offL = __shfl_sync(kFull, lane_off, L);
+            int key = -1;
+            float phi = 0.f, plo = 0.f;
+            const int zz = zL + lane;
+            const int k2m = kxyL + zz * zz;
+            if (lane < lenL && k2m != 0) {
+                const float2 v = *reinterpret_cast<const float2*>(tb + offL + 8 * lane);
+                mode_value<EXACT>(v.x, v.y, iwL, s_wt[zz], phi, plo);
+                key = bin_of(k2m, g.c1, s_thr, g.nrbins);
+            }
+            bool tail;
+            warp_seg_pair(key, phi, plo, tail);
+            if (tail && key >= 0) add_pair(s_H, s_L, key, phi, plo);
+        }
+        if (T.wg == 1) __syncwarp();
+        else named_sync(1 + grp, gsz);
+        if (leader && k + STAGES < my_n) {
+            const long long r0 = (gg + (k + STAGES) * TG) * T.trows;
+            const unsigned bytes = (unsigned)((nrows - r0 < T.trows ? nrows - r0 : T.trows) * g.nz * 8);
+            ptx::mbar_expect_tx(&gbar[s], bytes);
+            ptx::bulk_g2s(gstage + s * T.stage_bytes, gsrc + r0 * g.nz * 8, bytes, &gbar[s]);
+        }
+        if (++s == STAGES) {
+            s = 0;
+            phase ^= 1;
+        }
+    }
+    if (!ok && leader) {
+        atomicOr(status, kStTimeout);
+        for (long long kk = k; kk < my_n && kk < k + STAGES; kk++) {
+            ptx::mbar_wait_bounded(&gbar[s], phase);
+            if (++s == STAGES) {
+                s = 0;
+                phase ^= 1;
+            }
+        }
+    }
+    __syncthreads();
+    if (blockIdx.x == 0 && tid == 0 && g.slab0 == 0 && g.nmodes > 0) {
+        const float re = grid[0], im = grid[1];
+        *F0sq = (double)__fadd_rn(__fmul_rn(re, re), __fmul_rn(im, im));
+    }
+    for (int b = tid; b < g.nrbins; b += blockDim.x) {
+        const double v = (double)s_H[b] + (double)s_L[b];
+        if (v != 0.0) atomicAdd(bin_sum + b, v);
+    }
+}
+
 int sm_count_s() {
     static int n = 0;
     if (!n) {
@@ -608,6 +873,31 @@ int run_bin_stream(const GridGeom& g, const GridArgs& a, const float* grid, doub
     return cudaPeekAtLastError() == cudaSuccess ? 0 : -2;
 }
 
+template <int WARPS, int STAGES, bool EXACT>
+int run_bin_rows(const GridGeom& g, const GridArgs& a, const float* grid, double* bin_sum, double* F0sq,
+                 unsigned* status, cudaStream_t st) {
+    if ((reinterpret_cast<uintptr_t>(grid) & 15) != 0) return -1;
+    const RowTiling T = make_row_tiling(a.nz);
+    if (WARPS % T.wg != 0) return -1;
+    const long long nrows = (long long)g.nslab * g.N;
+    if (nrows <= 0) return -1;
+    const StreamPlan P = plan_bin_rows(WARPS, STAGES, g.nrbins, a.nz, EXACT, T);
+    if (P.total > 220 * 1024) return -1;
+    auto kern = k_bin_rows<WARPS, STAGES, EXACT>;
+    cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)P.total);
+    int per_sm = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, WARPS * 32, P.total) != cudaSuccess ||
+        per_sm < 1)
+        return -1;
+    const long long ntiles = (nrows + T.trows - 1) / T.trows;
+    const int groups = WARPS / T.wg;
+    long long n = (long long)sm_count_s() * per_sm;
+    const long long need = (ntiles + groups - 1) / groups;
+    if (n > need) n = need > 0 ? need : 1;
+    kern<<<(int)n, WARPS * 32, P.total, st>>>(a, T, g.thresh, g.w1, grid, bin_sum, F0sq, status, ntiles, nrows);
+    return cudaPeekAtLastError() == cudaSuccess ? 0 : -2;
+}
+
 template <int WARPS, int STAGES>
 int run_corr_stream(const GridArgs& a, float* grid, CorrTable corr, unsigned* status, cudaStream_t st) {
     CUtensorMap map;
@@ -635,6 +925,19 @@ int launch_bin_stream(const GridGeom& g, const GridArgs& a, const float* grid, d
 #undef KSP_BS
     return exact ? run_bin_stream<8, 2, true>(g, a, grid, bin_sum, F0sq, status, st)
                  : run_bin_stream<8, 2, false>(g, a, grid, bin_sum, F0sq, status, st);
+}
+
+int launch_bin_rows(const GridGeom& g, const GridArgs& a, const float* grid, double* bin_sum, double* F0sq,
+                    unsigned* status, int warps, int stages, bool exact, cudaStream_t st) {
+    if (a.N >= 32768) return -1;
+#define KSP_BR(W, S)                                                                            \
+    if (warps == W && stages == S)                                                              \
+        return exact ? run_bin_rows<W, S, true>(g, a, grid, bin_sum, F0sq, status, st)          \
+                     : run_bin_rows<W, S, false>(g, a, grid, bin_sum, F0sq, status, st);
+    KSP_BR(4, 2) KSP_BR(4, 3) KSP_BR(8, 2) KSP_BR(8, 3)
+#undef KSP_BR
+    return exact ? run_bin_rows<8, 2, true>(g, a, grid, bin_sum, F0sq, status, st)
+                 : run_bin_rows<8, 2, false>(g, a, grid, bin_sum, F0sq, status, st);
 }
 
 int launch_correct_stream(const GridArgs& a, float* grid, CorrTable corr, unsigned* status, int warps, int stages,

@@ -18,7 +18,7 @@ import workloads as W
 pytestmark = pytest.mark.gpu
 
 L_BOX = 512.0
-SHAPES = [(256, 2), (256, 3), (128, 2), (128, 4)]  # rows per CTA (32 per warp), stages per warp
+SHAPES = [(256, 2), (256, 3), (128, 2), (128, 3)]  # rows per CTA (32 per warp), stages per warp
 TOL_EXACT = 1e-12
 TOL_LEAN = 1e-6
 
@@ -37,9 +37,9 @@ def test_binning_stream_variants(gpu, oracle, N, nb):
     nk_o, p_o, c_o, _ = oracle.total_powerspectrum(g, N, nb)
     k = _instance(gpu, nb)
     gd = torch.as_tensor(g).cuda()
-    worst = {3: 0.0, 4: 0.0}
+    worst = {3: 0.0, 4: 0.0, 5: 0.0, 6: 0.0}
     for rows, stages in SHAPES:
-        for tma, tol in ((3, TOL_EXACT), (4, TOL_LEAN)):
+        for tma, tol in ((3, TOL_EXACT), (4, TOL_LEAN), (5, TOL_EXACT), (6, TOL_LEAN)):
             k.set_tuning(tma=tma, rows=rows, stages=stages)
             nk_g, p_g, c_g, _ = k.total_powerspectrum(N, gd, nb)
             assert nk_g == nk_o
@@ -52,7 +52,7 @@ def test_binning_stream_variants(gpu, oracle, N, nb):
     _, p_1, _, _ = k.total_powerspectrum(N, gd, nb)
     assert cases.rel_err(p_1, p_o) < TOL_EXACT
     k.close()
-    print("N=%d worst P error: exact %.2e lean %.2e" % (N, worst[3], worst[4]))
+    print("N=%d worst P error: exact %.2e / %.2e, lean %.2e / %.2e" % (N, worst[3], worst[5], worst[4], worst[6]))
 
 
 @pytest.mark.parametrize("N,nb,cuts", [(96, 64, (0, 37, 96)), (128, 100, (0, 1, 64, 127, 128))])
@@ -108,4 +108,24 @@ def test_correction_stream_variants(gpu, oracle, N, nb):
         k.apply_delta_pow(L_BOX, gd, N, nb, logk, ratio, norm, slabstart_y=s0, nslab_y=s1 - s0)
         rel = np.abs(gd.cpu().numpy() - gos) / np.maximum(np.abs(gos), 1e-30)
         assert rel.max() < 1e-6, (s0, s1, rel.max())
+    k.close()
+
+
+def test_binning_rows_warp_groups(gpu, oracle):
+    """N=560: rows of 281 modes are 17 runs, a two-row tile is 34 runs, so tiles go to
+    groups of two warps sharing a stage ring (the N >= 1024 shape, at a size the oracle
+    bins in seconds)."""
+    import torch
+    N, nb = 560, 120
+    g = W.make_grid(N, seed=11)
+    nk_o, p_o, c_o, _ = oracle.total_powerspectrum(g, N, nb)
+    k = _instance(gpu, nb)
+    gd = torch.as_tensor(g).cuda()
+    del g
+    for rows, stages in ((256, 2), (128, 3)):
+        for tma, tol in ((5, TOL_EXACT), (6, TOL_LEAN)):
+            k.set_tuning(tma=tma, rows=rows, stages=stages)
+            nk_g, p_g, c_g, _ = k.total_powerspectrum(N, gd, nb)
+            assert nk_g == nk_o and np.array_equal(c_g, c_o)
+            assert cases.rel_err(p_g, p_o) < tol, (rows, stages, tma)
     k.close()
