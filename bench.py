@@ -42,6 +42,69 @@ def peaks():
         return 6800.0, "fallback"
 
 
+class NvmlClockSampler:
+    """SM clock and clock-event (throttle) reasons polled every millisecond through NVML
+    (the driver's libnvidia-ml) while running; a timed region of a few ms still gets
+    samples.  Falls back to ClockSampler (nvidia-smi) where NVML cannot be opened."""
+
+    REASONS = {0x4: "sw_power_cap", 0x8: "hw_slowdown", 0x20: "sw_thermal_slowdown",
+               0x40: "hw_thermal_slowdown", 0x80: "hw_power_brake_slowdown"}
+
+    def __init__(self, gpu_index=0):
+        import ctypes
+        self.C = ctypes
+        self.samples = []
+        self.stop = False
+        vis = os.environ.get("CUDA_VISIBLE_DEVICES", "")
+        ids = [x for x in vis.split(",") if x.strip()]
+        idx = int(ids[gpu_index]) if gpu_index < len(ids) and ids[gpu_index].strip().isdigit() else gpu_index
+        self.lib = ctypes.CDLL("libnvidia-ml.so.1")
+        if self.lib.nvmlInit_v2() != 0:
+            raise RuntimeError("nvmlInit failed")
+        self.h = ctypes.c_void_p()
+        if self.lib.nvmlDeviceGetHandleByIndex_v2(ctypes.c_uint(idx), ctypes.byref(self.h)) != 0:
+            raise RuntimeError("no NVML handle")
+        mx = ctypes.c_uint()
+        self.max_mhz = float(mx.value) if self.lib.nvmlDeviceGetMaxClockInfo(self.h, 1, ctypes.byref(mx)) == 0 else None
+        self.reason_fn = getattr(self.lib, "nvmlDeviceGetCurrentClocksEventReasons", None) or \
+            getattr(self.lib, "nvmlDeviceGetCurrentClocksThrottleReasons")
+
+    def _poll(self):
+        C = self.C
+        clk, rs = C.c_uint(), C.c_ulonglong()
+        while not self.stop:
+            if self.lib.nvmlDeviceGetClockInfo(self.h, 1, C.byref(clk)) == 0 and \
+                    self.reason_fn(self.h, C.byref(rs)) == 0:
+                self.samples.append((float(clk.value), int(rs.value)))
+            time.sleep(0.001)
+
+    def __enter__(self):
+        self.t = threading.Thread(target=self._poll, daemon=True)
+        self.t.start()
+        return self
+
+    def __exit__(self, *a):
+        self.stop = True
+        self.t.join(timeout=2)
+
+    def summary(self):
+        sm = [c for c, _ in self.samples]
+        reasons = set()
+        for _, r in self.samples:
+            for bit, name in self.REASONS.items():
+                if r & bit:
+                    reasons.add(name)
+        return {"sm_mhz": float(np.median(sm)) if sm else None, "sm_max_mhz": self.max_mhz,
+                "reasons": sorted(reasons), "samples": len(sm), "source": "nvml, 1 ms polling"}
+
+
+def clock_sampler(gpu_index=0):
+    try:
+        return NvmlClockSampler(gpu_index)
+    except Exception:
+        return ClockSampler(gpu_index)
+
+
 class ClockSampler:
     """nvidia-smi clocks/throttle reasons sampled every 200 ms while running."""
 
@@ -166,7 +229,7 @@ def run_gb300(args, cfg):
     if world > 1:
         dist.barrier()
     torch.cuda.synchronize()
-    with ClockSampler(local) as clk:
+    with clock_sampler(local) as clk:
         ev0.record(stream)
         for i in range(args.steps):
             k.add_nu_power_to_rhogrid(a_list[args.warmup + i], L, grid, N, slab0, nslab)
@@ -212,10 +275,14 @@ def run_gb300(args, cfg):
         dom = {"kernel": k3_name + " (grid multiply)", "bytes": 2 * bytes_grid, "ms": k3_ms, "gbs": k3_gbs}
     else:
         dom = {"kernel": k1_name + " (binning)", "bytes": bytes_grid, "ms": k1_ms, "gbs": k1_gbs}
-    traffic = None
+    traffic, traffic_note = None, None
     try:
         with open(os.path.join(ROOT, "profiles", "traffic.json")) as f:
             traffic = json.load(f).get(dom["kernel"].split()[0])
+        if traffic is not None and bytes_grid != 538968064:
+            # captured on the N=512 grid; DRAM bytes scale with the grid
+            traffic = traffic * bytes_grid / 538968064
+            traffic_note = "ncu capture at N=512 scaled by the grid size"
     except Exception:
         pass
     res = {
@@ -232,7 +299,7 @@ def run_gb300(args, cfg):
         "stage_gbs": {"K1": k1_gbs, "K3": k3_gbs},
         "roofline": {"bound": "hbm", "kernel": dom["kernel"], "achieved": dom["gbs"], "peak": hbm,
                      "peak_kind": peak_kind, "unit": "GB/s", "frac": (dom["gbs"] / hbm) if dom["gbs"] else None,
-                     "traffic": traffic, "algorithmic_bytes_per_launch": dom["bytes"]},
+                     "traffic": traffic, "traffic_note": traffic_note, "algorithmic_bytes_per_launch": dom["bytes"]},
         "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": bytes_grid,
                 "d2h_bytes_per_step": bytes_grid, "ms_per_step": 1e3 * t_e2e / args.steps},
         "gpu_launches": launches,
@@ -498,7 +565,7 @@ def run_batch(args, cfg):
         dcdm_h.copy_(torch.from_numpy(base * a_list[0] / a_end))
         tune = B.autotune(np.full(MT, a_list[0]), dcdm_h, reps=2)
     dev_ms, host_s, outs = [], [], []
-    with ClockSampler(0) as clk:
+    with clock_sampler(0) as clk:
         for i in range(nsteps):
             dcdm_h.copy_(torch.from_numpy(base * a_list[i] / a_end))
             t0 = time.perf_counter()

@@ -229,6 +229,7 @@ extern "C" int kspace_gpu_init_omega_nu(kspace_ctx* c, const double MNu[3], doub
     B.tcmb0 = tcmb0;
     B.kBtnu = kBolEvK * (pow(4 / 11., 1 / 3.) * 1.00328) * tcmb0;
     B.rhocrit = (3 * kHubble * h * kHubble * h) / (8 * kPi * kGravity);
+    B.irhocrit = 1.0 / B.rhocrit;
     B.conv = rho_nu_conversion();
     B.omegag0 = 4 * kStefanBoltzmann / (kLightCgs * kLightCgs * kLightCgs) * pow(tcmb0, 4) / B.rhocrit;
     for (int mi = 0; mi < kNuSpecies; mi++) {

@@ -118,8 +118,7 @@ __global__ void kb_fs_segments(BatchDev b, GL4b gl) {
                 const double c = 0.5 * (xa + xb), h = 0.5 * (xb - xa);
                 const int j = q & 1;
                 const double x = (q < 2) ? c - h * gl.x[j] : c + h * gl.x[j];
-                const double ax = exp(x);
-                v = gl.w[j] * h * (1. / (ax * (ax * hubble(*b.insts[i].B, ax, x))));
+                v = gl.w[j] * h * fsl_integrand(*b.insts[i].B, x);
             }
             if (q == 0) b.insts[i].fs_x[seg] = xa;
         }

@@ -45,12 +45,17 @@ struct RhoTable {
     int has_table;
     double mnu;
     double loga[kNRhoTab], rhonu[kNRhoTab], c[kNRhoTab];
+    // filled with c (k_rho_splines): the node-independent spline terms of each segment
+    // (as cspline_seg forms them), 1 / knot spacing and 1 / mnu, for fsl_integrand
+    double sb[kNRhoTab], sd[kNRhoTab];
+    double inv_dx, imnu;
 };
 
 // omega_nu_single.h:100-113 (_omega_nu, _hybrid_nu) plus the parameters of the host's
 // hubble_function (delta_tot_table_test.c:33-45; curvature as gadget-2/0003 patch:38).
 struct Background {
     double rhocrit, kBtnu, tcmb0, conv, omegag0;
+    double irhocrit;  // 1 / rhocrit
     int deg[kNuSpecies];
     double mnu[kNuSpecies];
     double mnu_J[kNuSpecies];  // mass inside J's argument (get_delta_nu's mnu, delta_tot_table.c:507)
@@ -198,6 +203,55 @@ KSP_HD double hubble(const Background& B, double a, double loga = NAN) {
     if (B.radiation) om += B.omegag0 / (a3 * a);
     return B.hubble * sqrt(om);
 }
+
+#ifdef __CUDACC__
+// rho_nu for fsl_integrand: the same branches as rho_nu, with 1/a given and the table
+// spline in per-segment polynomial form (RhoTable::sb, sd).
+__device__ __forceinline__ double rho_nu_ia(const RhoTable& T, double a, double ia, double loga, double kT,
+                                            double conv) {
+    const double amnu = a * T.mnu;
+    const double kTamnu = kT * ia * T.imnu, kTamnu2 = kTamnu * kTamnu;
+    bool nonrel = kNuSw * kNuSw * kTamnu2 < 1;
+    bool rel = !nonrel && amnu < 1e-6 * kT;
+    if (!nonrel && !rel && (!T.has_table || loga < T.loga[0])) {
+        rel = amnu < 1e-4 * kT;
+        nonrel = !rel;
+    }
+    if (nonrel) {
+        const double ia4 = (ia * ia) * (ia * ia);
+        return amnu * (kT * kT * kT) * ia4 *
+               (1.5 * kZeta3 + kTamnu2 * 45. / 4. * 1.0369277551433704 +
+                2835. / 32. * kTamnu2 * kTamnu2 * 1.0083492773819229 +
+                80325 / 32. * kTamnu2 * kTamnu2 * kTamnu2 * 1.0020083928260826) * conv;
+    }
+    if (rel) {
+        const double t = kPi * kT * ia, t2 = t * t;
+        return 7 * (t2 * t2) / 120. * conv;
+    }
+    int i = (int)((loga - T.loga[0]) * T.inv_dx);
+    i = i < 0 ? 0 : (i > kNRhoTab - 2 ? kNRhoTab - 2 : i);
+    while (i > 0 && loga < T.loga[i]) i--;
+    while (i < kNRhoTab - 2 && loga >= T.loga[i + 1]) i++;
+    const double dx = loga - T.loga[i];
+    return T.rhonu[i] + dx * (T.sb[i] + dx * (T.c[i] + dx * T.sd[i]));
+}
+
+// The fslength integrand 1/(a^2 H(a)) at a = e^x (delta_tot_table.c:378-383) with H as
+// hubble() forms it, 1/a computed once (one exp, one sqrt, two divisions per node).
+__device__ __forceinline__ double fsl_integrand(const Background& B, double x) {
+    const double a = exp(x);
+    const double ia = 1.0 / a;
+    const double ia2 = ia * ia, ia3 = ia2 * ia;
+    double om = B.Omega_nonu_H * ia3 + B.OmegaLambda;
+    if (B.OmegaK != 0.0) om += B.OmegaK * ia2;
+    double rhonu = 0;
+    for (int mi = 0; mi < kNuSpecies; mi++)
+        if (B.deg[mi] > 0) rhonu += B.deg[mi] * rho_nu_ia(B.tab[mi], a, ia, x, B.kBtnu, B.conv);
+    om += rhonu * B.irhocrit;
+    if (B.radiation) om += B.omegag0 * (ia3 * ia);
+    return ia2 / (B.hubble * sqrt(om));
+}
+#endif
 
 // delta_tot_table.c:613-617
 KSP_HD double get_delta_tot(double dnu, double dcdm, double OmegaNua3, double Omeganonu, double Omeganu1,
@@ -501,16 +555,24 @@ __device__ __forceinline__ void gk61_lane_sums(const Gk61Nodes& N, const double*
     double z = (b4 ? rs[1] : rs[0]) + __shfl_xor_sync(0xffffffffu, b4 ? rs[0] : rs[1], 16);
 #pragma unroll
     for (int o = 8; o > 0; o >>= 1) z += __shfl_xor_sync(0xffffffffu, z, o);
-    const double rk[2] = {rk0, rk1};
-    const double rg[2] = {__shfl_sync(0xffffffffu, y, 4), __shfl_sync(0xffffffffu, y, 20)};
-    const double ra[2] = {__shfl_sync(0xffffffffu, y, 8), __shfl_sync(0xffffffffu, y, 24)};
-    const double rsum[2] = {__shfl_sync(0xffffffffu, z, 0), __shfl_sync(0xffffffffu, z, 16)};
-    for (int t = 0; t < nint; t++) {
-        const double err = (rk[t] - rg[t]) * h[t];
-        out[t].result = rk[t] * h[t];
-        out[t].resabs = ra[t] * fabs(h[t]);
-        out[t].resasc = rsum[t] * fabs(h[t]);
-        out[t].abserr = rescale_error(err, out[t].resabs, out[t].resasc);
+    // the outputs of interval t on the lanes with t = lane & 1 (one evaluation per lane),
+    // then broadcast
+    const int t = lane & 1;
+    const double ht = t ? h[1] : h[0];
+    const double rkt = t ? rk1 : rk0;
+    const double rgt = __shfl_sync(0xffffffffu, y, t ? 20 : 4);
+    const double rat = __shfl_sync(0xffffffffu, y, t ? 24 : 8);
+    const double rst = __shfl_sync(0xffffffffu, z, t ? 16 : 0);
+    GkOut o;
+    o.result = rkt * ht;
+    o.resabs = rat * fabs(ht);
+    o.resasc = rst * fabs(ht);
+    o.abserr = rescale_error((rkt - rgt) * ht, o.resabs, o.resasc);
+    for (int u = 0; u < nint; u++) {
+        out[u].result = __shfl_sync(0xffffffffu, o.result, u);
+        out[u].resabs = __shfl_sync(0xffffffffu, o.resabs, u);
+        out[u].resasc = __shfl_sync(0xffffffffu, o.resasc, u);
+        out[u].abserr = __shfl_sync(0xffffffffu, o.abserr, u);
     }
 }
 
@@ -533,8 +595,7 @@ __device__ __forceinline__ void gk61_warp_c(const F& f, const Gk61Nodes& N, int 
         if (s < nslots) {
             const int t = s >= 61 ? 1 : 0;
             const int j = s - 61 * t;
-            const double x = __dadd_rn(c[t], __dmul_rn(h[t], N.x[j]));
-            fv[m] = f.node(slot[t], j, x);
+            fv[m] = f.node_at(slot[t], j, c[t], h[t], N.x[j]);
         }
     }
     gk61_lane_sums(N, fv, nslots, nint, h, out);
@@ -641,8 +702,7 @@ __device__ __forceinline__ void gk61_block_c(const F& f, const Gk61Nodes& N, int
     for (int s = tid; s < nslots; s += blockDim.x) {
         const int t = s >= 61 ? 1 : 0;
         const int j = s - 61 * t;
-        const double x = __dadd_rn(c[t], __dmul_rn(h[t], N.x[j]));
-        sh.fv[s] = f.node(slot[t], j, x);
+        sh.fv[s] = f.node_at(slot[t], j, c[t], h[t], N.x[j]);
     }
     __syncthreads();
     if (tid < 32) {  // warp 0: the sums exactly as gk61_warp_c forms them
@@ -856,6 +916,21 @@ struct DnuIntegrandC {
             t.j = __ldg(nc.j + q);
         } else {
             t = dnu_node_terms(B, fs_x, fs_y, fs_c, nfs, fs_x0, fs_inv, kx, na, x);
+        }
+        return dnu_combine(t, k_over_m, qc, nfl, ky, kc, sb, sd, na, ks);
+    }
+    // node jn of the interval with centre c and half-length h: x = c + h x_jn is needed
+    // only where the node table has no entry
+    __device__ double node_at(int slot, int jn, double c, double h, double xj) const {
+        NodeTerms t;
+        if (slot >= 0) {
+            const int q = slot * 61 + jn;
+            t.g = __ldg(nc.g + q);
+            t.fsl = __ldg(nc.fsl + q);
+            t.dx = __ldg(nc.dx + q);
+            t.j = __ldg(nc.j + q);
+        } else {
+            t = dnu_node_terms(B, fs_x, fs_y, fs_c, nfs, fs_x0, fs_inv, kx, na, __dadd_rn(c, __dmul_rn(h, xj)));
         }
         return dnu_combine(t, k_over_m, qc, nfl, ky, kc, sb, sd, na, ks);
     }

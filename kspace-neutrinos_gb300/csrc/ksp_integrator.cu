@@ -90,8 +90,16 @@ __global__ void k_rho_splines(Background* B, double* scratch) {
     const int s = threadIdx.x;
     if (s >= kNuSpecies) return;
     RhoTable& T = B->tab[s];
+    T.imnu = 1.0 / T.mnu;
     if (!B->deg[s] || !T.has_table) return;
     natural_spline_coeffs(T.loga, T.rhonu, kNRhoTab, T.c, scratch + s * 2 * kNRhoTab);
+    // the node-independent terms of cspline_seg, per segment
+    for (int i = 0; i + 1 < kNRhoTab; i++) {
+        const double h = T.loga[i + 1] - T.loga[i];
+        T.sb[i] = (T.rhonu[i + 1] - T.rhonu[i]) / h - h * (T.c[i + 1] + 2.0 * T.c[i]) / 3.0;
+        T.sd[i] = (T.c[i + 1] - T.c[i]) / (3.0 * h);
+    }
+    T.inv_dx = (kNRhoTab - 1) / (T.loga[kNRhoTab - 1] - T.loga[0]);
 }
 
 void launch_background_tables(Background* dB, double a0, cudaStream_t st, unsigned* status) {
@@ -236,10 +244,7 @@ struct GL4 { double x[2], w[2]; };  // positive half of the 4-point Gauss-Legend
 
 struct FslIntegrand {  // delta_tot_table.c:378-383
     const Background* B;
-    __device__ double operator()(double loga) const {
-        const double a = exp(loga);
-        return 1. / (a * (a * hubble(*B, a, loga)));
-    }
+    __device__ double operator()(double loga) const { return fsl_integrand(*B, loga); }
 };
 
 // 4 lanes per segment: lane q evaluates node q of the 4-point Gauss-Legendre rule on
