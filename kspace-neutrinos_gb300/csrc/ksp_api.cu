@@ -86,9 +86,17 @@ extern "C" int kspace_gpu_create(kspace_ctx** out, int device) {
     CK(dalloc(&c->dB, 1));
     for (int i = 0; i < 5; i++) CK(cudaEventCreate(&c->ev[i]));
     CK(cudaStreamCreateWithFlags(&c->side, cudaStreamNonBlocking));
+    CK(cudaStreamCreateWithFlags(&c->copy, cudaStreamNonBlocking));
+    for (int i = 0; i < kspace_ctx::kChunks; i++) {
+        CK(cudaEventCreateWithFlags(&c->ev_up[i], cudaEventDisableTiming));
+        CK(cudaEventCreateWithFlags(&c->ev_done[i], cudaEventDisableTiming));
+    }
+    CK(cudaEventCreateWithFlags(&c->ev_copy_start, cudaEventDisableTiming));
+    CK(cudaEventCreateWithFlags(&c->ev_copy_end, cudaEventDisableTiming));
     CK(cudaEventCreateWithFlags(&c->ev_fork, cudaEventDisableTiming));
     CK(cudaEventCreateWithFlags(&c->ev_join, cudaEventDisableTiming));
     if (const char* e = getenv("KSPACE_GPU_TMA")) c->tma = atoi(e);
+    if (const char* e = getenv("KSPACE_GPU_CHUNKS")) c->chunks = atoi(e);
     if (const char* e = getenv("KSPACE_GPU_ROWS")) c->rows = atoi(e);
     if (const char* e = getenv("KSPACE_GPU_STAGES")) c->stages = atoi(e);
     if (const char* e = getenv("KSPACE_GPU_QAG_WARPS")) c->qag_warps = atoi(e);
@@ -155,6 +163,13 @@ extern "C" int kspace_gpu_destroy(kspace_ctx* c) {
     if (c->ev_fork) cudaEventDestroy(c->ev_fork);
     if (c->ev_join) cudaEventDestroy(c->ev_join);
     if (c->side) cudaStreamDestroy(c->side);
+    for (int i = 0; i < kspace_ctx::kChunks; i++) {
+        if (c->ev_up[i]) cudaEventDestroy(c->ev_up[i]);
+        if (c->ev_done[i]) cudaEventDestroy(c->ev_done[i]);
+    }
+    if (c->ev_copy_start) cudaEventDestroy(c->ev_copy_start);
+    if (c->ev_copy_end) cudaEventDestroy(c->ev_copy_end);
+    if (c->copy) cudaStreamDestroy(c->copy);
     if (c->own_stream) cudaStreamDestroy(c->own_stream);
     delete c;
     return KSPACE_OK;
@@ -663,8 +678,14 @@ static int update_device(kspace_ctx* c, double a, int nk_in, const double* keff_
     if (nk_in != c->nk) return KSPACE_ERR_NK_MISMATCH;
     if (c->nk < 2) return KSPACE_ERR_NK_SMALL;
     const double loga = log(a);
-    CK(cudaMemsetAsync(I.qag_max, 0, sizeof(int), c->stream));
-    CK(cudaMemsetAsync(I.qag_total, 0, sizeof(long long), c->stream));
+    // the delta_cdm-independent part already ran beside the binning pass (it also zeroes
+    // the QAG statistics)
+    const bool prepared = c->prep_valid && c->prep_Na == c->ia + 1 && c->prep_loga == loga &&
+                          !(loga - c->h_scalefact[c->ia - 1] < kFloatAcc) && c->ia < I.namax;
+    if (!prepared) {
+        CK(cudaMemsetAsync(I.qag_max, 0, sizeof(int), c->stream));
+        CK(cudaMemsetAsync(I.qag_total, 0, sizeof(long long), c->stream));
+    }
     if (loga - c->h_scalefact[c->ia - 1] < kFloatAcc) {
         // same scale factor: return delta_nu_last unchanged (delta_tot_table.c:209-213)
         CK(cudaMemcpyAsync(I.dnu, I.nu_last, sizeof(double) * c->nk, cudaMemcpyDeviceToDevice, c->stream));
@@ -682,15 +703,17 @@ static int update_device(kspace_ctx* c, double a, int nk_in, const double* keff_
         return sync_status(c);
     }
     if (c->ia >= I.namax) return KSPACE_ERR_NAMAX;
-    // provisional row from delta_nu_last (delta_tot_table.c:222)
-    launch_update_row(I, c->nk, c->ia, a, loga, I.dcdm, I.nu_last, c->stream);
+    // provisional row from delta_nu_last (delta_tot_table.c:222): written here, or, after
+    // the prepared scalars, as the rows' splines are solved
+    const int prov_row = c->ia;
+    if (!prepared) launch_update_row(I, c->nk, prov_row, a, loga, I.dcdm, I.nu_last, c->stream);
     c->h_scalefact[c->ia] = loga;
     c->ia++;
     const int Na = c->ia;
-    if (c->prep_valid && c->prep_Na == Na && c->prep_loga == loga) {
-        // the delta_cdm-independent part already ran beside the binning pass
+    if (prepared) {
         CK(cudaStreamWaitEvent(c->stream, c->ev_join, 0));
-        launch_integrator_rest(I, c->nk, Na, c->nspec, c->spec_ids, c->qag_warps, c->stream, c->qag_split);
+        launch_integrator_rest(I, c->nk, Na, c->nspec, c->spec_ids, c->qag_warps, c->stream, c->qag_split, prov_row,
+                               true);
     } else {
         launch_delta_nu_combined(I, c->nk, Na, a, loga, c->loga0, c->TimeTransfer, c->fact_valid, c->nspec,
                                  c->spec_ids, c->qag_warps, c->stream, c->qag_split);
@@ -700,7 +723,7 @@ static int update_device(kspace_ctx* c, double a, int nk_in, const double* keff_
     const bool commit = a >= exp(c->h_scalefact[Na - 2]) + 0.009;
     launch_finish_update(I, c->nk, commit ? Na - 1 : -1, a, loga, want_corr ? keff_d : nullptr, dnu_out_d,
                          want_corr ? c->logk_d : nullptr, want_corr ? c->ratio_d : nullptr,
-                         want_corr ? c->corr : CorrTable{}, c->norm_d, c->stream);
+                         want_corr ? c->corr : CorrTable{}, c->norm_d, c->stream, prepared);
     g_launches += 10;
     if (commit) {
         c->fact_valid = Na - 2 > 0 ? Na - 2 : 0;
@@ -811,12 +834,7 @@ static int get_geo(kspace_ctx* c, int N, int nrbins, Geo** out) {
 
 // Device pointer for the grid: the caller's device memory, or the staging buffer after
 // a host->device copy.
-static int grid_in(kspace_ctx* c, const void* grid, size_t bytes, float** gd, bool* staged) {
-    if (is_device_ptr(grid)) {
-        *gd = const_cast<float*>(reinterpret_cast<const float*>(grid));
-        *staged = false;
-        return KSPACE_OK;
-    }
+static int stage_alloc(kspace_ctx* c, size_t bytes) {
     if (c->stage_bytes < bytes) {
         if (c->stage_d) cudaFree(c->stage_d);
         c->stage_d = nullptr;
@@ -824,15 +842,42 @@ static int grid_in(kspace_ctx* c, const void* grid, size_t bytes, float** gd, bo
         CK(cudaMalloc(&c->stage_d, bytes));
         c->stage_bytes = bytes;
     }
+    return KSPACE_OK;
+}
+
+static int grid_in(kspace_ctx* c, const void* grid, size_t bytes, float** gd, bool* staged) {
+    if (is_device_ptr(grid)) {
+        *gd = const_cast<float*>(reinterpret_cast<const float*>(grid));
+        *staged = false;
+        return KSPACE_OK;
+    }
+    const int st = stage_alloc(c, bytes);
+    if (st) return st;
     CK(cudaMemcpyAsync(c->stage_d, grid, bytes, cudaMemcpyHostToDevice, c->stream));
     *gd = reinterpret_cast<float*>(c->stage_d);
     *staged = true;
     return KSPACE_OK;
 }
 
+// Slab chunks of a host grid: chunk k covers local slabs [first[k], first[k+1]).
+struct SlabChunks {
+    int n = 0;
+    int first[kspace_ctx::kChunks + 1];
+    size_t slab_bytes = 0;
+};
+static SlabChunks make_chunks(int nslab, int pmgrid, int want) {
+    SlabChunks ch;
+    want = want < 1 ? 1 : (want > kspace_ctx::kChunks ? kspace_ctx::kChunks : want);
+    ch.n = nslab < want ? (nslab > 0 ? nslab : 1) : want;
+    for (int k = 0; k <= ch.n; k++) ch.first[k] = (int)((long long)nslab * k / ch.n);
+    ch.slab_bytes = sizeof(float) * 2 * (size_t)pmgrid * (pmgrid / 2 + 1);
+    return ch;
+}
+
 // K1 + allreduce + normalisation into compacted arrays (device): power, keff (grid
 // units), dcdm and keff (physical) for the integrator.
-static int bin_grid(kspace_ctx* c, Geo* G, const float* gd, int pmgrid, int slab0, int nslab, double BoxSize) {
+static int bin_grid(kspace_ctx* c, Geo* G, const float* gd, int pmgrid, int slab0, int nslab, double BoxSize,
+                    const SlabChunks* ch = nullptr) {
     NEED(c->table_ready && c->buf_nb >= G->g.nrbins, KSPACE_ERR_ORDER);
     const int nb = G->g.nrbins;
     G->g.slab0 = slab0;
@@ -841,9 +886,26 @@ static int bin_grid(kspace_ctx* c, Geo* G, const float* gd, int pmgrid, int slab
     CK(cudaMemsetAsync(c->bin_sum_d, 0, sizeof(double) * (nb + 1), c->stream));
     c->F0sq_d = c->bin_sum_d + nb;
     if (c->prof) cudaEventRecord(c->ev[0], c->stream);
-    if (launch_bin_power(G->g, gd, c->bin_sum_d, c->F0sq_d, c->status_d, c->tma, c->rows, c->stages, c->stream) < 0)
-        return KSPACE_ERR_CUDA;
-    g_launches += 1;
+    if (!ch) {
+        if (launch_bin_power(G->g, gd, c->bin_sum_d, c->F0sq_d, c->status_d, c->tma, c->rows, c->stages,
+                             c->stream) < 0)
+            return KSPACE_ERR_CUDA;
+        g_launches += 1;
+    } else {
+        // each chunk as soon as its upload has landed
+        for (int k = 0; k < ch->n; k++) {
+            GridGeom gk = G->g;
+            gk.slab0 = slab0 + ch->first[k];
+            gk.nslab = ch->first[k + 1] - ch->first[k];
+            gk.nmodes = (long long)gk.nslab * pmgrid * (pmgrid / 2 + 1);
+            CK(cudaStreamWaitEvent(c->stream, c->ev_up[k], 0));
+            if (gk.nslab > 0 &&
+                launch_bin_power(gk, gd + (ch->first[k] * ch->slab_bytes) / sizeof(float), c->bin_sum_d, c->F0sq_d,
+                                 c->status_d, c->tma, c->rows, c->stages, c->stream) < 0)
+                return KSPACE_ERR_CUDA;
+            g_launches += 1;
+        }
+    }
     if (c->prof) cudaEventRecord(c->ev[1], c->stream);
     if (c->ar_fn) {
         CK(cudaMemcpyAsync(c->ar_h, c->bin_sum_d, sizeof(double) * (nb + 1), cudaMemcpyDeviceToHost, c->stream));
@@ -887,14 +949,37 @@ extern "C" int kspace_gpu_total_powerspectrum(kspace_ctx* c, int dims, const voi
     return KSPACE_OK;
 }
 
-static int correct_grid(kspace_ctx* c, Geo* G, float* gd, double BoxSize, int nk) {
+static int correct_grid(kspace_ctx* c, Geo* G, float* gd, double BoxSize, int nk, const SlabChunks* ch = nullptr,
+                        void* host = nullptr) {
     CorrTable corr = c->corr;
     corr.nk = nk;
     const float lnscale = (float)log(2 * kPi / BoxSize);
     if (c->prof) cudaEventRecord(c->ev[2], c->stream);
-    if (launch_apply_correction(G->g, gd, corr, lnscale, c->status_d, c->tma, c->rows, c->stages, c->stream) < 0)
-        return KSPACE_ERR_CUDA;
-    g_launches += 1;
+    if (!ch) {
+        if (launch_apply_correction(G->g, gd, corr, lnscale, c->status_d, c->tma, c->rows, c->stages, c->stream) < 0)
+            return KSPACE_ERR_CUDA;
+        g_launches += 1;
+    } else {
+        // each chunk goes back to the host while the next one is corrected
+        for (int k = 0; k < ch->n; k++) {
+            GridGeom gk = G->g;
+            gk.slab0 = G->g.slab0 + ch->first[k];
+            gk.nslab = ch->first[k + 1] - ch->first[k];
+            gk.nmodes = (long long)gk.nslab * G->g.N * (G->g.N / 2 + 1);
+            const size_t off = ch->first[k] * ch->slab_bytes, len = (size_t)gk.nslab * ch->slab_bytes;
+            if (gk.nslab > 0 && launch_apply_correction(gk, gd + off / sizeof(float), corr, lnscale, c->status_d,
+                                                        c->tma, c->rows, c->stages, c->stream) < 0)
+                return KSPACE_ERR_CUDA;
+            g_launches += 1;
+            CK(cudaEventRecord(c->ev_done[k], c->stream));
+            CK(cudaStreamWaitEvent(c->copy, c->ev_done[k], 0));
+            if (len)
+                CK(cudaMemcpyAsync(reinterpret_cast<char*>(host) + off, reinterpret_cast<char*>(gd) + off, len,
+                                   cudaMemcpyDeviceToHost, c->copy));
+        }
+        CK(cudaEventRecord(c->ev_copy_end, c->copy));
+        CK(cudaStreamWaitEvent(c->stream, c->ev_copy_end, 0));
+    }
     if (c->prof) cudaEventRecord(c->ev[3], c->stream);
     return KSPACE_OK;
 }
@@ -910,9 +995,27 @@ extern "C" int kspace_gpu_add_nu_power_to_rhogrid(kspace_ctx* c, double Time, do
     if (c->prof) cudaEventRecord(c->ev[4], c->stream);
     const size_t bytes = sizeof(float) * 2 * (size_t)nslab * pmgrid * (pmgrid / 2 + 1);
     float* gd;
-    bool staged;
-    st = grid_in(c, grid, bytes, &gd, &staged);
-    if (st) return st;
+    const bool staged = !is_device_ptr(grid);
+    SlabChunks ch;
+    if (staged) {
+        // a host grid: upload in slab chunks on the copy stream (after the work queued so
+        // far on the context's stream, which may still read the staging buffer)
+        st = stage_alloc(c, bytes);
+        if (st) return st;
+        gd = reinterpret_cast<float*>(c->stage_d);
+        ch = make_chunks(nslab, pmgrid, c->chunks);
+        CK(cudaEventRecord(c->ev_copy_start, c->stream));
+        CK(cudaStreamWaitEvent(c->copy, c->ev_copy_start, 0));
+        for (int k = 0; k < ch.n; k++) {
+            const size_t off = ch.first[k] * ch.slab_bytes, len = (size_t)(ch.first[k + 1] - ch.first[k]) * ch.slab_bytes;
+            if (len)
+                CK(cudaMemcpyAsync(reinterpret_cast<char*>(gd) + off, reinterpret_cast<const char*>(grid) + off, len,
+                                   cudaMemcpyHostToDevice, c->copy));
+            CK(cudaEventRecord(c->ev_up[k], c->copy));
+        }
+    } else {
+        gd = reinterpret_cast<float*>(grid);
+    }
     // The integrator work that does not depend on this step's delta_cdm (scalars, knot
     // factorisation, fslength and node tables) starts now on the side stream, beside
     // the binning pass; update_device waits for it.  Only for the common case: a new
@@ -934,7 +1037,7 @@ extern "C" int kspace_gpu_add_nu_power_to_rhogrid(kspace_ctx* c, double Time, do
         }
     }
     // compute_neutrino_power_spectrum (interface_gadget.c:75-102)
-    st = bin_grid(c, G, gd, pmgrid, slab0, nslab, BoxSize);
+    st = bin_grid(c, G, gd, pmgrid, slab0, nslab, BoxSize, staged ? &ch : nullptr);
     if (st) return st;
     // the integrator (interface_common.c:125-148)
     st = update_device(c, Time, G->nk, c->keff_d, c->I.dcdm, c->dnu_out_d, true);
@@ -942,9 +1045,8 @@ extern "C" int kspace_gpu_add_nu_power_to_rhogrid(kspace_ctx* c, double Time, do
     c->last_nk = G->nk;
     c->last_BoxSize = BoxSize;
     // the multiply (interface_gadget.c:163-188)
-    st = correct_grid(c, G, gd, BoxSize, G->nk);
+    st = correct_grid(c, G, gd, BoxSize, G->nk, staged ? &ch : nullptr, staged ? grid : nullptr);
     if (st) return st;
-    if (staged) CK(cudaMemcpyAsync(grid, gd, bytes, cudaMemcpyDeviceToHost, c->stream));
     st = sync_status(c);
     if (c->prof) {
         cudaEventElapsedTime(&c->stage_ms[0], c->ev[0], c->ev[1]);

@@ -80,6 +80,12 @@ struct kspace_ctx {
     // binning pass runs (add_nu_power_to_rhogrid)
     cudaStream_t side = nullptr;
     cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
+    // host grids move in slab chunks on a copy stream: the binning pass runs behind the
+    // upload, the download behind the correction pass
+    static constexpr int kChunks = 16;
+    int chunks = 8;  // slab chunks of a host grid (1..kChunks)
+    cudaStream_t copy = nullptr;
+    cudaEvent_t ev_up[kChunks] = {}, ev_done[kChunks] = {}, ev_copy_start = nullptr, ev_copy_end = nullptr;
     bool prep_valid = false;
     int prep_Na = 0;
     double prep_loga = 0;

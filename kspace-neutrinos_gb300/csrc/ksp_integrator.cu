@@ -166,6 +166,17 @@ void launch_update_row(const IntegratorDev& I, int nk, int row, double a, double
     k_update_row<<<(nk + 255) / 256, 256, 0, st>>>(I, nk, row, a, loga, dcdm, dnu);
 }
 
+// the same row from the call's scalars (after k_scalars), delta_nu_last and delta_cdm
+__global__ void k_update_row_s(IntegratorDev I, int nk, int row) {
+    const StepScalars& S = *I.sc;
+    for (int ik = blockIdx.x * blockDim.x + threadIdx.x; ik < nk; ik += gridDim.x * blockDim.x)
+        I.dtot[(size_t)ik * I.ld + row] =
+            get_delta_tot(I.nu_last[ik], I.dcdm[ik], S.OmegaNua3, S.Omeganonu, S.OmegaNu1, S.partnu);
+}
+void launch_update_row_scalars(const IntegratorDev& I, int nk, int row, cudaStream_t st) {
+    k_update_row_s<<<(nk + 255) / 256, 256, 0, st>>>(I, nk, row);
+}
+
 // delta_tot_table.c:94-129: transfer spline, first row (fresh start), delta_nu_init
 __global__ void k_delta_tot_init(IntegratorDev I, int nk, const double* wavenum, const double* dcdm, int fresh,
                                  double TimeTransfer) {
@@ -210,6 +221,10 @@ void launch_delta_tot_init(const IntegratorDev& I, int nk, const double* wavenum
 // so the per-row sweeps need no divisions.
 __global__ void k_scalars(IntegratorDev I, int Na, double a, double loga, double loga0, double TimeTransfer,
                           int start_row, int write_knot) {
+    if (threadIdx.x == 0) {  // this call's QAG statistics start from zero
+        *I.qag_max = 0;
+        *I.qag_total = 0;
+    }
     if (write_knot) {  // the provisional knot (update_row writes the same value)
         if (threadIdx.x == 0) I.scalefact[Na - 1] = loga;
         __syncthreads();
@@ -358,12 +373,20 @@ __global__ void k_fs_coeffs(IntegratorDev I, int Nfs, double loga0, double loga)
 // ------------------------------------------------------------------ history splines
 // Forward/back substitution of every history row against the shared factorisation,
 // warp per row (warp-parallel affine scans when the row fits in shared memory).
-__global__ void k_dtot_coeffs(IntegratorDev I, int nk, int Na, int staged) {
+__global__ void k_dtot_coeffs(IntegratorDev I, int nk, int Na, int staged, int update_row) {
     extern __shared__ __align__(16) double sdc[];
     const int warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
     double* sy = staged ? sdc + (size_t)warp * 2 * I.ld : nullptr;
     double* sc = staged ? sy + I.ld : nullptr;
     for (int ik = blockIdx.x * nw + warp; ik < nk; ik += gridDim.x * nw) {
+        if (update_row >= 0) {  // update_delta_tot (delta_tot_table.c:177-191), as k_update_row
+            if ((threadIdx.x & 31) == 0) {
+                const StepScalars& S = *I.sc;
+                I.dtot[(size_t)ik * I.ld + update_row] =
+                    get_delta_tot(I.nu_last[ik], I.dcdm[ik], S.OmegaNua3, S.Omeganonu, S.OmegaNu1, S.partnu);
+            }
+            __syncwarp();
+        }
         if (staged) dtot_row_coeffs_scan(I, ik, Na, sy, sc);
         else dtot_row_coeffs_warp(I, ik, Na, nullptr, nullptr);
     }
@@ -641,7 +664,11 @@ void launch_integrator_prepare(const IntegratorDev& I, int Na, double a, double 
 // The rest, after the provisional history row: spline coefficients of the rows, the
 // integrals, the species sum.
 void launch_integrator_rest(const IntegratorDev& I, int nk, int Na, int nspec, const int* spec_ids,
-                            int warps_per_block, cudaStream_t st, int qag_split) {
+                            int warps_per_block, cudaStream_t st, int qag_split, int update_row, bool defer_combine) {
+    if (update_row >= 0 && Na <= 2) {
+        launch_update_row_scalars(I, nk, update_row, st);
+        update_row = -1;
+    }
     if (Na > 2) {
         static bool dc_attr = false;
         if (!dc_attr) {
@@ -650,7 +677,7 @@ void launch_integrator_rest(const IntegratorDev& I, int nk, int Na, int nspec, c
         }
         const size_t smem = 4 * 2 * sizeof(double) * I.ld;
         const int staged = smem <= 200 * 1024;
-        k_dtot_coeffs<<<(nk + 3) / 4, 128, staged ? smem : 0, st>>>(I, nk, Na, staged);
+        k_dtot_coeffs<<<(nk + 3) / 4, 128, staged ? smem : 0, st>>>(I, nk, Na, staged, update_row);
     }
     int wpb = warps_per_block < 1 ? 1 : (warps_per_block > 4 ? 4 : warps_per_block);
     while (wpb > 1 && dnu_qag_smem(I.ld, wpb) > 227 * 1024) wpb--;
@@ -686,7 +713,7 @@ void launch_integrator_rest(const IntegratorDev& I, int nk, int Na, int nspec, c
                                                       make_int4(spec_ids[0], spec_ids[1], spec_ids[2], 0));
         }
     }
-    k_combine<<<(nk + 255) / 256, 256, 0, st>>>(I, nk);
+    if (!defer_combine) k_combine<<<(nk + 255) / 256, 256, 0, st>>>(I, nk);
 }
 
 void launch_delta_nu_combined(const IntegratorDev& I, int nk, int Na, double a, double loga, double loga0,
@@ -703,7 +730,18 @@ void launch_delta_nu_combined(const IntegratorDev& I, int nk, int Na, double a, 
 // same-scale-factor path, delta_tot_table.c:209-213: no NaN check, no clamp);
 // -3: a differentiable step: like -1 but delta_nu_last is left unchanged.
 __global__ void k_finish(IntegratorDev I, int nk, int commit_row, double a, double loga, const double* keff,
-                         double* dnu_out, double* logk_out, double* ratio_out, CorrTable corr, double* norm_out) {
+                         double* dnu_out, double* logk_out, double* ratio_out, CorrTable corr, double* norm_out,
+                         int combine) {
+    if (combine) {  // k_combine's species sum first (same arithmetic)
+        const StepScalars& S = *I.sc;
+        for (int ik = threadIdx.x; ik < nk; ik += blockDim.x) {
+            double acc = 0;
+            for (int mi = 0; mi < kNuSpecies; mi++)
+                if (I.B->deg[mi] > 0) acc += I.dnu_s[(size_t)mi * I.nk_alloc + ik] * S.omeganu[mi] / S.Omega_nu_tot;
+            I.dnu[ik] = acc;
+        }
+        __syncthreads();
+    }
     __shared__ double s3[3];
     const StepScalars& S = *I.sc;
     const bool pass = commit_row == -2;
@@ -752,8 +790,9 @@ __global__ void k_finish(IntegratorDev I, int nk, int commit_row, double a, doub
 
 void launch_finish_update(const IntegratorDev& I, int nk, int commit_row, double a, double loga,
                           const double* keff, double* dnu_out, double* logk_out, double* ratio_out,
-                          CorrTable corr, double* norm_out, cudaStream_t st) {
-    k_finish<<<1, 1024, 0, st>>>(I, nk, commit_row, a, loga, keff, dnu_out, logk_out, ratio_out, corr, norm_out);
+                          CorrTable corr, double* norm_out, cudaStream_t st, bool combine) {
+    k_finish<<<1, 1024, 0, st>>>(I, nk, commit_row, a, loga, keff, dnu_out, logk_out, ratio_out, corr, norm_out,
+                                 combine ? 1 : 0);
 }
 
 }  // namespace ksp

@@ -375,14 +375,18 @@ void launch_delta_nu_combined(const IntegratorDev& I, int nk, int Na, double a, 
 void launch_integrator_prepare(const IntegratorDev& I, int Na, double a, double loga, double loga0,
                                double TimeTransfer, int start_row, int write_knot, bool scalars_only,
                                cudaStream_t st);
+// update_row >= 0: write the provisional row `update_row` (update_delta_tot, from
+// delta_nu_last and delta_cdm with the call's scalars) as each row's spline is solved;
+// defer_combine: leave the species sum to launch_finish_update(..., combine = true)
 void launch_integrator_rest(const IntegratorDev& I, int nk, int Na, int nspec, const int* spec_ids,
-                            int warps_per_block, cudaStream_t st, int qag_split);
+                            int warps_per_block, cudaStream_t st, int qag_split, int update_row = -1,
+                            bool defer_combine = false);
 size_t dnu_qag_smem(int ld, int wpb);
 // end of get_delta_nu_update (delta_tot_table.c:226-248) + interface_common.c:134-146:
 // delta_nu_last, committed row, NaN check, clamp, ratio/log k/kspace_prefac, grid table
 void launch_finish_update(const IntegratorDev& I, int nk, int commit_row, double a, double loga,
                           const double* keff, double* dnu_out, double* logk_out, double* ratio_out,
-                          CorrTable corr, double* norm_out, cudaStream_t st);
+                          CorrTable corr, double* norm_out, cudaStream_t st, bool combine = false);
 
 // ---- adjoint (ksp_adjoint.cu)
 struct AdjBinsHost {

@@ -40,10 +40,10 @@ def J_tab(x, m, T):
     sb = m["KSP_JFIT_SUB_BITS"]
     sub = (bits >> (52 - sb)) & ((1 << sb) - 1)
     p = T[((e - m["KSP_JFIT_E0"]) << sb) | sub]
-    u = (x - p[0]) * p[1]
+    t = x - p[0]  # coefficients of the polynomial in x - centre
     v = 0.0
-    for c in reversed(p[2:]):
-        v = v * u + c
+    for c in reversed(p[1:]):
+        v = v * t + c
     return v
 
 
@@ -52,7 +52,8 @@ def test_table_matches_formula():
     rng = np.random.default_rng(0)
     xs = np.exp(rng.uniform(np.log(2.0 ** m["KSP_JFIT_E0"]), np.log(2.0 ** m["KSP_JFIT_E1"]), 3000))
     # piece edges and their neighbours
-    edges = [2.0 ** e * (1 + s / 32) for e in range(m["KSP_JFIT_E0"], m["KSP_JFIT_E1"]) for s in range(0, 32, 3)]
+    nsub = 1 << m["KSP_JFIT_SUB_BITS"]
+    edges = [2.0 ** e * (1 + s / nsub) for e in range(m["KSP_JFIT_E0"], m["KSP_JFIT_E1"]) for s in range(0, nsub, 5)]
     worst = 0.0
     for x in list(xs) + edges + [np.nextafter(x, 0) for x in edges[1:]]:
         ex = J_exact(x)
