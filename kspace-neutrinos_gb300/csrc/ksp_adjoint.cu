@@ -474,7 +474,6 @@ __global__ void __launch_bounds__(128) k_dnu_adj(IntegratorDev I, DnuAdjArgs A, 
             if (Na > 2) seg_poly(row, rc, Na, ks, sb, sd, lane, 32);
             __syncwarp();
             const double qc = S.partnu_now > 0 ? B->vcrit * mnubykT : 0.0;
-            const double fs_inv = (S.Nfs - 1.) / (S.loga - S.loga0);
             // the final subdivision of the forward QAG: stored, or recomputed (same decisions)
             int nint;
             const double* iv = nullptr;

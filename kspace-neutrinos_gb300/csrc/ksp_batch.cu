@@ -192,21 +192,40 @@ __global__ void kb_fs_coeffs(BatchDev b) {
 }
 
 // ------------------------------------------------------------------ history splines
-// warp per (instance, bin): the row staged into shared memory and solved by the warp's
-// affine scans (dtot_row_coeffs_scan, as k_dtot_coeffs)
+// thread per (instance, bin): the same substitutions as k_dtot_coeffs, each thread
+// sweeping its own row in global memory.  With a million rows in flight the latency of
+// the strided loads is hidden by parallelism, which a warp-per-row solve (one active
+// lane per row) cannot match at this size.
 __global__ void kb_dtot_coeffs(BatchDev b) {
-    extern __shared__ __align__(16) double sdc[];
-    const int warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
-    double* sy = sdc + (size_t)warp * 2 * b.ldmax;
-    double* sc = sy + b.ldmax;
     const int total = b.hdr->total_bins;
-    for (int g = blockIdx.x * nw + warp; g < total; g += gridDim.x * nw) {
+    for (int g = blockIdx.x * blockDim.x + threadIdx.x; g < total; g += gridDim.x * blockDim.x) {
         const int i = owner_of(b.bin_off, b.M, g);
         const int ik = g - __ldg(b.bin_off + i);
         const BatchCall& P = b.calls[i];
         const int Na = P.Na;
-        if (!P.active || P.commit_row == -2 || Na <= 2) continue;  // uniform over the warp
-        dtot_row_coeffs_scan(b.insts[i], ik, Na, sy, sc);
+        if (!P.active || P.commit_row == -2 || Na <= 2) continue;
+        const IntegratorDev& I = b.insts[i];
+        const double* y = I.dtot + (size_t)ik * I.ld;
+        double* c = I.coef + (size_t)ik * I.ld;
+        const double* ih = I.knot_invh;
+        const int m = Na - 2;
+        double prev = 0;
+        for (int k = 0; k < m; k++) {
+            double r = 3.0 * ((y[k + 2] - y[k + 1]) * ih[k + 1] - (y[k + 1] - y[k]) * ih[k]);
+            if (k > 0) r -= I.knot_fac[k] * prev;
+            prev = r;
+            c[k + 1] = r;
+        }
+        c[0] = 0.0;
+        c[Na - 1] = 0.0;
+        double next = c[m] * I.knot_invdiag[m - 1];
+        c[m] = next;
+        const double* x = I.scalefact;
+        for (int k = m - 1; k-- > 0;) {
+            const double off = x[k + 2] - x[k + 1];
+            next = (c[k + 1] - off * next) * I.knot_invdiag[k];
+            c[k + 1] = next;
+        }
     }
 }
 
@@ -401,7 +420,6 @@ static void gl_nodes_b(int n, double* X, double* Wt) {  // Newton on P_n, positi
 
 void batch_set_attributes() {
     cudaFuncSetAttribute(kb_dnu_qag, cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024);
-    cudaFuncSetAttribute(kb_dtot_coeffs, cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024);
 }
 
 void launch_batch_update(const BatchDev& b, cudaStream_t st) {
@@ -416,7 +434,7 @@ void launch_batch_update(const BatchDev& b, cudaStream_t st) {
     kb_fs_segments<<<nb, 256, 0, st>>>(b, gl);
     kb_fs_finish<<<b.M < 2 * 152 ? b.M : 2 * 152, 1024, 0, st>>>(b);
     kb_fs_coeffs<<<nb, 128, 0, st>>>(b);
-    kb_dtot_coeffs<<<nb, 128, 4 * 2 * sizeof(double) * b.ldmax, st>>>(b);
+    kb_dtot_coeffs<<<nb, 128, 0, st>>>(b);
     kb_nc_build<<<nb, 128, 0, st>>>(b);
     kb_dnu_qag<<<b.qag_blocks, 32 * b.wpb, batch_qag_smem(b.ldmax, b.wpb), st>>>(b);
     kb_finish<<<nb, 256, 0, st>>>(b);

@@ -555,19 +555,21 @@ __device__ __forceinline__ void gk61_lane_sums(const Gk61Nodes& N, const double*
     double z = (b4 ? rs[1] : rs[0]) + __shfl_xor_sync(0xffffffffu, b4 ? rs[0] : rs[1], 16);
 #pragma unroll
     for (int o = 8; o > 0; o >>= 1) z += __shfl_xor_sync(0xffffffffu, z, o);
-    // the outputs of interval t on the lanes with t = lane & 1 (one evaluation per lane),
-    // then broadcast
+    // the outputs of interval t on lane t only (FP64 is issued per active lane), then
+    // broadcast
     const int t = lane & 1;
-    const double ht = t ? h[1] : h[0];
-    const double rkt = t ? rk1 : rk0;
     const double rgt = __shfl_sync(0xffffffffu, y, t ? 20 : 4);
     const double rat = __shfl_sync(0xffffffffu, y, t ? 24 : 8);
     const double rst = __shfl_sync(0xffffffffu, z, t ? 16 : 0);
-    GkOut o;
-    o.result = rkt * ht;
-    o.resabs = rat * fabs(ht);
-    o.resasc = rst * fabs(ht);
-    o.abserr = rescale_error((rkt - rgt) * ht, o.resabs, o.resasc);
+    GkOut o = {0.0, 0.0, 0.0, 0.0};
+    if (lane < nint) {
+        const double ht = t ? h[1] : h[0];
+        const double rkt = t ? rk1 : rk0;
+        o.result = rkt * ht;
+        o.resabs = rat * fabs(ht);
+        o.resasc = rst * fabs(ht);
+        o.abserr = rescale_error((rkt - rgt) * ht, o.resabs, o.resasc);
+    }
     for (int u = 0; u < nint; u++) {
         out[u].result = __shfl_sync(0xffffffffu, o.result, u);
         out[u].resabs = __shfl_sync(0xffffffffu, o.resabs, u);
@@ -622,7 +624,7 @@ __device__ QagResult qag_warp_c(const F& f, const Gk61Nodes& N, QagList& L, doub
     if ((g[0].abserr <= tol && g[0].abserr != g[0].resasc) || g[0].abserr == 0.0) { R.ok = 1; return R; }
     if (limit == 1) { R.ok = 0; return R; }
     double area = g[0].result, errsum = g[0].abserr;
-    int n = 1, roundoff1 = 0, roundoff2 = 0, error_type = 0;
+    int n = 1, roundoff1 = 0, roundoff2 = 0, error_type = 0, cont = 0;
     do {
         double best = -1.0;
         int bk = 0x7fffffff;
@@ -644,34 +646,38 @@ __device__ QagResult qag_warp_c(const F& f, const Gk61Nodes& N, QagList& L, doub
         ss[0] = nc_child(s_i, 0, f.nc.nslots);
         ss[1] = nc_child(s_i, 1, f.nc.nslots);
         gk61_warp_c(f, N, 2, aa, bb, ss, g);
-        const double area12 = g[0].result + g[1].result, error12 = g[0].abserr + g[1].abserr;
-        errsum += error12 - e_i;
-        area += area12 - r_i;
-        if (g[0].resasc != g[0].abserr && g[1].resasc != g[1].abserr) {
-            if (fabs(r_i - area12) <= 1.0e-5 * fabs(area12) && error12 >= 0.99 * e_i) roundoff1++;
-            if (n >= 10 && error12 > e_i) roundoff2++;
-        }
-        tol = fmax(epsabs, epsrel * fabs(area));
-        if (errsum > tol) {
-            if (roundoff1 >= 6 || roundoff2 >= 20) error_type = 2;
-            const double tiny = (1 + 100 * DBL_EPSILON) * (fabs(a2) + 1000 * DBL_MIN);
-            if (fabs(a1) <= tiny && fabs(b2) <= tiny) error_type = 3;
-        }
+        // QUADPACK's bookkeeping on lane 0 (its FP64 is not repeated on 32 lanes)
+        cont = 0;
         __syncwarp();
         if (lane == 0) {
+            const double area12 = g[0].result + g[1].result, error12 = g[0].abserr + g[1].abserr;
+            errsum += error12 - e_i;
+            area += area12 - r_i;
+            if (g[0].resasc != g[0].abserr && g[1].resasc != g[1].abserr) {
+                if (fabs(r_i - area12) <= 1.0e-5 * fabs(area12) && error12 >= 0.99 * e_i) roundoff1++;
+                if (n >= 10 && error12 > e_i) roundoff2++;
+            }
+            tol = fmax(epsabs, epsrel * fabs(area));
+            if (errsum > tol) {
+                if (roundoff1 >= 6 || roundoff2 >= 20) error_type = 2;
+                const double tiny = (1 + 100 * DBL_EPSILON) * (fabs(a2) + 1000 * DBL_MIN);
+                if (fabs(a1) <= tiny && fabs(b2) <= tiny) error_type = 3;
+            }
             L.b[k] = b1; L.r[k] = g[0].result; L.e[k] = g[0].abserr; L.slot[k] = ss[0];
             L.a[n] = a2; L.b[n] = b2; L.r[n] = g[1].result; L.e[n] = g[1].abserr; L.slot[n] = ss[1];
+            cont = n + 1 < limit && !error_type && errsum > tol;
         }
+        cont = __shfl_sync(0xffffffffu, cont, 0);
         __syncwarp();
         n++;
-    } while (n < limit && !error_type && errsum > tol);
+    } while (cont);
     double sum = 0;
     if (lane == 0)
         for (int i = 0; i < n; i++) sum += L.r[i];
     R.result = bcast0(sum);
-    R.abserr = errsum;
+    R.abserr = bcast0(errsum);
     R.nint = n;
-    R.ok = errsum <= tol;
+    R.ok = __shfl_sync(0xffffffffu, (int)(errsum <= tol), 0);
     __syncwarp();
     return R;
 }
@@ -687,6 +693,8 @@ struct QagBlockSmem {
     GkOut out[2];
     double a[2], b[2];
     int slot[2];
+    int k, cont, ok;   // the interval to bisect, whether to go on, errsum <= tol
+    double errsum;
 };
 
 template <class F>
@@ -744,20 +752,24 @@ __device__ QagResult qag_block_c(const F& f, const Gk61Nodes& N, QagList& L, dou
     double area = g[0].result, errsum = g[0].abserr;
     int n = 1, roundoff1 = 0, roundoff2 = 0, error_type = 0;
     do {
-        // every warp computes the same argmax (lowest index on ties)
-        double best = -1.0;
-        int bk = 0x7fffffff;
-        for (int i = lane; i < n; i += 32) {
-            const double e = L.e[i];
-            if (e > best) { best = e; bk = i; }
-        }
+        // warp 0 finds the interval of largest error (lowest index on ties)
+        if (tid < 32) {
+            double best = -1.0;
+            int bk = 0x7fffffff;
+            for (int i = lane; i < n; i += 32) {
+                const double e = L.e[i];
+                if (e > best) { best = e; bk = i; }
+            }
 #pragma unroll
-        for (int o = 16; o > 0; o >>= 1) {
-            const double ob = __shfl_down_sync(0xffffffffu, best, o);
-            const int ok = __shfl_down_sync(0xffffffffu, bk, o);
-            if (ob > best || (ob == best && ok < bk)) { best = ob; bk = ok; }
+            for (int o = 16; o > 0; o >>= 1) {
+                const double ob = __shfl_down_sync(0xffffffffu, best, o);
+                const int ok = __shfl_down_sync(0xffffffffu, bk, o);
+                if (ob > best || (ob == best && ok < bk)) { best = ob; bk = ok; }
+            }
+            if (lane == 0) sh.k = bk;
         }
-        const int k = __shfl_sync(0xffffffffu, bk, 0);
+        __syncthreads();
+        const int k = sh.k;
         const double a_i = L.a[k], b_i = L.b[k], r_i = L.r[k], e_i = L.e[k];
         const int s_i = L.slot[k];
         const double a1 = a_i, b1 = 0.5 * (a_i + b_i), a2 = b1, b2 = b_i;
@@ -765,33 +777,37 @@ __device__ QagResult qag_block_c(const F& f, const Gk61Nodes& N, QagList& L, dou
         ss[0] = nc_child(s_i, 0, f.nc.nslots);
         ss[1] = nc_child(s_i, 1, f.nc.nslots);
         gk61_block_c(f, N, 2, aa, bb, ss, g, sh);
-        const double area12 = g[0].result + g[1].result, error12 = g[0].abserr + g[1].abserr;
-        errsum += error12 - e_i;
-        area += area12 - r_i;
-        if (g[0].resasc != g[0].abserr && g[1].resasc != g[1].abserr) {
-            if (fabs(r_i - area12) <= 1.0e-5 * fabs(area12) && error12 >= 0.99 * e_i) roundoff1++;
-            if (n >= 10 && error12 > e_i) roundoff2++;
-        }
-        tol = fmax(epsabs, epsrel * fabs(area));
-        if (errsum > tol) {
-            if (roundoff1 >= 6 || roundoff2 >= 20) error_type = 2;
-            const double tiny = (1 + 100 * DBL_EPSILON) * (fabs(a2) + 1000 * DBL_MIN);
-            if (fabs(a1) <= tiny && fabs(b2) <= tiny) error_type = 3;
-        }
+        // QUADPACK's bookkeeping on thread 0
         if (tid == 0) {
+            const double area12 = g[0].result + g[1].result, error12 = g[0].abserr + g[1].abserr;
+            errsum += error12 - e_i;
+            area += area12 - r_i;
+            if (g[0].resasc != g[0].abserr && g[1].resasc != g[1].abserr) {
+                if (fabs(r_i - area12) <= 1.0e-5 * fabs(area12) && error12 >= 0.99 * e_i) roundoff1++;
+                if (n >= 10 && error12 > e_i) roundoff2++;
+            }
+            tol = fmax(epsabs, epsrel * fabs(area));
+            if (errsum > tol) {
+                if (roundoff1 >= 6 || roundoff2 >= 20) error_type = 2;
+                const double tiny = (1 + 100 * DBL_EPSILON) * (fabs(a2) + 1000 * DBL_MIN);
+                if (fabs(a1) <= tiny && fabs(b2) <= tiny) error_type = 3;
+            }
             L.b[k] = b1; L.r[k] = g[0].result; L.e[k] = g[0].abserr; L.slot[k] = ss[0];
             L.a[n] = a2; L.b[n] = b2; L.r[n] = g[1].result; L.e[n] = g[1].abserr; L.slot[n] = ss[1];
+            sh.cont = n + 1 < limit && !error_type && errsum > tol;
+            sh.errsum = errsum;
+            sh.ok = errsum <= tol;
         }
         __syncthreads();
         n++;
-    } while (n < limit && !error_type && errsum > tol);
+    } while (sh.cont);
     double sum = 0;
     if (lane == 0)
         for (int i = 0; i < n; i++) sum += L.r[i];
     R.result = bcast0(sum);
-    R.abserr = errsum;
+    R.abserr = sh.errsum;
     R.nint = n;
-    R.ok = errsum <= tol;
+    R.ok = sh.ok;
     __syncthreads();
     return R;
 }
