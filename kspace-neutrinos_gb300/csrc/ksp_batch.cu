@@ -93,38 +93,27 @@ __global__ void kb_prologue(BatchDev b) {
 // ------------------------------------------------------------------ fslength table
 struct GL4b { double x[2], w[2]; };
 
-// 4 lanes per segment over the segments of all instances (flat, so that instances of
-// any length balance), as k_fs_segments
+// groups of 4 lanes over the fslength segments of all instances (flat, so that
+// instances of any length balance), as k_fs_segments
 __global__ void kb_fs_segments(BatchDev b, GL4b gl) {
-    const int total = b.hdr->total_segs;
+    const int total = b.hdr->total_segs;  // groups
     const long long stride = (long long)gridDim.x * blockDim.x;  // a multiple of 4
     const long long end = 4LL * total;
     for (long long base = (long long)blockIdx.x * blockDim.x; base < end; base += stride) {
         const long long gt = base + threadIdx.x;
-        const int gseg = (int)(gt >> 2), q = (int)(gt & 3);
-        double v = 0.0;
+        const int gg = (int)(gt >> 2), q = (int)(gt & 3);
         const bool live = gt < end;
-        int i = 0, seg = 0;
+        int i = 0, g = 0;
         if (live) {
-            i = owner_of(b.fs_off, b.M, gseg);
-            seg = gseg - __ldg(b.fs_off + i);
-            const BatchCall& P = b.calls[i];
-            const int Nfs = P.nfs;
-            const double loga0 = P.loga0, loga = P.loga;
-            const double xa = loga0 + seg * (loga - loga0) / (Nfs - 1.);
-            double xb = loga0 + (seg + 1) * (loga - loga0) / (Nfs - 1.);
-            if (seg == Nfs - 1) xb = loga;
-            if (xb > xa) {
-                const double c = 0.5 * (xa + xb), h = 0.5 * (xb - xa);
-                const int j = q & 1;
-                const double x = (q < 2) ? c - h * gl.x[j] : c + h * gl.x[j];
-                v = gl.w[j] * h * fsl_integrand(*b.insts[i].B, x);
-            }
-            if (q == 0) b.insts[i].fs_x[seg] = xa;
+            i = owner_of(b.fs_off, b.M, gg);
+            g = gg - __ldg(b.fs_off + i);
         }
-        v += __shfl_down_sync(0xffffffffu, v, 2, 4);
-        v += __shfl_down_sync(0xffffffffu, v, 1, 4);
-        if (live && q == 0) b.insts[i].fs_seg[seg] = v;
+        const BatchCall& P = b.calls[i];
+        const int Nfs = live ? P.nfs : 1;
+        const double loga0 = P.loga0, loga = P.loga;
+        const int npts = live ? fs_rule_points(Nfs, loga0, loga) : 4;
+        fs_group_eval(*b.insts[i].B, Nfs, loga0, loga, npts, g, q, live, gl.x, gl.w, b.insts[i].fs_x,
+                      b.insts[i].fs_seg);
     }
 }
 

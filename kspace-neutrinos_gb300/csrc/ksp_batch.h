@@ -25,7 +25,7 @@ struct BatchCall {
 // captured graph serves every call) and stride over these.
 struct BatchHeader {
     int M;
-    int total_segs;   // sum of nfs
+    int total_segs;   // fslength segment groups (fs_groups of each instance)
     int total_fsc;    // sum of max(nfs-2, 0): fslength spline unknowns
     int total_bins;   // sum of nk
     int total_tasks;  // sum of nspec*nk over integrating instances

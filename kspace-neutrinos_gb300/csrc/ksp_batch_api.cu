@@ -403,7 +403,7 @@ static int plan_call(kspace_batch* b, const double* a, bool dry, std::vector<int
             }
         }
         const bool integ = P.active && P.commit_row != -2;
-        fs_off[i + 1] = fs_off[i] + (integ ? P.nfs : 0);
+        fs_off[i + 1] = fs_off[i] + (integ && P.nfs > 0 ? fs_groups(P.nfs, P.loga0, P.loga) : 0);
         fsc_off[i + 1] = fsc_off[i] + (integ && P.nfs > 2 ? P.nfs - 2 : 0);
         bin_off[i + 1] = b->off[i + 1];
         task_off[i + 1] = task_off[i] + (integ ? P.nspec * P.nk : 0);

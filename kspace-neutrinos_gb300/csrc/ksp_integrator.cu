@@ -262,31 +262,10 @@ struct FslIntegrand {  // delta_tot_table.c:378-383
     __device__ double operator()(double loga) const { return fsl_integrand(*B, loga); }
 };
 
-// 4 lanes per segment: lane q evaluates node q of the 4-point Gauss-Legendre rule on
-// [x_i, x_{i+1}] (segment Nfs-1 is the rounding sliver [x_{Nfs-1}, log a]).  The 4-point
-// rule leaves delta_nu as close to the reference's adaptive fslength integrals as an
-// 8-point rule does (both within ~2e-12 on 16..512-row histories).
-__global__ void k_fs_segments(IntegratorDev I, int Nfs, double loga0, double loga, GL4 gl) {
+// The segment integrals of the fslength table, 4 lanes per group (fs_group_eval).
+__global__ void k_fs_segments(IntegratorDev I, int Nfs, double loga0, double loga, GL4 gl, int npts, int ngroups) {
     const int gt = blockIdx.x * blockDim.x + threadIdx.x;
-    const int seg = gt >> 2, q = gt & 3;
-    const bool live = seg < Nfs;
-    double v = 0.0;
-    if (live) {
-        const double xa = loga0 + seg * (loga - loga0) / (Nfs - 1.);
-        double xb = loga0 + (seg + 1) * (loga - loga0) / (Nfs - 1.);
-        if (seg == Nfs - 1) xb = loga;
-        if (xb > xa) {
-            const double c = 0.5 * (xa + xb), h = 0.5 * (xb - xa);
-            const int j = q & 1;
-            const double x = (q < 2) ? c - h * gl.x[j] : c + h * gl.x[j];
-            v = gl.w[j] * h * FslIntegrand{I.B}(x);
-        }
-        if (q == 0) I.fs_x[seg] = xa;
-    }
-    // sum the 4 lanes of the segment (fixed order)
-    v += __shfl_down_sync(0xffffffffu, v, 2, 4);
-    v += __shfl_down_sync(0xffffffffu, v, 1, 4);
-    if (live && q == 0) I.fs_seg[seg] = v;
+    fs_group_eval(*I.B, Nfs, loga0, loga, npts, gt >> 2, gt & 3, (gt >> 2) < ngroups, gl.x, gl.w, I.fs_x, I.fs_seg);
 }
 
 // One block: suffix sums of the segment integrals -> fslength at every node.
@@ -649,8 +628,9 @@ void launch_integrator_prepare(const IntegratorDev& I, int Na, double a, double 
     // the fslength table (always built: it also gives fslength(log a0, log a))
     const int Nfs = 16 * (Na > 1 ? Na : 1);
     if (loga > loga0) {
-        const long long threads = 4LL * Nfs;
-        k_fs_segments<<<(unsigned)((threads + 255) / 256), 256, 0, st>>>(I, Nfs, loga0, loga, gl);
+        const int npts = fs_rule_points(Nfs, loga0, loga), ngroups = fs_groups(Nfs, loga0, loga);
+        const long long threads = 4LL * ngroups;
+        k_fs_segments<<<(unsigned)((threads + 255) / 256), 256, 0, st>>>(I, Nfs, loga0, loga, gl, npts, ngroups);
         k_fs_finish<<<1, 1024, 0, st>>>(I, Nfs);
         if (Nfs > 2) k_fs_coeffs<<<(Nfs - 2 + 31) / 32, 32, 0, st>>>(I, Nfs, loga0, loga);
     } else {

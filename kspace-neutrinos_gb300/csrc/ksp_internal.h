@@ -150,6 +150,59 @@ __device__ __forceinline__ void dtot_row_coeffs_warp(const IntegratorDev& I, int
     __syncwarp();
 }
 
+// The fslength table's segment integrals (the segments between its 16*Na uniform knots
+// in log a): a group of 4 lanes takes one segment with the 4-point Gauss-Legendre rule
+// or, where the knots are closer than 1.5e-3 in log a (the 2-point rule's relative
+// error per segment is then below ~3e-14 for this smooth integrand), two segments with
+// the 2-point rule.
+__host__ __device__ inline int fs_rule_points(int Nfs, double loga0, double loga) {
+    return (loga - loga0) / (Nfs - 1.) < 1.5e-3 ? 2 : 4;
+}
+__host__ __device__ inline int fs_groups(int Nfs, double loga0, double loga) {
+    return fs_rule_points(Nfs, loga0, loga) == 4 ? Nfs : (Nfs + 1) / 2;
+}
+#ifdef __CUDACC__
+// lane q (0..3) of group g; called by whole warps (groups are aligned to 4 lanes).
+// gx, gw: the positive half of the 4-point rule.
+__device__ __forceinline__ void fs_group_eval(const Background& B, int Nfs, double loga0, double loga, int npts,
+                                              int g, int q, bool live, const double* gx, const double* gw,
+                                              double* fs_x, double* fs_seg) {
+    double v = 0.0;
+    int seg = -1;
+    if (live) {
+        const int node = npts == 4 ? q : (q & 1);
+        seg = npts == 4 ? g : 2 * g + (q >> 1);
+        if (seg < Nfs) {
+            const double xa = loga0 + seg * (loga - loga0) / (Nfs - 1.);
+            double xb = loga0 + (seg + 1) * (loga - loga0) / (Nfs - 1.);
+            if (seg == Nfs - 1) xb = loga;
+            if (xb > xa) {
+                const double c = 0.5 * (xa + xb), h = 0.5 * (xb - xa);
+                double x, w;
+                if (npts == 4) {
+                    const int j = node & 1;
+                    x = node < 2 ? c - h * gx[j] : c + h * gx[j];
+                    w = gw[j];
+                } else {
+                    x = node ? c + h * 0.57735026918962576451 : c - h * 0.57735026918962576451;  // 1/sqrt(3)
+                    w = 1.0;
+                }
+                v = w * h * fsl_integrand(B, x);
+            }
+            if (node == 0) fs_x[seg] = xa;
+        } else {
+            seg = -1;
+        }
+    }
+    const double s1 = v + __shfl_down_sync(0xffffffffu, v, 1, 4);
+    const double s2 = s1 + __shfl_down_sync(0xffffffffu, s1, 2, 4);
+    if (seg >= 0) {
+        if (npts == 4 && q == 0) fs_seg[seg] = s2;
+        if (npts == 2 && (q & 1) == 0) fs_seg[seg] = s1;
+    }
+}
+#endif
+
 // Natural-spline second derivatives c[0..n-1] of a table y on uniform spacing h, by
 // one warp: tridiag(1,4,1) c[1..n-2] = 3/h^2 (y[u+2] - 2 y[u+1] + y[u]), c[0] = c[n-1]
 // = 0.  Gaussian elimination has pivots d_0 = 4, d_u = 4 - 1/d_{u-1}; they reach

@@ -613,9 +613,13 @@ static void fs_table(ko_state *s, double a, int Nfs, double *fsscales, double *f
         return;
     }
     gl8_init();
-    /* fs_mode 1: 8-point rule per segment; fs_mode 2: 4-point rule */
-    const int np = s->fs_mode == 2 ? 2 : 4;
-    const double *GX = s->fs_mode == 2 ? GL4_X : GL8_X, *GW = s->fs_mode == 2 ? GL4_W : GL8_W;
+    /* fs_mode 1: 8-point rule per segment; fs_mode 2: 4-point rule; fs_mode 3: the GPU's
+     * rule, 2-point where the knots are closer than 1.5e-3 in log a, else 4-point */
+    static const double GL2_X[1] = {0.57735026918962576451}, GL2_W[1] = {1.0};
+    const int use2 = s->fs_mode == 3 && (la - l0) / (Nfs - 1.) < 1.5e-3;
+    const int np = use2 ? 1 : (s->fs_mode >= 2 ? 2 : 4);
+    const double *GX = use2 ? GL2_X : (s->fs_mode >= 2 ? GL4_X : GL8_X);
+    const double *GW = use2 ? GL2_W : (s->fs_mode >= 2 ? GL4_W : GL8_W);
     double acc = 0;
     /* tail beyond the last node (non-zero only through rounding of the node formula) */
     if (fsscales[Nfs - 1] < la) {

@@ -30,7 +30,7 @@ def _instance(gpu, nb):
     return k
 
 
-@pytest.mark.parametrize("N,nb", [(16, 15), (64, 48), (96, 80), (128, 128), (256, 200)])
+@pytest.mark.parametrize("N,nb", [(16, 15), (64, 48), (96, 80), (128, 128), (256, 200), (64, 1000), (100, 2500)])
 def test_binning_stream_variants(gpu, oracle, N, nb):
     import torch
     g = W.make_grid(N, seed=100 + N)
@@ -82,7 +82,7 @@ def _table(N, nb):
     return np.log(kph), ratio, 0.37
 
 
-@pytest.mark.parametrize("N,nb", [(16, 15), (64, 48), (96, 80), (128, 100)])
+@pytest.mark.parametrize("N,nb", [(16, 15), (64, 48), (96, 80), (128, 100), (64, 1000)])
 def test_correction_stream_variants(gpu, oracle, N, nb):
     import torch
     logk, ratio, norm = _table(N, nb)

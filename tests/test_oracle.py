@@ -240,14 +240,17 @@ def test_e2e_golden_oracle(oracle):
         assert rel.max() < 1e-6
 
 
-def test_fs_table_fixed_order_vs_qag(oracle):
-    """The cumulative fixed-order (4-point Gauss-Legendre per segment) fslength table, as the
-    GPU computes it, changes delta_nu by far less than the 1e-10 bar."""
-    c = cases.make_case(64, 48, 40, 1.0, (0.02, 0.03, 0.06), grid=False)
+@pytest.mark.parametrize("Na", [40, 256])
+def test_fs_table_fixed_order_vs_qag(oracle, Na):
+    """The cumulative fixed-order fslength table, as the GPU computes it (4-point
+    Gauss-Legendre per segment, or 2-point where the knots are closer than 1.5e-3 in
+    log a: the 256-row history), changes delta_nu by far less than the 1e-10 bar."""
+    c = cases.make_case(64, 48, Na, 1.0, (0.02, 0.03, 0.06), grid=False, extra_rows=12 + Na // 4)
     res = []
-    for mode in (0, 2):
+    for mode in (0, 2, 3):
         bg, s = cases.oracle_state(oracle, c, fs_mode=mode)
         st, d = oracle.get_delta_nu_update(s, 1.01, c["kphys"], np.sqrt(W.spectrum(c["kphys"])))
         assert st == 0
         res.append(d)
     assert cases.rel_err(res[1], res[0]) < 1e-11
+    assert cases.rel_err(res[2], res[0]) < 1e-11
