@@ -609,6 +609,7 @@ struct RowTiling {
     int wg;           // warps per tile group
     int tile_bytes;   // trows * nz * 8
     int stage_bytes;  // tile + read-past slack, 128-byte multiple
+    int copies;       // copies of the CTA's bin totals: tile row r adds to copy r % copies
 };
 
 inline RowTiling make_row_tiling(int nz) {
@@ -620,11 +621,12 @@ inline RowTiling make_row_tiling(int nz) {
     t.wg = (t.trows * t.R + 31) / 32;
     t.tile_bytes = t.trows * nz * 8;
     t.stage_bytes = (t.tile_bytes + kRun * 8 + 127) & ~127;
+    t.copies = 1;
     return t;
 }
 
-// stage rings (per group) | mbarriers | per-warp spill slots | float-pair bin totals |
-// thresholds | {w1[z], multiplicity} for z < nz + 17 (zero past nz)
+// stage rings (per group) | mbarriers | per-warp spill slots | float-pair bin totals
+// (T.copies copies) | thresholds | {w1[z], multiplicity} for z < nz + 17 (zero past nz)
 __host__ __device__ inline StreamPlan plan_bin_rows(int warps, int stages, int nrbins, int nz, bool exact,
                                                    const RowTiling& T) {
     StreamPlan p{};
@@ -638,7 +640,7 @@ __host__ __device__ inline StreamPlan plan_bin_rows(int warps, int stages, int n
     p.spill_off = o;
     o += (size_t)warps * kRun * 32 * (exact ? 8 : 4);  // a slot per bin of a run: at most kRun
     p.hist_off = o;
-    o += sizeof(float) * 2 * (size_t)nrbins;
+    o += sizeof(float) * 2 * (size_t)nrbins * T.copies;
     p.thr_off = o;
     o += sizeof(int) * (size_t)(nrbins + 1);
     o = (o + 15) & ~size_t(15);
@@ -677,11 +679,10 @@ __global__ void __launch_bounds__(WARPS * 32)
     unsigned char* gstage = base + P.stage_off + (size_t)grp * STAGES * T.stage_bytes;
     uint64_t* gbar = reinterpret_cast<uint64_t*>(base + P.bar_off) + grp * STAGES;
     Spill* my_spill = reinterpret_cast<Spill*>(base + P.spill_off) + (size_t)warp * kRun * 32 + lane;
-    float* s_H = reinterpret_cast<float*>(base + P.hist_off);
-    float* s_L = s_H + g.nrbins;
+    float* s_H0 = reinterpret_cast<float*>(base + P.hist_off);
     int* s_thr = reinterpret_cast<int*>(base + P.thr_off);
     float2* s_wt = reinterpret_cast<float2*>(base + P.tab_off);
-    for (int i = tid; i < 2 * g.nrbins; i += blockDim.x) s_H[i] = 0.f;
+    for (int i = tid; i < 2 * g.nrbins * T.copies; i += blockDim.x) s_H0[i] = 0.f;
     for (int i = tid; i < g.nrbins; i += blockDim.x) s_thr[i] = thresh[i];
     for (int i = tid; i < g.nz + kRun; i += blockDim.x)
         s_wt[i] = i < g.nz ? make_float2(w1g[i], (i == 0 || i == g.half) ? 1.f : 2.f) : make_float2(0.f, 0.f);
@@ -720,6 +721,11 @@ __global__ void __launch_bounds__(WARPS * 32)
     const unsigned lane_off = (unsigned)(row_t * g.nz + z0) * 8u;
     const float2* wz = s_wt + z0;
     const int gsz = T.wg * 32;
+    // Lanes of one warp on different tile rows cover nearly the same bins at the same
+    // time (neighbouring rows have nearly the same kx^2 + ky^2); separate copies of the
+    // totals keep their shared atomics off each other's addresses.
+    float* s_H = s_H0 + (size_t)(row_t % T.copies) * 2 * g.nrbins;
+    float* s_L = s_H + g.nrbins;
 
     const long long gg = (long long)blockIdx.x * groups + grp, TG = (long long)gridDim.x * groups;
     const long long my_n = gg < ntiles ? (ntiles - 1 - gg) / TG + 1 : 0;
@@ -824,7 +830,9 @@ __global__ void __launch_bounds__(WARPS * 32)
         *F0sq = (double)__fadd_rn(__fmul_rn(re, re), __fmul_rn(im, im));
     }
     for (int b = tid; b < g.nrbins; b += blockDim.x) {
-        const double v = (double)s_H[b] + (double)s_L[b];
+        double v = 0.0;
+        for (int c = 0; c < T.copies; c++)
+            v += (double)s_H0[2 * c * g.nrbins + b] + (double)s_H0[(2 * c + 1) * g.nrbins + b];
         if (v != 0.0) atomicAdd(bin_sum + b, v);
     }
 }
@@ -877,18 +885,33 @@ template <int WARPS, int STAGES, bool EXACT>
 int run_bin_rows(const GridGeom& g, const GridArgs& a, const float* grid, double* bin_sum, double* F0sq,
                  unsigned* status, cudaStream_t st) {
     if ((reinterpret_cast<uintptr_t>(grid) & 15) != 0) return -1;
-    const RowTiling T = make_row_tiling(a.nz);
+    RowTiling T = make_row_tiling(a.nz);
     if (WARPS % T.wg != 0) return -1;
     const long long nrows = (long long)g.nslab * g.N;
     if (nrows <= 0) return -1;
-    const StreamPlan P = plan_bin_rows(WARPS, STAGES, g.nrbins, a.nz, EXACT, T);
-    if (P.total > 220 * 1024) return -1;
     auto kern = k_bin_rows<WARPS, STAGES, EXACT>;
+    auto blocks_per_sm = [&](const RowTiling& t) -> int {
+        const StreamPlan p = plan_bin_rows(WARPS, STAGES, g.nrbins, a.nz, EXACT, t);
+        if (p.total > 220 * 1024) return 0;
+        cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)p.total);
+        int n = 0;
+        if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, kern, WARPS * 32, p.total) != cudaSuccess) return 0;
+        return n;
+    };
+    const int per_sm = blocks_per_sm(T);
+    if (per_sm < 1) return -1;
+    // a copy of the totals per tile row of a warp (at most 4), while that costs no
+    // resident blocks
+    for (int c = T.wg == 1 ? (T.trows < 4 ? T.trows : 4) : 1; c > 1; c /= 2) {
+        RowTiling t2 = T;
+        t2.copies = c;
+        if (blocks_per_sm(t2) == per_sm) {
+            T = t2;
+            break;
+        }
+    }
+    const StreamPlan P = plan_bin_rows(WARPS, STAGES, g.nrbins, a.nz, EXACT, T);
     cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)P.total);
-    int per_sm = 0;
-    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, WARPS * 32, P.total) != cudaSuccess ||
-        per_sm < 1)
-        return -1;
     const long long ntiles = (nrows + T.trows - 1) / T.trows;
     const int groups = WARPS / T.wg;
     long long n = (long long)sm_count_s() * per_sm;
