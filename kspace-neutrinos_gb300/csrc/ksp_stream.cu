@@ -612,6 +612,10 @@ struct RowTiling {
     int copies;       // copies of the CTA's bin totals: tile row r adds to copy r % copies
 };
 
+// floats from one copy of the bin totals ({H[nrbins]}, {L[nrbins]}) to the next: 2 nrbins
+// padded to 16 modulo 32, so that a bin sits in opposite half-banks of neighbouring copies
+__host__ __device__ inline int totals_stride(int nrbins) { return 2 * nrbins + ((48 - (2 * nrbins) % 32) % 32); }
+
 inline RowTiling make_row_tiling(int nz) {
     RowTiling t;
     t.R = (nz + kRun - 1) / kRun;
@@ -640,7 +644,7 @@ __host__ __device__ inline StreamPlan plan_bin_rows(int warps, int stages, int n
     p.spill_off = o;
     o += (size_t)warps * kRun * 32 * (exact ? 8 : 4);  // a slot per bin of a run: at most kRun
     p.hist_off = o;
-    o += sizeof(float) * 2 * (size_t)nrbins * T.copies;
+    o += sizeof(float) * (size_t)totals_stride(nrbins) * T.copies;
     p.thr_off = o;
     o += sizeof(int) * (size_t)(nrbins + 1);
     o = (o + 15) & ~size_t(15);
@@ -682,7 +686,8 @@ __global__ void __launch_bounds__(WARPS * 32)
     float* s_H0 = reinterpret_cast<float*>(base + P.hist_off);
     int* s_thr = reinterpret_cast<int*>(base + P.thr_off);
     float2* s_wt = reinterpret_cast<float2*>(base + P.tab_off);
-    for (int i = tid; i < 2 * g.nrbins * T.copies; i += blockDim.x) s_H0[i] = 0.f;
+    const int hstride = totals_stride(g.nrbins);
+    for (int i = tid; i < hstride * T.copies; i += blockDim.x) s_H0[i] = 0.f;
     for (int i = tid; i < g.nrbins; i += blockDim.x) s_thr[i] = thresh[i];
     for (int i = tid; i < g.nz + kRun; i += blockDim.x)
         s_wt[i] = i < g.nz ? make_float2(w1g[i], (i == 0 || i == g.half) ? 1.f : 2.f) : make_float2(0.f, 0.f);
@@ -724,7 +729,7 @@ __global__ void __launch_bounds__(WARPS * 32)
     // Lanes of one warp on different tile rows cover nearly the same bins at the same
     // time (neighbouring rows have nearly the same kx^2 + ky^2); separate copies of the
     // totals keep their shared atomics off each other's addresses.
-    float* s_H = s_H0 + (size_t)(row_t % T.copies) * 2 * g.nrbins;
+    float* s_H = s_H0 + (size_t)(row_t % T.copies) * hstride;
     float* s_L = s_H + g.nrbins;
 
     const long long gg = (long long)blockIdx.x * groups + grp, TG = (long long)gridDim.x * groups;
@@ -832,7 +837,7 @@ __global__ void __launch_bounds__(WARPS * 32)
     for (int b = tid; b < g.nrbins; b += blockDim.x) {
         double v = 0.0;
         for (int c = 0; c < T.copies; c++)
-            v += (double)s_H0[2 * c * g.nrbins + b] + (double)s_H0[(2 * c + 1) * g.nrbins + b];
+            v += (double)s_H0[c * hstride + b] + (double)s_H0[c * hstride + g.nrbins + b];
         if (v != 0.0) atomicAdd(bin_sum + b, v);
     }
 }
