@@ -290,12 +290,20 @@ __global__ void __launch_bounds__(128) kb_dnu_qag(BatchDev b) {
         const Background* B = I.B;
         const StepScalars& S = *I.sc;
         const int Na = P.Na;
-        const double mnubykT = B->mnu_J[mi] / B->kBtnu;
         const double k = I.wavenum[ik];
-        // initial-condition piece (delta_tot_table.c:525-535); qc = 0 here
-        const double specJ0 = specialJ(k * S.fsl_A0a / (mnubykT > 0 ? mnubykT : 1), 0.0, B->nufrac_low[0]);
-        double val = specJ0 * I.nu_init[ik] * (1. + S.deriv_prefac * S.fsl_A0a);
-        if (!S.skip_integral && Na > 1 && mnubykT > 0) {
+        // the task's divisions on lane 0
+        double mnubykT = 0, kom = 0, fsi = 0;
+        if (lane == 0) {
+            mnubykT = B->mnu_J[mi] / B->kBtnu;
+            kom = k / mnubykT;
+            fsi = (S.Nfs - 1.) / (S.loga - S.loga0);
+        }
+        mnubykT = __shfl_sync(0xffffffffu, mnubykT, 0);
+        kom = __shfl_sync(0xffffffffu, kom, 0);
+        fsi = __shfl_sync(0xffffffffu, fsi, 0);
+        double integral = 0;
+        const bool integrate = !S.skip_integral && Na > 1 && mnubykT > 0;
+        if (integrate) {
             const unsigned bytes = (unsigned)(((Na + 1) & ~1) * sizeof(double));
             __syncwarp();
             if (lane == 0) {
@@ -316,12 +324,12 @@ __global__ void __launch_bounds__(128) kb_dnu_qag(BatchDev b) {
             if (Na > 2) seg_poly(row, rc, Na, ks, sb, sd, lane, 32);
             __syncwarp();
             const double qc = S.partnu_now > 0 ? B->vcrit * mnubykT : 0.0;
-            const DnuIntegrandC f = dnu_integrand(I, S, k, mnubykT, qc, knots, row, rc, sb, sd, Na);
+            const DnuIntegrandC f = dnu_integrand_pre(I, S, kom, fsi, qc, knots, row, rc, sb, sd, Na);
             const QagResult r = qag_warp_c(f, N, L, S.loga0, S.loga, 0.0, S.relerr, kQagLimit);
-            val += S.prefac * r.result;
+            integral = r.result;
             if (!r.ok && lane == 0) atomicOr(I.status, kStGsl);
         }
-        if (lane == 0) I.dnu_s[(size_t)mi * I.nk_alloc + ik] = val;
+        if (lane == 0) I.dnu_s[(size_t)mi * I.nk_alloc + ik] = dnu_task_value(I, S, ik, k, mnubykT, integrate, integral);
     }
 }
 

@@ -812,6 +812,184 @@ __device__ QagResult qag_block_c(const F& f, const Gk61Nodes& N, QagList& L, dou
     return R;
 }
 
+// ------------------------------------------------------------------ block QAG with look-ahead
+// qag_block_c with one level of look-ahead.  On these integrands QAG nearly always
+// bisects next the right half it has just made (the late-time end, where delta_tot and
+// the free-streaming kernel change fastest).  A round that evaluates the halves of
+// interval k therefore also evaluates the halves of k's right half; when the next round
+// picks that half, its rule results are already there and the round is bookkeeping only,
+// so the sequential evaluation rounds are halved.  Node values come from the same
+// node_at, and each interval's sums are formed by one warp in the lane layout of a
+// two-interval gk61_block_c call, so every rule result -- and every decision -- is bit
+// for bit that of qag_block_c.  blockDim.x = 256: the 244 node slots of a round in one
+// pass.  Shared scratch: QagSpecSmem.
+struct QagSpecSmem {
+    double fv[244];  // group A: slots [0, 122), group B: [122, 244)
+    GkOut out[4];    // group A intervals 0, 1 | group B intervals 0, 1
+    GkOut pg[2];     // rule results of the halves of list entry pre_k
+    int k, hit, cont, ok, pre_k;
+    double errsum;
+};
+
+template <class T>
+__device__ __forceinline__ T pick4(int q, T v0, T v1, T v2, T v3) {
+    return q < 2 ? (q == 0 ? v0 : v1) : (q == 2 ? v2 : v3);
+}
+
+// Rule results of two groups of intervals, nA in {1, 2} (intervals 0, 1) and nB in
+// {0, 1, 2} (intervals 2, 3): ends a[q], b[q], node-table slots slot[q].  Warp 0 sums
+// group A, warp 1 group B, each as gk61_block_c sums a call of that many intervals.
+template <class F>
+__device__ __forceinline__ void gk61_block_groups(const F& f, const Gk61Nodes& N, int nA, int nB, const double* a,
+                                                  const double* b, const int* slot, QagSpecSmem& sh) {
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    double c[4], h[4];
+#pragma unroll
+    for (int q = 0; q < 4; q++) {
+        c[q] = __dmul_rn(0.5, __dadd_rn(a[q], b[q]));
+        h[q] = __dmul_rn(0.5, __dsub_rn(b[q], a[q]));
+    }
+    for (int s = tid; s < 244; s += blockDim.x) {
+        const int g = s >= 122 ? 1 : 0;
+        const int u = s - 122 * g;
+        const int t = u >= 61 ? 1 : 0;
+        const int j = u - 61 * t;
+        if (t < (g ? nB : nA)) {
+            const int q = 2 * g + t;
+            sh.fv[s] = f.node_at(pick4(q, slot[0], slot[1], slot[2], slot[3]), j, pick4(q, c[0], c[1], c[2], c[3]),
+                                 pick4(q, h[0], h[1], h[2], h[3]), N.x[j]);
+        }
+    }
+    __syncthreads();
+    const int ng = warp == 0 ? nA : (warp == 1 ? nB : 0);
+    if (ng > 0) {  // warp-uniform
+        const double* fvg = sh.fv + 122 * warp;
+        double fv[4];
+#pragma unroll
+        for (int m = 0; m < 4; m++) {
+            const int sl = lane + 32 * m;
+            fv[m] = sl < 61 * ng ? fvg[sl] : 0.0;
+        }
+        const double hh[2] = {warp ? h[2] : h[0], warp ? h[3] : h[1]};
+        GkOut o[2];
+        gk61_lane_sums(N, fv, 61 * ng, ng, hh, o);
+        if (lane == 0) {
+            sh.out[2 * warp] = o[0];
+            if (ng > 1) sh.out[2 * warp + 1] = o[1];
+        }
+    }
+    __syncthreads();
+}
+
+template <class F>
+__device__ QagResult qag_block_spec_c(const F& f, const Gk61Nodes& N, QagList& L, double a, double b, double epsabs,
+                                      double epsrel, int limit, QagSpecSmem& sh) {
+    const int tid = threadIdx.x, lane = tid & 31;
+    const int ns = f.nc.nslots;
+    QagResult R;
+    const int s0 = ns > 0 ? 0 : -1;
+    {  // the root, and its halves ahead
+        const double m = 0.5 * (a + b);
+        const double aa[4] = {a, a, a, m}, bb[4] = {b, b, m, b};
+        const int ss[4] = {s0, -1, nc_child(s0, 0, ns), nc_child(s0, 1, ns)};
+        gk61_block_groups(f, N, 1, 2, aa, bb, ss, sh);
+    }
+    const GkOut g0 = sh.out[0];
+    if (tid == 0) {
+        L.a[0] = a; L.b[0] = b; L.r[0] = g0.result; L.e[0] = g0.abserr; L.slot[0] = s0;
+        sh.pre_k = 0; sh.pg[0] = sh.out[2]; sh.pg[1] = sh.out[3];
+    }
+    __syncthreads();
+    double tol = fmax(epsabs, epsrel * fabs(g0.result));
+    const double round_off = 50 * DBL_EPSILON * g0.resabs;
+    R.nint = 1;
+    R.result = g0.result;
+    R.abserr = g0.abserr;
+    if (g0.abserr <= round_off && g0.abserr > tol) { R.ok = 0; return R; }
+    if ((g0.abserr <= tol && g0.abserr != g0.resasc) || g0.abserr == 0.0) { R.ok = 1; return R; }
+    if (limit == 1) { R.ok = 0; return R; }
+    double area = g0.result, errsum = g0.abserr;
+    int n = 1, roundoff1 = 0, roundoff2 = 0, error_type = 0;
+    do {
+        // warp 0 finds the interval of largest error (lowest index on ties) and whether
+        // its halves are already evaluated
+        if (tid < 32) {
+            double best = -1.0;
+            int bk = 0x7fffffff;
+            for (int i = lane; i < n; i += 32) {
+                const double e = L.e[i];
+                if (e > best) { best = e; bk = i; }
+            }
+#pragma unroll
+            for (int o = 16; o > 0; o >>= 1) {
+                const double ob = __shfl_down_sync(0xffffffffu, best, o);
+                const int ok = __shfl_down_sync(0xffffffffu, bk, o);
+                if (ob > best || (ob == best && ok < bk)) { best = ob; bk = ok; }
+            }
+            if (lane == 0) {
+                sh.k = bk;
+                sh.hit = bk == sh.pre_k;
+            }
+        }
+        __syncthreads();
+        const int k = sh.k;
+        if (!sh.hit) {  // block-uniform: the halves of k, and the halves of its right half ahead
+            const double a_i = L.a[k], b_i = L.b[k];
+            const int s_i = L.slot[k];
+            const double b1 = 0.5 * (a_i + b_i);
+            const double m2 = 0.5 * (b1 + b_i);
+            const int c1 = nc_child(s_i, 1, ns);
+            const double aa[4] = {a_i, b1, b1, m2}, bb[4] = {b1, b_i, m2, b_i};
+            const int ss[4] = {nc_child(s_i, 0, ns), c1, nc_child(c1, 0, ns), nc_child(c1, 1, ns)};
+            gk61_block_groups(f, N, 2, 2, aa, bb, ss, sh);
+        }
+        // QUADPACK's bookkeeping on thread 0
+        if (tid == 0) {
+            const bool hit = sh.hit;
+            const double a_i = L.a[k], b_i = L.b[k], r_i = L.r[k], e_i = L.e[k];
+            const int s_i = L.slot[k];
+            const double a1 = a_i, b1 = 0.5 * (a_i + b_i), a2 = b1, b2 = b_i;
+            const GkOut g[2] = {hit ? sh.pg[0] : sh.out[0], hit ? sh.pg[1] : sh.out[1]};
+            const double area12 = g[0].result + g[1].result, error12 = g[0].abserr + g[1].abserr;
+            errsum += error12 - e_i;
+            area += area12 - r_i;
+            if (g[0].resasc != g[0].abserr && g[1].resasc != g[1].abserr) {
+                if (fabs(r_i - area12) <= 1.0e-5 * fabs(area12) && error12 >= 0.99 * e_i) roundoff1++;
+                if (n >= 10 && error12 > e_i) roundoff2++;
+            }
+            tol = fmax(epsabs, epsrel * fabs(area));
+            if (errsum > tol) {
+                if (roundoff1 >= 6 || roundoff2 >= 20) error_type = 2;
+                const double tiny = (1 + 100 * DBL_EPSILON) * (fabs(a2) + 1000 * DBL_MIN);
+                if (fabs(a1) <= tiny && fabs(b2) <= tiny) error_type = 3;
+            }
+            L.b[k] = b1; L.r[k] = g[0].result; L.e[k] = g[0].abserr; L.slot[k] = nc_child(s_i, 0, ns);
+            L.a[n] = a2; L.b[n] = b2; L.r[n] = g[1].result; L.e[n] = g[1].abserr; L.slot[n] = nc_child(s_i, 1, ns);
+            if (hit) {
+                sh.pre_k = -1;
+            } else {
+                sh.pre_k = n;
+                sh.pg[0] = sh.out[2];
+                sh.pg[1] = sh.out[3];
+            }
+            sh.cont = n + 1 < limit && !error_type && errsum > tol;
+            sh.errsum = errsum;
+            sh.ok = errsum <= tol;
+        }
+        __syncthreads();
+        n++;
+    } while (sh.cont);
+    double sum = 0;
+    if (lane == 0)
+        for (int i = 0; i < n; i++) sum += L.r[i];
+    R.result = bcast0(sum);
+    R.abserr = sh.errsum;
+    R.nint = n;
+    R.ok = sh.ok;
+    __syncthreads();
+    return R;
+}
+
 }  // namespace ksp
 #include "ksp_jfit.cuh"
 namespace ksp {

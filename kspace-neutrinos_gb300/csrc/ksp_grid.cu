@@ -467,8 +467,9 @@ __global__ void k_finalize_power(const double* bin_sum, const double* F0sq, cons
 void launch_finalize_power(const double* bin_sum, const double* F0sq, const long long* count, const double* ksum,
                            const int* compact_bins, int nk, double BoxSize, double* power_out, double* keff_out,
                            double* dcdm_out, double* keffphys_out, cudaStream_t st) {
-    k_finalize_power<<<(nk + 127) / 128, 128, 0, st>>>(bin_sum, F0sq, count, ksum, compact_bins, nk, BoxSize,
-                                                       power_out, keff_out, dcdm_out, keffphys_out);
+    // a warp per block: the FP64 pow, sqrt and divisions of the bins spread over SMs
+    k_finalize_power<<<(nk + 31) / 32, 32, 0, st>>>(bin_sum, F0sq, count, ksum, compact_bins, nk, BoxSize, power_out,
+                                                    keff_out, dcdm_out, keffphys_out);
 }
 
 // ------------------------------------------------------------------ host launchers

@@ -430,12 +430,18 @@ __global__ void __launch_bounds__(128) k_dnu_qag(IntegratorDev I, int nk, int Na
     for (int task = blockIdx.x * nw + warp; task < ntask; task += gridDim.x * nw) {
         const int si = task / nk, ik = task % nk;
         const int mi = si == 0 ? spec_ids.x : (si == 1 ? spec_ids.y : spec_ids.z);
-        const double mnu = B->mnu_J[mi];
-        const double mnubykT = mnu / B->kBtnu;
         const double k = I.wavenum[ik];
-        // initial-condition piece (delta_tot_table.c:525-535); qc = 0 here
-        const double specJ0 = specialJ(k * S.fsl_A0a / (mnubykT > 0 ? mnubykT : 1), 0.0, B->nufrac_low[0]);
-        double val = specJ0 * I.nu_init[ik] * (1. + S.deriv_prefac * S.fsl_A0a);
+        // the task's divisions on lane 0
+        double mnubykT = 0, kom = 0, fsi = 0;
+        if (lane == 0) {
+            mnubykT = B->mnu_J[mi] / B->kBtnu;
+            kom = k / mnubykT;
+            fsi = (S.Nfs - 1.) / (S.loga - S.loga0);
+        }
+        mnubykT = __shfl_sync(0xffffffffu, mnubykT, 0);
+        kom = __shfl_sync(0xffffffffu, kom, 0);
+        fsi = __shfl_sync(0xffffffffu, fsi, 0);
+        double integral = 0;
         const bool integrate = !S.skip_integral && Na > 1 && mnubykT > 0;
         if (integrate) {
             // stage the history row and its spline coefficients (TMA bulk copies)
@@ -459,9 +465,9 @@ __global__ void __launch_bounds__(128) k_dnu_qag(IntegratorDev I, int nk, int Na
             if (Na > 2) seg_poly(row, rc, Na, ks, sb, sd, lane, 32);
             __syncwarp();
             const double qc = S.partnu_now > 0 ? B->vcrit * mnubykT : 0.0;
-            const DnuIntegrandC f = dnu_integrand(I, S, k, mnubykT, qc, knots, row, rc, sb, sd, Na);
+            const DnuIntegrandC f = dnu_integrand_pre(I, S, kom, fsi, qc, knots, row, rc, sb, sd, Na);
             QagResult r = qag_warp_c(f, N, L, S.loga0, S.loga, 0.0, S.relerr, kQagLimit);
-            val += S.prefac * r.result;
+            integral = r.result;
             if (I.ivals) {  // keep the final subdivision for the adjoint
                 double* dst = I.ivals + ((size_t)mi * I.nk_alloc + ik) * kQagLimit * 2;
                 for (int q = lane; q < r.nint; q += 32) {
@@ -474,7 +480,7 @@ __global__ void __launch_bounds__(128) k_dnu_qag(IntegratorDev I, int nk, int Na
             my_max = max(my_max, r.nint);
             my_tot += r.nint;
         }
-        if (lane == 0) I.dnu_s[(size_t)mi * I.nk_alloc + ik] = val;
+        if (lane == 0) I.dnu_s[(size_t)mi * I.nk_alloc + ik] = dnu_task_value(I, S, ik, k, mnubykT, integrate, integral);
     }
     if (lane == 0 && my_tot) {
         atomicMax(I.qag_max, my_max);
@@ -482,12 +488,22 @@ __global__ void __launch_bounds__(128) k_dnu_qag(IntegratorDev I, int nk, int Na
     }
 }
 
-// One (species, bin) task per block of W warps: the same integral as k_dnu_qag with the
-// GK61 nodes of each step spread over the block (qag_block_c, bit-identical results).
-// For calls with few tasks, where one warp per task leaves the SMs' FP64 pipes idle
-// between the long dependent chains of a single warp.
-// Shared memory: Gk61Nodes | knots[ld] | row[ld] | coef[ld] | QagList | QagBlockSmem | mbarrier
-__global__ void __launch_bounds__(128) k_dnu_qag_blk(IntegratorDev I, int nk, int Na, int nspec, int4 spec_ids) {
+// One (species, bin) task per block of 8 warps: the same integral as k_dnu_qag with the
+// GK61 nodes of each step spread over the block and one bisection level evaluated ahead
+// (qag_block_spec_c, bit-identical results).  For calls with few tasks, where one warp
+// per task leaves the SMs' FP64 pipes idle between the long dependent chains of a single
+// warp and the sequential QAG rounds set the time.
+// SPEC = false: blocks of 4 warps and qag_block_c (no look-ahead).
+// Shared memory: Gk61Nodes | knots[ld] | row[ld] | coef[ld] | QagList | QagSpecSmem or QagBlockSmem | mbarrier
+template <bool SPEC>
+struct QagBlkSmemOf { typedef QagSpecSmem type; };
+template <>
+struct QagBlkSmemOf<false> { typedef QagBlockSmem type; };
+
+template <bool SPEC>
+__global__ void __launch_bounds__(SPEC ? 256 : 128)
+    k_dnu_qag_blk(IntegratorDev I, int nk, int Na, int nspec, int4 spec_ids) {
+    typedef typename QagBlkSmemOf<SPEC>::type Smem;
     extern __shared__ __align__(16) unsigned char sm[];
     Gk61Nodes& N = *reinterpret_cast<Gk61Nodes*>(sm);
     size_t off = (sizeof(Gk61Nodes) + 15) & ~size_t(15);
@@ -502,9 +518,10 @@ __global__ void __launch_bounds__(128) k_dnu_qag_blk(IntegratorDev I, int nk, in
     off += 2 * sizeof(double) * I.ld;
     QagList& L = *reinterpret_cast<QagList*>(sm + off);
     off += (sizeof(QagList) + 15) & ~size_t(15);
-    QagBlockSmem& sh = *reinterpret_cast<QagBlockSmem*>(sm + off);
-    off += (sizeof(QagBlockSmem) + 15) & ~size_t(15);
+    Smem& sh = *reinterpret_cast<Smem*>(sm + off);
+    off += (sizeof(Smem) + 15) & ~size_t(15);
     uint64_t* bar = reinterpret_cast<uint64_t*>(sm + off);
+    __shared__ double s_task[3];  // m/kT, k/(m/kT), (Nfs-1)/(log a - log a0) of the current task
     const int tid = threadIdx.x;
     gk61_fill(N, tid, blockDim.x);
     for (int i = tid; i < Na; i += blockDim.x) knots[i] = I.scalefact[i];
@@ -521,14 +538,21 @@ __global__ void __launch_bounds__(128) k_dnu_qag_blk(IntegratorDev I, int nk, in
     for (int task = blockIdx.x; task < ntask; task += gridDim.x) {
         const int si = task / nk, ik = task % nk;
         const int mi = si == 0 ? spec_ids.x : (si == 1 ? spec_ids.y : spec_ids.z);
-        const double mnu = B->mnu_J[mi];
-        const double mnubykT = mnu / B->kBtnu;
         const double k = I.wavenum[ik];
-        const double specJ0 = specialJ(k * S.fsl_A0a / (mnubykT > 0 ? mnubykT : 1), 0.0, B->nufrac_low[0]);
-        double val = specJ0 * I.nu_init[ik] * (1. + S.deriv_prefac * S.fsl_A0a);
+        // the task's divisions on thread 0 (the barrier also ends the previous task's
+        // reads of row / rc and of these scalars)
+        __syncthreads();
+        if (tid == 0) {
+            const double m = B->mnu_J[mi] / B->kBtnu;
+            s_task[0] = m;
+            s_task[1] = k / m;
+            s_task[2] = (S.Nfs - 1.) / (S.loga - S.loga0);
+        }
+        __syncthreads();
+        const double mnubykT = s_task[0];
+        double integral = 0;
         const bool integrate = !S.skip_integral && Na > 1 && mnubykT > 0;
         if (integrate) {
-            __syncthreads();  // the previous task's readers of row / rc are done
             if (tid == 0) {
                 asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
                 mbar_expect_tx(bar, Na > 2 ? 2 * row_bytes : row_bytes);
@@ -546,9 +570,11 @@ __global__ void __launch_bounds__(128) k_dnu_qag_blk(IntegratorDev I, int nk, in
             if (Na > 2) seg_poly(row, rc, Na, ks, sb, sd, tid, blockDim.x);
             __syncthreads();
             const double qc = S.partnu_now > 0 ? B->vcrit * mnubykT : 0.0;
-            const DnuIntegrandC f = dnu_integrand(I, S, k, mnubykT, qc, knots, row, rc, sb, sd, Na);
-            const QagResult r = qag_block_c(f, N, L, S.loga0, S.loga, 0.0, S.relerr, kQagLimit, sh);
-            val += S.prefac * r.result;
+            const DnuIntegrandC f = dnu_integrand_pre(I, S, s_task[1], s_task[2], qc, knots, row, rc, sb, sd, Na);
+            QagResult r;
+            if constexpr (SPEC) r = qag_block_spec_c(f, N, L, S.loga0, S.loga, 0.0, S.relerr, kQagLimit, sh);
+            else r = qag_block_c(f, N, L, S.loga0, S.loga, 0.0, S.relerr, kQagLimit, sh);
+            integral = r.result;
             if (I.ivals) {  // keep the final subdivision for the adjoint
                 double* dst = I.ivals + ((size_t)mi * I.nk_alloc + ik) * kQagLimit * 2;
                 for (int q = tid; q < r.nint; q += blockDim.x) {
@@ -561,7 +587,7 @@ __global__ void __launch_bounds__(128) k_dnu_qag_blk(IntegratorDev I, int nk, in
             my_max = max(my_max, r.nint);
             my_tot += r.nint;
         }
-        if (tid == 0) I.dnu_s[(size_t)mi * I.nk_alloc + ik] = val;
+        if (tid == 0) I.dnu_s[(size_t)mi * I.nk_alloc + ik] = dnu_task_value(I, S, ik, k, mnubykT, integrate, integral);
     }
     if (tid == 0 && my_tot) {
         atomicMax(I.qag_max, my_max);
@@ -569,9 +595,9 @@ __global__ void __launch_bounds__(128) k_dnu_qag_blk(IntegratorDev I, int nk, in
     }
 }
 
-size_t dnu_qag_blk_smem(int ld) {
+size_t dnu_qag_blk_smem(int ld, bool spec) {
     return ((sizeof(Gk61Nodes) + 15) & ~size_t(15)) + 5 * sizeof(double) * ld + ((sizeof(QagList) + 15) & ~size_t(15)) +
-           ((sizeof(QagBlockSmem) + 15) & ~size_t(15)) + sizeof(uint64_t);
+           (((spec ? sizeof(QagSpecSmem) : sizeof(QagBlockSmem)) + 15) & ~size_t(15)) + sizeof(uint64_t);
 }
 
 // delta_tot_table.c:155-170: combine the species
@@ -655,9 +681,10 @@ void launch_integrator_rest(const IntegratorDev& I, int nk, int Na, int nspec, c
             cudaFuncSetAttribute(k_dtot_coeffs, cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024);
             dc_attr = true;
         }
-        const size_t smem = 4 * 2 * sizeof(double) * I.ld;
+        // a warp (one row at a time) per block: the latency-bound solves spread over SMs
+        const size_t smem = 2 * sizeof(double) * I.ld;
         const int staged = smem <= 200 * 1024;
-        k_dtot_coeffs<<<(nk + 3) / 4, 128, staged ? smem : 0, st>>>(I, nk, Na, staged, update_row);
+        k_dtot_coeffs<<<nk, 32, staged ? smem : 0, st>>>(I, nk, Na, staged, update_row);
     }
     int wpb = warps_per_block < 1 ? 1 : (warps_per_block > 4 ? 4 : warps_per_block);
     while (wpb > 1 && dnu_qag_smem(I.ld, wpb) > 227 * 1024) wpb--;
@@ -676,17 +703,21 @@ void launch_integrator_rest(const IntegratorDev& I, int nk, int Na, int nspec, c
             cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
             if (nsm <= 0) nsm = 1;
         }
-        // few tasks: a block of 4 warps per task; many: a warp per task
-        const int split = qag_split > 0 ? qag_split : (ntask < 4 * nsm ? 4 : 1);
-        const size_t bsmem = dnu_qag_blk_smem(I.ld);
+        // few tasks: a block of 8 warps per task with look-ahead (split 8) or of 4 warps
+        // without (split 4); many: a warp per task
+        const int split = qag_split > 0 ? qag_split : (ntask < 4 * nsm ? 8 : 1);
+        const bool spec = split >= 8;
+        const size_t bsmem = dnu_qag_blk_smem(I.ld, spec);
         if (split > 1 && bsmem <= 227 * 1024) {
             static bool blk_attr = false;
             if (!blk_attr) {
-                cudaFuncSetAttribute(k_dnu_qag_blk, cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024);
+                cudaFuncSetAttribute(k_dnu_qag_blk<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024);
+                cudaFuncSetAttribute(k_dnu_qag_blk<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024);
                 blk_attr = true;
             }
-            k_dnu_qag_blk<<<ntask, 32 * (split >= 4 ? 4 : 2), bsmem, st>>>(
-                I, nk, Na, nspec, make_int4(spec_ids[0], spec_ids[1], spec_ids[2], 0));
+            const int4 sp = make_int4(spec_ids[0], spec_ids[1], spec_ids[2], 0);
+            if (spec) k_dnu_qag_blk<true><<<ntask, 256, bsmem, st>>>(I, nk, Na, nspec, sp);
+            else k_dnu_qag_blk<false><<<ntask, split >= 4 ? 128 : 64, bsmem, st>>>(I, nk, Na, nspec, sp);
         } else {
             const int blocks = (ntask + wpb - 1) / wpb;
             k_dnu_qag<<<blocks, 32 * wpb, smem, st>>>(I, nk, Na, nspec,
@@ -712,58 +743,56 @@ void launch_delta_nu_combined(const IntegratorDev& I, int nk, int Na, double a, 
 __global__ void k_finish(IntegratorDev I, int nk, int commit_row, double a, double loga, const double* keff,
                          double* dnu_out, double* logk_out, double* ratio_out, CorrTable corr, double* norm_out,
                          int combine) {
-    if (combine) {  // k_combine's species sum first (same arithmetic)
-        const StepScalars& S = *I.sc;
-        for (int ik = threadIdx.x; ik < nk; ik += blockDim.x) {
-            double acc = 0;
-            for (int mi = 0; mi < kNuSpecies; mi++)
-                if (I.B->deg[mi] > 0) acc += I.dnu_s[(size_t)mi * I.nk_alloc + ik] * S.omeganu[mi] / S.Omega_nu_tot;
-            I.dnu[ik] = acc;
-        }
-        __syncthreads();
-    }
-    __shared__ double s3[3];
     const StepScalars& S = *I.sc;
     const bool pass = commit_row == -2;
-    if (threadIdx.x == 0) {
-        s3[0] = S.OmegaNua3; s3[1] = S.OmegaNu1; s3[2] = S.partnu;
+    if (blockIdx.x == 0 && threadIdx.x == 0) {
         if (commit_row >= 0) I.scalefact[commit_row] = loga;
         if (norm_out) *norm_out = S.kspace_prefac;
     }
-    __syncthreads();
     const double norm = S.kspace_prefac;
-    for (int ik = threadIdx.x; ik < nk; ik += blockDim.x) {
-        const double v = I.dnu[ik];
+    // delta_nu of bin ik: k_combine's species sum (same arithmetic) or the combined value
+    auto dnu_of = [&](int ik) -> double {
+        if (!combine) return I.dnu[ik];
+        double acc = 0;
+        for (int mi = 0; mi < kNuSpecies; mi++)
+            if (I.B->deg[mi] > 0) acc += I.dnu_s[(size_t)mi * I.nk_alloc + ik] * S.omeganu[mi] / S.Omega_nu_tot;
+        return acc;
+    };
+    // Bin ik's slope needs bin ik+1's final value: recomputed here rather than read back,
+    // so the bins are independent and spread over many blocks (their FP64 logs and
+    // divisions would otherwise queue on one SM).
+    for (int ik = blockIdx.x * blockDim.x + threadIdx.x; ik < nk; ik += gridDim.x * blockDim.x) {
+        const double v = dnu_of(ik);
+        if (combine) I.dnu[ik] = v;
         double out = v;
         if (!pass) {
             if (commit_row != -3) I.nu_last[ik] = v;
             if (commit_row >= 0)
                 I.dtot[(size_t)ik * I.ld + commit_row] =
-                    get_delta_tot(v, I.dcdm[ik], s3[0], S.Omeganonu, s3[1], s3[2]);
+                    get_delta_tot(v, I.dcdm[ik], S.OmegaNua3, S.Omeganonu, S.OmegaNu1, S.partnu);
             if (isnan(v)) atomicOr(I.status, kStDnuNaN);
             out = v < 0 ? 0.0 : v;  // delta_tot_table.c:246-247
         }
         dnu_out[ik] = out;
         if (keff) {
-            if (logk_out) logk_out[ik] = log(keff[ik]);
-            if (ratio_out) ratio_out[ik] = out / I.dcdm[ik];
-        }
-    }
-    __syncthreads();
-    if (keff && corr.xf) {
-        for (int j = threadIdx.x; j < nk; j += blockDim.x) {
-            const double lk = log(keff[j]);
-            const double r = dnu_out[j] / I.dcdm[j];
-            corr.xf[j] = (float)lk;
-            corr.rn[j] = (float)(norm * r);
-            double s = 0;
-            if (j + 1 < nk) {
-                const double lk1 = log(keff[j + 1]);
-                const double r1 = dnu_out[j + 1] / I.dcdm[j + 1];
-                s = norm * (r1 - r) / (lk1 - lk);
+            const double lk = log(keff[ik]);
+            const double r = out / I.dcdm[ik];
+            if (logk_out) logk_out[ik] = lk;
+            if (ratio_out) ratio_out[ik] = r;
+            if (corr.xf) {
+                corr.xf[ik] = (float)lk;
+                corr.rn[ik] = (float)(norm * r);
+                double sl = 0;
+                if (ik + 1 < nk) {
+                    const double v1 = dnu_of(ik + 1);
+                    const double out1 = pass ? v1 : (v1 < 0 ? 0.0 : v1);
+                    const double lk1 = log(keff[ik + 1]);
+                    const double r1 = out1 / I.dcdm[ik + 1];
+                    sl = norm * (r1 - r) / (lk1 - lk);
+                }
+                corr.sn[ik] = (float)sl;
+                if (!isfinite(norm * r) || !isfinite(sl)) atomicOr(I.status, kStGridNaN);
             }
-            corr.sn[j] = (float)s;
-            if (!isfinite(norm * r) || !isfinite(s)) atomicOr(I.status, kStGridNaN);
         }
     }
 }
@@ -771,8 +800,9 @@ __global__ void k_finish(IntegratorDev I, int nk, int commit_row, double a, doub
 void launch_finish_update(const IntegratorDev& I, int nk, int commit_row, double a, double loga,
                           const double* keff, double* dnu_out, double* logk_out, double* ratio_out,
                           CorrTable corr, double* norm_out, cudaStream_t st, bool combine) {
-    k_finish<<<1, 1024, 0, st>>>(I, nk, commit_row, a, loga, keff, dnu_out, logk_out, ratio_out, corr, norm_out,
-                                 combine ? 1 : 0);
+    k_finish<<<(nk + 31) / 32 > 0 ? (nk + 31) / 32 : 1, 32, 0, st>>>(I, nk, commit_row, a, loga, keff, dnu_out,
+                                                                     logk_out, ratio_out, corr, norm_out,
+                                                                     combine ? 1 : 0);
 }
 
 }  // namespace ksp

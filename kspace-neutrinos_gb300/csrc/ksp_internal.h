@@ -381,19 +381,37 @@ __device__ __forceinline__ void dtot_row_coeffs_scan(const IntegratorDev& I, int
 // The delta_nu integrand of one (species, bin) with the instance's node table; knots,
 // row and rc may be staged copies (shared memory) of the instance's arrays.
 // sb, sd: seg_poly of (row, rc), filled by the caller
-__device__ __forceinline__ DnuIntegrandC dnu_integrand(const IntegratorDev& I, const StepScalars& S, double k,
-                                                       double mnubykT, double qc, const double* knots,
-                                                       const double* row, const double* rc, const double* sb,
-                                                       const double* sd, int Na) {
+// k_over_m = k / (m / kT) and fs_inv = (Nfs - 1) / (log a - log a0) given: the integral
+// kernels form those divisions on one lane per task and broadcast them
+__device__ __forceinline__ DnuIntegrandC dnu_integrand_pre(const IntegratorDev& I, const StepScalars& S,
+                                                           double k_over_m, double fs_inv, double qc,
+                                                           const double* knots, const double* row, const double* rc,
+                                                           const double* sb, const double* sd, int Na) {
     DnuIntegrandC f;
-    f.B = I.B; f.k_over_m = k / mnubykT; f.qc = qc; f.nfl = I.B->nufrac_low[0];
+    f.B = I.B; f.k_over_m = k_over_m; f.qc = qc; f.nfl = I.B->nufrac_low[0];
     f.fs_x = I.fs_x; f.fs_y = I.fs_y; f.fs_c = I.fs_c; f.nfs = S.Nfs; f.fs_x0 = S.loga0;
-    f.fs_inv = (S.Nfs - 1.) / (S.loga - S.loga0);
+    f.fs_inv = fs_inv;
     f.kx = knots; f.ky = row; f.kc = rc; f.na = Na;
     f.sb = sb; f.sd = sd;
     f.ks = KnotSeg{I.knot_invh, I.knot_h3, I.knot_ih3};
     f.nc = NodeCache{I.nc_g, I.nc_fsl, I.nc_dx, I.nc_j, I.nc_slots};
     return f;
+}
+__device__ __forceinline__ DnuIntegrandC dnu_integrand(const IntegratorDev& I, const StepScalars& S, double k,
+                                                       double mnubykT, double qc, const double* knots,
+                                                       const double* row, const double* rc, const double* sb,
+                                                       const double* sd, int Na) {
+    return dnu_integrand_pre(I, S, k / mnubykT, (S.Nfs - 1.) / (S.loga - S.loga0), qc, knots, row, rc, sb, sd, Na);
+}
+// The delta_nu of one (species, bin) task (delta_tot_table.c:525-535 and :597-603): the
+// initial-condition term plus prefac times the integral; one lane forms it (FP64 log and
+// exp of the J fit are issued per active lane).
+__device__ __forceinline__ double dnu_task_value(const IntegratorDev& I, const StepScalars& S, int ik,
+                                                 double k, double mnubykT, bool integrated, double integral) {
+    const double specJ0 = specialJ(k * S.fsl_A0a / (mnubykT > 0 ? mnubykT : 1), 0.0, I.B->nufrac_low[0]);
+    double val = specJ0 * I.nu_init[ik] * (1. + S.deriv_prefac * S.fsl_A0a);
+    if (integrated) val += S.prefac * integral;
+    return val;
 }
 #endif
 
