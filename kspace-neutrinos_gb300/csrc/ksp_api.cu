@@ -874,10 +874,33 @@ static SlabChunks make_chunks(int nslab, int pmgrid, int want) {
     return ch;
 }
 
+// The integrator work that does not depend on this step's delta_cdm (scalars, knot
+// factorisation, fslength and node tables), on the side stream beside the binning pass;
+// update_device waits for it.  Only for the common case: a new scale factor on an
+// initialised table with room for the provisional row.  Queued after the binning pass
+// (but ordered only after ev_fork, recorded before it), so that the device starts on
+// the grid without waiting for these launches.
+static int start_prep(kspace_ctx* c, const Geo* G, double Time) {
+    c->prep_valid = false;
+    if (!(c->init_done && c->ia >= 1 && c->ia < c->I.namax && G->nk == c->nk && c->nk >= 2)) return KSPACE_OK;
+    const double loga = log(Time);
+    if (loga - c->h_scalefact[c->ia - 1] < kFloatAcc) return KSPACE_OK;
+    const int Na = c->ia + 1;
+    CK(cudaStreamWaitEvent(c->side, c->ev_fork, 0));  // recorded before the binning pass
+    launch_integrator_prepare(c->I, Na, Time, loga, c->loga0, c->TimeTransfer, c->fact_valid, 1, false, c->side);
+    CK(cudaEventRecord(c->ev_join, c->side));
+    g_launches += 5;
+    c->prep_valid = true;
+    c->prep_Na = Na;
+    c->prep_loga = loga;
+    return KSPACE_OK;
+}
+
 // K1 + allreduce + normalisation into compacted arrays (device): power, keff (grid
-// units), dcdm and keff (physical) for the integrator.
+// units), dcdm and keff (physical) for the integrator.  prep_time > 0: start the
+// integrator's preparation for that scale factor once the binning pass is queued.
 static int bin_grid(kspace_ctx* c, Geo* G, const float* gd, int pmgrid, int slab0, int nslab, double BoxSize,
-                    const SlabChunks* ch = nullptr) {
+                    const SlabChunks* ch = nullptr, double prep_time = 0) {
     NEED(c->table_ready && c->buf_nb >= G->g.nrbins, KSPACE_ERR_ORDER);
     const int nb = G->g.nrbins;
     G->g.slab0 = slab0;
@@ -907,6 +930,10 @@ static int bin_grid(kspace_ctx* c, Geo* G, const float* gd, int pmgrid, int slab
         }
     }
     if (c->prof) cudaEventRecord(c->ev[1], c->stream);
+    if (prep_time > 0) {
+        const int sp = start_prep(c, G, prep_time);
+        if (sp) return sp;
+    }
     if (c->ar_fn) {
         CK(cudaMemcpyAsync(c->ar_h, c->bin_sum_d, sizeof(double) * (nb + 1), cudaMemcpyDeviceToHost, c->stream));
         CK(cudaStreamSynchronize(c->stream));
@@ -1016,28 +1043,12 @@ extern "C" int kspace_gpu_add_nu_power_to_rhogrid(kspace_ctx* c, double Time, do
     } else {
         gd = reinterpret_cast<float*>(grid);
     }
-    // The integrator work that does not depend on this step's delta_cdm (scalars, knot
-    // factorisation, fslength and node tables) starts now on the side stream, beside
-    // the binning pass; update_device waits for it.  Only for the common case: a new
-    // scale factor on an initialised table with room for the provisional row.
+    // compute_neutrino_power_spectrum (interface_gadget.c:75-102); the integrator's
+    // delta_cdm-independent work starts beside the binning pass (start_prep), after the
+    // work queued so far on the context's stream
     c->prep_valid = false;
-    if (c->init_done && c->ia >= 1 && c->ia < c->I.namax && G->nk == c->nk && c->nk >= 2) {
-        const double loga = log(Time);
-        if (!(loga - c->h_scalefact[c->ia - 1] < kFloatAcc)) {
-            const int Na = c->ia + 1;
-            CK(cudaEventRecord(c->ev_fork, c->stream));
-            CK(cudaStreamWaitEvent(c->side, c->ev_fork, 0));
-            launch_integrator_prepare(c->I, Na, Time, loga, c->loga0, c->TimeTransfer, c->fact_valid, 1, false,
-                                      c->side);
-            CK(cudaEventRecord(c->ev_join, c->side));
-            g_launches += 5;
-            c->prep_valid = true;
-            c->prep_Na = Na;
-            c->prep_loga = loga;
-        }
-    }
-    // compute_neutrino_power_spectrum (interface_gadget.c:75-102)
-    st = bin_grid(c, G, gd, pmgrid, slab0, nslab, BoxSize, staged ? &ch : nullptr);
+    CK(cudaEventRecord(c->ev_fork, c->stream));
+    st = bin_grid(c, G, gd, pmgrid, slab0, nslab, BoxSize, staged ? &ch : nullptr, Time);
     if (st) return st;
     // the integrator (interface_common.c:125-148)
     st = update_device(c, Time, G->nk, c->keff_d, c->I.dcdm, c->dnu_out_d, true);

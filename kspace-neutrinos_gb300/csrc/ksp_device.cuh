@@ -583,10 +583,18 @@ template <class F>
 __device__ __forceinline__ void gk61_warp_c(const F& f, const Gk61Nodes& N, int nint, const double* a,
                                             const double* b, const int* slot, GkOut* out) {
     const int lane = threadIdx.x & 31;
-    double c[2], h[2];
+    // the intervals' geometry on lane 0, broadcast (FP64 is issued per active lane)
+    double c[2] = {0.0, 0.0}, h[2] = {0.0, 0.0};
+    if (lane == 0) {
+        for (int t = 0; t < 2; t++) {
+            c[t] = __dmul_rn(0.5, __dadd_rn(a[t], b[t]));
+            h[t] = __dmul_rn(0.5, __dsub_rn(b[t], a[t]));
+        }
+    }
+#pragma unroll
     for (int t = 0; t < 2; t++) {
-        c[t] = __dmul_rn(0.5, __dadd_rn(a[t], b[t]));
-        h[t] = __dmul_rn(0.5, __dsub_rn(b[t], a[t]));
+        c[t] = __shfl_sync(0xffffffffu, c[t], 0);
+        h[t] = __shfl_sync(0xffffffffu, h[t], 0);
     }
     double fv[4];
     const int nslots = 61 * nint;
@@ -827,28 +835,26 @@ struct QagSpecSmem {
     double fv[244];  // group A: slots [0, 122), group B: [122, 244)
     GkOut out[4];    // group A intervals 0, 1 | group B intervals 0, 1
     GkOut pg[2];     // rule results of the halves of list entry pre_k
+    double ic[4], ih[4];  // centre and half-width of the intervals of the next evaluation
+    int isl[4];           // and their node-table slots
     int k, hit, cont, ok, pre_k;
     double errsum;
 };
 
-template <class T>
-__device__ __forceinline__ T pick4(int q, T v0, T v1, T v2, T v3) {
-    return q < 2 ? (q == 0 ? v0 : v1) : (q == 2 ? v2 : v3);
+// The geometry of interval q of the next evaluation, formed once (one thread) as every
+// GK61 call forms it: c = (a + b) / 2, h = (b - a) / 2.
+__device__ __forceinline__ void spec_set_interval(QagSpecSmem& sh, int q, double a, double b, int slot) {
+    sh.ic[q] = __dmul_rn(0.5, __dadd_rn(a, b));
+    sh.ih[q] = __dmul_rn(0.5, __dsub_rn(b, a));
+    sh.isl[q] = slot;
 }
 
 // Rule results of two groups of intervals, nA in {1, 2} (intervals 0, 1) and nB in
-// {0, 1, 2} (intervals 2, 3): ends a[q], b[q], node-table slots slot[q].  Warp 0 sums
+// {0, 1, 2} (intervals 2, 3), whose geometry is in sh.ic / sh.ih / sh.isl.  Warp 0 sums
 // group A, warp 1 group B, each as gk61_block_c sums a call of that many intervals.
 template <class F>
-__device__ __forceinline__ void gk61_block_groups(const F& f, const Gk61Nodes& N, int nA, int nB, const double* a,
-                                                  const double* b, const int* slot, QagSpecSmem& sh) {
+__device__ __forceinline__ void gk61_block_groups(const F& f, const Gk61Nodes& N, int nA, int nB, QagSpecSmem& sh) {
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
-    double c[4], h[4];
-#pragma unroll
-    for (int q = 0; q < 4; q++) {
-        c[q] = __dmul_rn(0.5, __dadd_rn(a[q], b[q]));
-        h[q] = __dmul_rn(0.5, __dsub_rn(b[q], a[q]));
-    }
     for (int s = tid; s < 244; s += blockDim.x) {
         const int g = s >= 122 ? 1 : 0;
         const int u = s - 122 * g;
@@ -856,8 +862,7 @@ __device__ __forceinline__ void gk61_block_groups(const F& f, const Gk61Nodes& N
         const int j = u - 61 * t;
         if (t < (g ? nB : nA)) {
             const int q = 2 * g + t;
-            sh.fv[s] = f.node_at(pick4(q, slot[0], slot[1], slot[2], slot[3]), j, pick4(q, c[0], c[1], c[2], c[3]),
-                                 pick4(q, h[0], h[1], h[2], h[3]), N.x[j]);
+            sh.fv[s] = f.node_at(sh.isl[q], j, sh.ic[q], sh.ih[q], N.x[j]);
         }
     }
     __syncthreads();
@@ -870,7 +875,7 @@ __device__ __forceinline__ void gk61_block_groups(const F& f, const Gk61Nodes& N
             const int sl = lane + 32 * m;
             fv[m] = sl < 61 * ng ? fvg[sl] : 0.0;
         }
-        const double hh[2] = {warp ? h[2] : h[0], warp ? h[3] : h[1]};
+        const double hh[2] = {sh.ih[2 * warp], sh.ih[2 * warp + 1]};
         GkOut o[2];
         gk61_lane_sums(N, fv, 61 * ng, ng, hh, o);
         if (lane == 0) {
@@ -888,12 +893,14 @@ __device__ QagResult qag_block_spec_c(const F& f, const Gk61Nodes& N, QagList& L
     const int ns = f.nc.nslots;
     QagResult R;
     const int s0 = ns > 0 ? 0 : -1;
-    {  // the root, and its halves ahead
+    if (tid == 0) {  // the root, and its halves ahead
         const double m = 0.5 * (a + b);
-        const double aa[4] = {a, a, a, m}, bb[4] = {b, b, m, b};
-        const int ss[4] = {s0, -1, nc_child(s0, 0, ns), nc_child(s0, 1, ns)};
-        gk61_block_groups(f, N, 1, 2, aa, bb, ss, sh);
+        spec_set_interval(sh, 0, a, b, s0);
+        spec_set_interval(sh, 2, a, m, nc_child(s0, 0, ns));
+        spec_set_interval(sh, 3, m, b, nc_child(s0, 1, ns));
     }
+    __syncthreads();
+    gk61_block_groups(f, N, 1, 2, sh);
     const GkOut g0 = sh.out[0];
     if (tid == 0) {
         L.a[0] = a; L.b[0] = b; L.r[0] = g0.result; L.e[0] = g0.abserr; L.slot[0] = s0;
@@ -911,8 +918,9 @@ __device__ QagResult qag_block_spec_c(const F& f, const Gk61Nodes& N, QagList& L
     double area = g0.result, errsum = g0.abserr;
     int n = 1, roundoff1 = 0, roundoff2 = 0, error_type = 0;
     do {
-        // warp 0 finds the interval of largest error (lowest index on ties) and whether
-        // its halves are already evaluated
+        // warp 0 finds the interval of largest error (lowest index on ties); its lane 0
+        // notes whether the halves are already evaluated and, if not, lays out the halves
+        // of k and of k's right half
         if (tid < 32) {
             double best = -1.0;
             int bk = 0x7fffffff;
@@ -927,22 +935,25 @@ __device__ QagResult qag_block_spec_c(const F& f, const Gk61Nodes& N, QagList& L
                 if (ob > best || (ob == best && ok < bk)) { best = ob; bk = ok; }
             }
             if (lane == 0) {
+                const bool hit = bk == sh.pre_k;
                 sh.k = bk;
-                sh.hit = bk == sh.pre_k;
+                sh.hit = hit;
+                if (!hit) {
+                    const double a_i = L.a[bk], b_i = L.b[bk];
+                    const int s_i = L.slot[bk];
+                    const double b1 = 0.5 * (a_i + b_i);
+                    const double m2 = 0.5 * (b1 + b_i);
+                    const int c1 = nc_child(s_i, 1, ns);
+                    spec_set_interval(sh, 0, a_i, b1, nc_child(s_i, 0, ns));
+                    spec_set_interval(sh, 1, b1, b_i, c1);
+                    spec_set_interval(sh, 2, b1, m2, nc_child(c1, 0, ns));
+                    spec_set_interval(sh, 3, m2, b_i, nc_child(c1, 1, ns));
+                }
             }
         }
         __syncthreads();
         const int k = sh.k;
-        if (!sh.hit) {  // block-uniform: the halves of k, and the halves of its right half ahead
-            const double a_i = L.a[k], b_i = L.b[k];
-            const int s_i = L.slot[k];
-            const double b1 = 0.5 * (a_i + b_i);
-            const double m2 = 0.5 * (b1 + b_i);
-            const int c1 = nc_child(s_i, 1, ns);
-            const double aa[4] = {a_i, b1, b1, m2}, bb[4] = {b1, b_i, m2, b_i};
-            const int ss[4] = {nc_child(s_i, 0, ns), c1, nc_child(c1, 0, ns), nc_child(c1, 1, ns)};
-            gk61_block_groups(f, N, 2, 2, aa, bb, ss, sh);
-        }
+        if (!sh.hit) gk61_block_groups(f, N, 2, 2, sh);  // block-uniform
         // QUADPACK's bookkeeping on thread 0
         if (tid == 0) {
             const bool hit = sh.hit;

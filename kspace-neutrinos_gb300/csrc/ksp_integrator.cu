@@ -501,7 +501,7 @@ template <>
 struct QagBlkSmemOf<false> { typedef QagBlockSmem type; };
 
 template <bool SPEC>
-__global__ void __launch_bounds__(SPEC ? 256 : 128)
+__global__ void __launch_bounds__(SPEC ? 256 : 128, SPEC ? 2 : 4)
     k_dnu_qag_blk(IntegratorDev I, int nk, int Na, int nspec, int4 spec_ids) {
     typedef typename QagBlkSmemOf<SPEC>::type Smem;
     extern __shared__ __align__(16) unsigned char sm[];

@@ -24,6 +24,10 @@
 #include <cuda.h>
 #include <cuda_runtime.h>
 #include <stdint.h>
+#include <map>
+#include <mutex>
+#include <set>
+#include <tuple>
 #include "ksp_internal.h"
 #include "ksp_gridutil.cuh"
 #include "ksp_ptx.cuh"
@@ -853,13 +857,58 @@ int sm_count_s() {
     return n;
 }
 
+// Blocks of `kern` resident per SM with `threads` threads and `smem` bytes of dynamic
+// shared memory on the current device, memoised: the occupancy query and the attribute
+// call cost host microseconds, and at every step the device waits for the first launch.
+// The kernel's dynamic shared-memory limit is raised once per device to the largest any
+// of these passes asks for (220 KB); each launch still asks for its own size.
+constexpr int kMaxSmemPass = 220 * 1024;
+template <typename K>
+int resident_blocks(K kern, int threads, size_t smem) {
+    static std::mutex m;
+    static std::map<std::tuple<const void*, int, int, size_t>, int> memo;
+    static std::set<std::pair<const void*, int>> raised;
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess) return 0;
+    const void* kp = reinterpret_cast<const void*>(kern);
+    std::lock_guard<std::mutex> lock(m);
+    const auto key = std::make_tuple(kp, dev, threads, smem);
+    const auto it = memo.find(key);
+    if (it != memo.end()) return it->second;
+    if (raised.insert(std::make_pair(kp, dev)).second)
+        cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, kMaxSmemPass);
+    int n = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, kern, threads, smem) != cudaSuccess) n = 0;
+    memo[key] = n;
+    return n;
+}
+
+// The 2-D tensor map of a grid pointer, memoised per device (a handful of grids and slab
+// chunks recur at every step); at most 64 are kept.
+bool grid_tmap_cached(CUtensorMap* map, const void* grid, long long nrows16, int rows) {
+    static std::mutex m;
+    static std::map<std::tuple<int, const void*, long long, int>, CUtensorMap> memo;
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess) return false;
+    const auto key = std::make_tuple(dev, grid, nrows16, rows);
+    std::lock_guard<std::mutex> lock(m);
+    const auto it = memo.find(key);
+    if (it != memo.end()) {
+        *map = it->second;
+        return true;
+    }
+    if (!make_grid_tmap(map, grid, nrows16, rows)) return false;
+    if (memo.size() >= 64) memo.clear();
+    memo[key] = *map;
+    return true;
+}
+
 // grid size and the per-iteration advance of a warp's tile start (TW tiles)
 template <typename K>
 bool stream_grid(K kern, int warps, size_t smem, long long ntiles, int nz, int& grid_n, int& adv_r, int& adv_z) {
-    cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-    int per_sm = 0;
-    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, warps * 32, smem) != cudaSuccess || per_sm < 1)
-        return false;
+    if (smem > (size_t)kMaxSmemPass) return false;
+    const int per_sm = resident_blocks(kern, warps * 32, smem);
+    if (per_sm < 1) return false;
     long long n = (long long)sm_count_s() * per_sm;
     const long long need = (ntiles + warps - 1) / warps;
     if (n > need) n = need > 0 ? need : 1;
@@ -897,11 +946,7 @@ int run_bin_rows(const GridGeom& g, const GridArgs& a, const float* grid, double
     auto kern = k_bin_rows<WARPS, STAGES, EXACT>;
     auto blocks_per_sm = [&](const RowTiling& t) -> int {
         const StreamPlan p = plan_bin_rows(WARPS, STAGES, g.nrbins, a.nz, EXACT, t);
-        if (p.total > 220 * 1024) return 0;
-        cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)p.total);
-        int n = 0;
-        if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, kern, WARPS * 32, p.total) != cudaSuccess) return 0;
-        return n;
+        return p.total > (size_t)kMaxSmemPass ? 0 : resident_blocks(kern, WARPS * 32, p.total);
     };
     const int per_sm = blocks_per_sm(T);
     if (per_sm < 1) return -1;
@@ -916,7 +961,6 @@ int run_bin_rows(const GridGeom& g, const GridArgs& a, const float* grid, double
         }
     }
     const StreamPlan P = plan_bin_rows(WARPS, STAGES, g.nrbins, a.nz, EXACT, T);
-    cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)P.total);
     const long long ntiles = (nrows + T.trows - 1) / T.trows;
     const int groups = WARPS / T.wg;
     long long n = (long long)sm_count_s() * per_sm;
@@ -929,7 +973,7 @@ int run_bin_rows(const GridGeom& g, const GridArgs& a, const float* grid, double
 template <int WARPS, int STAGES>
 int run_corr_stream(const GridArgs& a, float* grid, CorrTable corr, unsigned* status, cudaStream_t st) {
     CUtensorMap map;
-    if (!make_grid_tmap(&map, grid, a.nrows16, kRowsPerWarp)) return -1;
+    if (!grid_tmap_cached(&map, grid, a.nrows16, kRowsPerWarp)) return -1;
     const StreamPlan P = plan_corr_stream(WARPS, STAGES, a.nk);
     if (P.total > 220 * 1024) return -1;
     auto kern = k_correct_stream<WARPS, STAGES>;
