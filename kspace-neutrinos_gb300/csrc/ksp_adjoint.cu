@@ -777,20 +777,20 @@ void launch_dnu_adj(const IntegratorDev& I, const double* dnu_bar, double* Dbar,
                     cudaStream_t st) {
     DnuAdjArgs A{dnu_bar, Dbar, mbar, ivals, nivals, recompute};
     wpb = wpb < 1 ? 1 : (wpb > 4 ? 4 : wpb);
-    while (wpb > 1 && dnu_adj_smem(I.ld, wpb) > 227 * 1024) wpb--;
+    while (wpb > 1 && dnu_adj_smem(I.ld, wpb) > 227 * 1024 - 256) wpb--;
     const size_t smem = dnu_adj_smem(I.ld, wpb);
     static bool attr = false;
     if (!attr) {
-        cudaFuncSetAttribute(k_dnu_adj, cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024);
+        raise_dynamic_smem_limit(reinterpret_cast<const void*>(k_dnu_adj));
         attr = true;
     }
     const int ntask = nspec * nk;
     if (ntask <= 0) return;
     const size_t bsmem = dnu_adj_blk_smem(I.ld, 4);
-    if (ntask < 4 * sm_count_a() && bsmem <= 227 * 1024) {
+    if (ntask < 4 * sm_count_a() && bsmem <= 227 * 1024 - 256) {
         static bool blk_attr = false;
         if (!blk_attr) {
-            cudaFuncSetAttribute(k_dnu_adj_blk, cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024);
+            raise_dynamic_smem_limit(reinterpret_cast<const void*>(k_dnu_adj_blk));
             blk_attr = true;
         }
         k_dnu_adj_blk<<<ntask, 128, bsmem, st>>>(I, A, nk, Na, nspec,

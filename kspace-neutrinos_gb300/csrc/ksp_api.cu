@@ -13,6 +13,8 @@
 #include <unistd.h>
 #include <atomic>
 #include <map>
+#include <mutex>
+#include <set>
 #include <string>
 #include <vector>
 #include "ksp_ctx.h"
@@ -61,6 +63,25 @@ static int sync_status(kspace_ctx* c) {
         fprintf(stderr, "kspace_gpu: a mode with k below half the smallest binned k was clamped to it\n");
     if (s) CK(cudaMemsetAsync(c->status_d, 0, sizeof(unsigned), c->stream));
     return map_status(s);
+}
+
+int ksp::raise_dynamic_smem_limit(const void* kernel) {
+    static std::mutex m;
+    static std::set<std::pair<const void*, int>> done;
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess) return -1;
+    std::lock_guard<std::mutex> lock(m);
+    if (done.count(std::make_pair(kernel, dev))) return 0;
+    cudaFuncAttributes fa;
+    int optin = 0;
+    if (cudaFuncGetAttributes(&fa, kernel) != cudaSuccess ||
+        cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev) != cudaSuccess)
+        return -1;
+    const int lim = optin - (int)fa.sharedSizeBytes;
+    if (lim <= 0 || cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, lim) != cudaSuccess)
+        return -1;
+    done.insert(std::make_pair(kernel, dev));
+    return 0;
 }
 
 bool ksp::is_device_ptr(const void* p) {

@@ -416,7 +416,7 @@ static void gl_nodes_b(int n, double* X, double* Wt) {  // Newton on P_n, positi
 }
 
 void batch_set_attributes() {
-    cudaFuncSetAttribute(kb_dnu_qag, cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024);
+    raise_dynamic_smem_limit(reinterpret_cast<const void*>(kb_dnu_qag));
 }
 
 void launch_batch_update(const BatchDev& b, cudaStream_t st) {

@@ -500,7 +500,7 @@ extern "C" int kspace_gpu_batch_status(kspace_batch* b, int* status) {
 
 extern "C" int kspace_gpu_batch_set_tuning(kspace_batch* b, int wpb, int blocks_per_sm, int use_graph) {
     if (!b || wpb < 1 || wpb > 4 || blocks_per_sm < 1 || blocks_per_sm > 16) return KSPACE_ERR_ARG;
-    if (batch_qag_smem(b->ldmax, wpb) > 227 * 1024) return KSPACE_ERR_ARG;
+    if (batch_qag_smem(b->ldmax, wpb) > 227 * 1024 - 256) return KSPACE_ERR_ARG;
     if (wpb != b->wpb || blocks_per_sm != b->blocks_per_sm) drop_graph(b);
     b->wpb = wpb;
     b->blocks_per_sm = blocks_per_sm;
@@ -523,7 +523,7 @@ extern "C" int kspace_gpu_batch_autotune(kspace_batch* b, const double* a, const
     int bw = wpb0, bb = bps0;
     for (int w = 1; w <= 4; w *= 2) {
         const size_t smem = batch_qag_smem(b->ldmax, w);
-        if (smem > 227 * 1024) continue;
+        if (smem > 227 * 1024 - 256) continue;
         const int fit = (int)((228 * 1024) / (smem + 1024));  // resident blocks by shared memory
         for (int bps = 1; bps <= std::min(fit, 8); bps++) {
             b->wpb = w;

@@ -297,6 +297,31 @@ KSP_HD double specialJ(double x, double qc, double nufrac_low) {
     return specialJ_fit(x);
 }
 
+// Index of the largest error among e[0..n) (lowest index on ties), on every lane of
+// the warp.  Errors are >= 0, so their IEEE bit patterns order as the numbers do: the
+// comparisons run on the integer pipe (a NaN, never chosen by the floating-point
+// comparison, gets key -1).
+__device__ __forceinline__ long long err_key(double e) {
+    const long long b = __double_as_longlong(e);
+    return (b & 0x7fffffffffffffffLL) > 0x7ff0000000000000LL ? -1LL : b;
+}
+__device__ __forceinline__ int warp_argmax_err(const double* e, int n) {
+    const int lane = threadIdx.x & 31;
+    long long best = -1;
+    int bk = 0x7fffffff;
+    for (int i = lane; i < n; i += 32) {
+        const long long v = err_key(e[i]);
+        if (v > best) { best = v; bk = i; }
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        const long long ob = __shfl_down_sync(0xffffffffu, best, o);
+        const int ok = __shfl_down_sync(0xffffffffu, bk, o);
+        if (ob > best || (ob == best && ok < bk)) { best = ob; bk = ok; }
+    }
+    return __shfl_sync(0xffffffffu, bk, 0);
+}
+
 // ------------------------------------------------------------------ QAG (GK61)
 #ifdef __CUDACC__
 struct Gk61Nodes {  // expanded 61-node table: slot j<30: -x_j, 30<=j<60: +x_{j-30}, 60: centre
@@ -429,19 +454,8 @@ __device__ QagResult qag_warp(const F& f, const Gk61Nodes& N, QagList& L, double
     int n = 1, roundoff1 = 0, roundoff2 = 0, error_type = 0;
     do {
         // argmax of the error list (lowest index on ties)
-        double best = -1.0;
-        int bk = 0x7fffffff;
-        for (int i = lane; i < n; i += 32) {
-            const double e = L.e[i];
-            if (e > best) { best = e; bk = i; }
-        }
-#pragma unroll
-        for (int o = 16; o > 0; o >>= 1) {
-            const double ob = __shfl_down_sync(0xffffffffu, best, o);
-            const int ok = __shfl_down_sync(0xffffffffu, bk, o);
-            if (ob > best || (ob == best && ok < bk)) { best = ob; bk = ok; }
-        }
-        const int k = __shfl_sync(0xffffffffu, bk, 0);
+        const int bk = warp_argmax_err(L.e, n);
+        const int k = bk;
         const double a_i = L.a[k], b_i = L.b[k], r_i = L.r[k], e_i = L.e[k];
         const double a1 = a_i, b1 = 0.5 * (a_i + b_i), a2 = b1, b2 = b_i;
         aa[0] = a1; bb[0] = b1; aa[1] = a2; bb[1] = b2;
@@ -634,19 +648,8 @@ __device__ QagResult qag_warp_c(const F& f, const Gk61Nodes& N, QagList& L, doub
     double area = g[0].result, errsum = g[0].abserr;
     int n = 1, roundoff1 = 0, roundoff2 = 0, error_type = 0, cont = 0;
     do {
-        double best = -1.0;
-        int bk = 0x7fffffff;
-        for (int i = lane; i < n; i += 32) {
-            const double e = L.e[i];
-            if (e > best) { best = e; bk = i; }
-        }
-#pragma unroll
-        for (int o = 16; o > 0; o >>= 1) {
-            const double ob = __shfl_down_sync(0xffffffffu, best, o);
-            const int ok = __shfl_down_sync(0xffffffffu, bk, o);
-            if (ob > best || (ob == best && ok < bk)) { best = ob; bk = ok; }
-        }
-        const int k = __shfl_sync(0xffffffffu, bk, 0);
+        const int bk = warp_argmax_err(L.e, n);
+        const int k = bk;
         const double a_i = L.a[k], b_i = L.b[k], r_i = L.r[k], e_i = L.e[k];
         const int s_i = L.slot[k];
         const double a1 = a_i, b1 = 0.5 * (a_i + b_i), a2 = b1, b2 = b_i;
@@ -762,18 +765,7 @@ __device__ QagResult qag_block_c(const F& f, const Gk61Nodes& N, QagList& L, dou
     do {
         // warp 0 finds the interval of largest error (lowest index on ties)
         if (tid < 32) {
-            double best = -1.0;
-            int bk = 0x7fffffff;
-            for (int i = lane; i < n; i += 32) {
-                const double e = L.e[i];
-                if (e > best) { best = e; bk = i; }
-            }
-#pragma unroll
-            for (int o = 16; o > 0; o >>= 1) {
-                const double ob = __shfl_down_sync(0xffffffffu, best, o);
-                const int ok = __shfl_down_sync(0xffffffffu, bk, o);
-                if (ob > best || (ob == best && ok < bk)) { best = ob; bk = ok; }
-            }
+            const int bk = warp_argmax_err(L.e, n);
             if (lane == 0) sh.k = bk;
         }
         __syncthreads();
@@ -922,18 +914,7 @@ __device__ QagResult qag_block_spec_c(const F& f, const Gk61Nodes& N, QagList& L
         // notes whether the halves are already evaluated and, if not, lays out the halves
         // of k and of k's right half
         if (tid < 32) {
-            double best = -1.0;
-            int bk = 0x7fffffff;
-            for (int i = lane; i < n; i += 32) {
-                const double e = L.e[i];
-                if (e > best) { best = e; bk = i; }
-            }
-#pragma unroll
-            for (int o = 16; o > 0; o >>= 1) {
-                const double ob = __shfl_down_sync(0xffffffffu, best, o);
-                const int ok = __shfl_down_sync(0xffffffffu, bk, o);
-                if (ob > best || (ob == best && ok < bk)) { best = ob; bk = ok; }
-            }
+            const int bk = warp_argmax_err(L.e, n);
             if (lane == 0) {
                 const bool hit = bk == sh.pre_k;
                 sh.k = bk;

@@ -678,7 +678,7 @@ void launch_integrator_rest(const IntegratorDev& I, int nk, int Na, int nspec, c
     if (Na > 2) {
         static bool dc_attr = false;
         if (!dc_attr) {
-            cudaFuncSetAttribute(k_dtot_coeffs, cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024);
+            raise_dynamic_smem_limit(reinterpret_cast<const void*>(k_dtot_coeffs));
             dc_attr = true;
         }
         // a warp (one row at a time) per block: the latency-bound solves spread over SMs
@@ -687,11 +687,11 @@ void launch_integrator_rest(const IntegratorDev& I, int nk, int Na, int nspec, c
         k_dtot_coeffs<<<nk, 32, staged ? smem : 0, st>>>(I, nk, Na, staged, update_row);
     }
     int wpb = warps_per_block < 1 ? 1 : (warps_per_block > 4 ? 4 : warps_per_block);
-    while (wpb > 1 && dnu_qag_smem(I.ld, wpb) > 227 * 1024) wpb--;
+    while (wpb > 1 && dnu_qag_smem(I.ld, wpb) > 227 * 1024 - 256) wpb--;
     const size_t smem = dnu_qag_smem(I.ld, wpb);
     static bool attr_set = false;
     if (!attr_set) {
-        cudaFuncSetAttribute(k_dnu_qag, cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024);
+        raise_dynamic_smem_limit(reinterpret_cast<const void*>(k_dnu_qag));
         attr_set = true;
     }
     const int ntask = nspec * nk;
@@ -708,11 +708,11 @@ void launch_integrator_rest(const IntegratorDev& I, int nk, int Na, int nspec, c
         const int split = qag_split > 0 ? qag_split : (ntask < 4 * nsm ? 8 : 1);
         const bool spec = split >= 8;
         const size_t bsmem = dnu_qag_blk_smem(I.ld, spec);
-        if (split > 1 && bsmem <= 227 * 1024) {
+        if (split > 1 && bsmem <= 227 * 1024 - 256) {
             static bool blk_attr = false;
             if (!blk_attr) {
-                cudaFuncSetAttribute(k_dnu_qag_blk<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024);
-                cudaFuncSetAttribute(k_dnu_qag_blk<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024);
+                raise_dynamic_smem_limit(reinterpret_cast<const void*>(k_dnu_qag_blk<true>));
+                raise_dynamic_smem_limit(reinterpret_cast<const void*>(k_dnu_qag_blk<false>));
                 blk_attr = true;
             }
             const int4 sp = make_int4(spec_ids[0], spec_ids[1], spec_ids[2], 0);

@@ -424,6 +424,12 @@ struct CorrTable {
     int nk;
 };
 
+// Raise a kernel's dynamic shared-memory limit to the most a block may have beside the
+// kernel's own static shared memory (the device's opt-in maximum minus it), once per
+// kernel and device (ksp_api.cu).  A fixed 227 KB request fails for a kernel with static
+// shared memory, and the failure would surface as the error of a later, unrelated launch.
+int raise_dynamic_smem_limit(const void* kernel);
+
 // ---- integrator launchers (ksp_integrator.cu)
 void launch_background_tables(Background* dB, double a0, cudaStream_t st, unsigned* status);
 void launch_spline_coeffs_1thread(const double* x, const double* y, double* c, double* scratch, int n,

@@ -89,3 +89,42 @@ def test_full_step(gpu, oracle, N, nb, Na):
         rel = np.abs(g_g - g_o) / np.maximum(np.abs(g_o), 1e-30)
         assert rel.max() < TOL_GRID, rel.max()
     k.close()
+
+
+_FRESH_PROCESS_STEPS = r"""
+import ctypes, os, sys
+sys.path[:0] = [sys.argv[1], sys.argv[1] + "/tests", sys.argv[1] + "/kspace-neutrinos_gb300"]
+import torch
+import cases, kspace_gpu as kg
+rt = None
+for name in ("libcudart.so.13", "libcudart.so"):
+    try:
+        rt = ctypes.CDLL(name)
+        break
+    except OSError:
+        pass
+c = cases.make_case(32, 32, 10, 0.5, (0.1, 0.1, 0.1))
+for split in ("8", "4", "1"):  # block QAG with and without look-ahead, warp QAG
+    os.environ["KSPACE_GPU_QAG_SPLIT"] = split  # read when a context is created
+    k = cases.gpu_instance(kg, c)
+    g = torch.as_tensor(c["grid"]).cuda()
+    for a in (0.51, 0.53):
+        k.add_nu_power_to_rhogrid(a, c["L"], g, 32)
+    k.close()
+torch.cuda.synchronize()
+print("pending", rt.cudaPeekAtLastError() if rt else 0)
+"""
+
+
+def test_no_pending_cuda_error_after_steps(gpu):
+    """Every launch path of a step leaves no CUDA error pending (a failed attribute call,
+    for instance, would otherwise surface as the error of a later, unrelated launch).
+    Run in a fresh process, since the kernels' attributes are set once per process."""
+    import os
+    import subprocess
+    import sys
+    root = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+    r = subprocess.run([sys.executable, "-c", _FRESH_PROCESS_STEPS, root], capture_output=True, text=True,
+                       timeout=600)
+    assert r.returncode == 0, r.stderr[-2000:]
+    assert "pending 0" in r.stdout, r.stdout[-500:]
