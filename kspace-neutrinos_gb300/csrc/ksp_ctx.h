@@ -34,7 +34,7 @@ struct kspace_ctx {
     kspace_allreduce_fn ar_fn = nullptr;
     void* ar_user = nullptr;
     int tma = 5, rows = 256, stages = 2, qag_warps = 1;
-    int nc_levels = 8;  // depths of QAG's rightmost bisections kept in the integrand node table
+    int nc_levels = 12;  // depths of QAG's rightmost bisections kept in the integrand node table (all)
     int qag_split = 0;  // warps per (species, bin) integral: 1, 2, 4, 8 (8: with look-ahead); 0 = by the task count
     // background
     bool bg_ready = false, hubble_ready = false;

@@ -521,7 +521,7 @@ __global__ void __launch_bounds__(SPEC ? 256 : 128, SPEC ? 2 : 4)
     Smem& sh = *reinterpret_cast<Smem*>(sm + off);
     off += (sizeof(Smem) + 15) & ~size_t(15);
     uint64_t* bar = reinterpret_cast<uint64_t*>(sm + off);
-    __shared__ double s_task[3];  // m/kT, k/(m/kT), (Nfs-1)/(log a - log a0) of the current task
+    __shared__ double s_task[4];  // m/kT, k/(m/kT), (Nfs-1)/(log a - log a0), integrate? of the current task
     const int tid = threadIdx.x;
     gk61_fill(N, tid, blockDim.x);
     for (int i = tid; i < Na; i += blockDim.x) knots[i] = I.scalefact[i];
@@ -539,26 +539,30 @@ __global__ void __launch_bounds__(SPEC ? 256 : 128, SPEC ? 2 : 4)
         const int si = task / nk, ik = task % nk;
         const int mi = si == 0 ? spec_ids.x : (si == 1 ? spec_ids.y : spec_ids.z);
         const double k = I.wavenum[ik];
-        // the task's divisions on thread 0 (the barrier also ends the previous task's
-        // reads of row / rc and of these scalars)
+        // thread 0 starts the copies of the history row and its spline coefficients, then
+        // forms the task's divisions while they land (the barrier before also ends the
+        // previous task's reads of row / rc and of these scalars)
         __syncthreads();
         if (tid == 0) {
-            const double m = B->mnu_J[mi] / B->kBtnu;
-            s_task[0] = m;
-            s_task[1] = k / m;
-            s_task[2] = (S.Nfs - 1.) / (S.loga - S.loga0);
-        }
-        __syncthreads();
-        const double mnubykT = s_task[0];
-        double integral = 0;
-        const bool integrate = !S.skip_integral && Na > 1 && mnubykT > 0;
-        if (integrate) {
-            if (tid == 0) {
+            const double mnu = B->mnu_J[mi];
+            const bool integ = !S.skip_integral && Na > 1 && mnu / B->kBtnu > 0;
+            if (integ) {
                 asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
                 mbar_expect_tx(bar, Na > 2 ? 2 * row_bytes : row_bytes);
                 bulk_g2s(row, I.dtot + (size_t)ik * I.ld, row_bytes, bar);
                 if (Na > 2) bulk_g2s(rc, I.coef + (size_t)ik * I.ld, row_bytes, bar);
             }
+            const double m = mnu / B->kBtnu;
+            s_task[0] = m;
+            s_task[1] = k / m;
+            s_task[2] = (S.Nfs - 1.) / (S.loga - S.loga0);
+            s_task[3] = integ ? 1.0 : 0.0;
+        }
+        __syncthreads();
+        const double mnubykT = s_task[0];
+        double integral = 0;
+        const bool integrate = s_task[3] != 0.0;
+        if (integrate) {
             const bool got = __syncthreads_and(mbar_wait_bounded(bar, phase));  // block-uniform
             phase ^= 1;
             if (!got) {
@@ -707,7 +711,10 @@ void launch_integrator_rest(const IntegratorDev& I, int nk, int Na, int nspec, c
         // without (split 4); many: a warp per task
         const int split = qag_split > 0 ? qag_split : (ntask < 4 * nsm ? 8 : 1);
         const bool spec = split >= 8;
-        const size_t bsmem = dnu_qag_blk_smem(I.ld, spec);
+        size_t bsmem = dnu_qag_blk_smem(I.ld, spec);
+        // split 9: one block per SM (shared memory padded past half an SM), so that the
+        // blocks beyond one per SM wait for a free SM instead of sharing one
+        if (split == 9 && bsmem < 120 * 1024) bsmem = 120 * 1024;
         if (split > 1 && bsmem <= 227 * 1024 - 256) {
             static bool blk_attr = false;
             if (!blk_attr) {
