@@ -711,10 +711,7 @@ void launch_integrator_rest(const IntegratorDev& I, int nk, int Na, int nspec, c
         // without (split 4); many: a warp per task
         const int split = qag_split > 0 ? qag_split : (ntask < 4 * nsm ? 8 : 1);
         const bool spec = split >= 8;
-        size_t bsmem = dnu_qag_blk_smem(I.ld, spec);
-        // split 9: one block per SM (shared memory padded past half an SM), so that the
-        // blocks beyond one per SM wait for a free SM instead of sharing one
-        if (split == 9 && bsmem < 120 * 1024) bsmem = 120 * 1024;
+        const size_t bsmem = dnu_qag_blk_smem(I.ld, spec);
         if (split > 1 && bsmem <= 227 * 1024 - 256) {
             static bool blk_attr = false;
             if (!blk_attr) {
