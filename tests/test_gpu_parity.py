@@ -104,22 +104,26 @@ for name in ("libcudart.so.13", "libcudart.so"):
     except OSError:
         pass
 c = cases.make_case(32, 32, 10, 0.5, (0.1, 0.1, 0.1))
+ratios = []
 for split in ("8", "4", "1"):  # block QAG with and without look-ahead, warp QAG
     os.environ["KSPACE_GPU_QAG_SPLIT"] = split  # read when a context is created
     k = cases.gpu_instance(kg, c)
     g = torch.as_tensor(c["grid"]).cuda()
     for a in (0.51, 0.53):
         k.add_nu_power_to_rhogrid(a, c["L"], g, 32)
+    ratios.append(k.last_correction()["ratio"].copy())
     k.close()
 torch.cuda.synchronize()
 print("pending", rt.cudaPeekAtLastError() if rt else 0)
+print("identical", int(all((r == ratios[0]).all() for r in ratios)))
 """
 
 
 def test_no_pending_cuda_error_after_steps(gpu):
     """Every launch path of a step leaves no CUDA error pending (a failed attribute call,
-    for instance, would otherwise surface as the error of a later, unrelated launch).
-    Run in a fresh process, since the kernels' attributes are set once per process."""
+    for instance, would otherwise surface as the error of a later, unrelated launch), and
+    the three shapes of the delta_nu integrals give bit-identical results.  Run in a fresh
+    process, since the kernels' attributes are set once per process."""
     import os
     import subprocess
     import sys
@@ -128,3 +132,4 @@ def test_no_pending_cuda_error_after_steps(gpu):
                        timeout=600)
     assert r.returncode == 0, r.stderr[-2000:]
     assert "pending 0" in r.stdout, r.stdout[-500:]
+    assert "identical 1" in r.stdout, r.stdout[-500:]
