@@ -697,8 +697,9 @@ __device__ QagResult qag_warp_c(const F& f, const Gk61Nodes& N, QagList& L, doub
 // The same rule and decisions with the node evaluations spread over the warps of a block
 // (blockDim.x = 32 * W, W = 2 or 4): thread t evaluates slot t, t + 32W, ...; warp 0
 // then forms every lane's partial sums over the slots lane + 32m in the order m = 0..3
-// and reduces them with the butterfly of gk61_warp_c, so the results are bit for bit
-// those of qag_warp_c.  Shared scratch: QagBlockSmem.
+// and reduces them with the butterfly of gk61_warp_c: the arithmetic of qag_warp_c in
+// the same order (the compiler may contract multiply-adds differently per kernel, so the
+// results agree to the last bits).  Shared scratch: QagBlockSmem.
 struct QagBlockSmem {
     double fv[128];
     GkOut out[2];
@@ -820,9 +821,10 @@ __device__ QagResult qag_block_c(const F& f, const Gk61Nodes& N, QagList& L, dou
 // picks that half, its rule results are already there and the round is bookkeeping only,
 // so the sequential evaluation rounds are halved.  Node values come from the same
 // node_at, and each interval's sums are formed by one warp in the lane layout of a
-// two-interval gk61_block_c call, so every rule result -- and every decision -- is bit
-// for bit that of qag_block_c.  blockDim.x = 256: the 244 node slots of a round in one
-// pass.  Shared scratch: QagSpecSmem.
+// two-interval gk61_block_c call, so every rule result is that of qag_block_c (to the
+// last bits, which the compiler's multiply-add contraction may change from kernel to
+// kernel) and so is every decision.  blockDim.x = 256: the 244 node slots of a round in
+// one pass.  Shared scratch: QagSpecSmem.
 struct QagSpecSmem {
     double fv[244];  // group A: slots [0, 122), group B: [122, 244)
     GkOut out[4];    // group A intervals 0, 1 | group B intervals 0, 1

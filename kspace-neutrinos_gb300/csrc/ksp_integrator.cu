@@ -490,7 +490,7 @@ __global__ void __launch_bounds__(128) k_dnu_qag(IntegratorDev I, int nk, int Na
 
 // One (species, bin) task per block of 8 warps: the same integral as k_dnu_qag with the
 // GK61 nodes of each step spread over the block and one bisection level evaluated ahead
-// (qag_block_spec_c, bit-identical results).  For calls with few tasks, where one warp
+// (qag_block_spec_c: the same decisions, sums equal to the last bits).  For calls with few tasks, where one warp
 // per task leaves the SMs' FP64 pipes idle between the long dependent chains of a single
 // warp and the sequential QAG rounds set the time.
 // SPEC = false: blocks of 4 warps and qag_block_c (no look-ahead).

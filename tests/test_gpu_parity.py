@@ -115,15 +115,19 @@ for split in ("8", "4", "1"):  # block QAG with and without look-ahead, warp QAG
     k.close()
 torch.cuda.synchronize()
 print("pending", rt.cudaPeekAtLastError() if rt else 0)
-print("identical", int(all((r == ratios[0]).all() for r in ratios)))
+import numpy as np
+dev = max(float(np.max(np.abs(r / ratios[0] - 1)[ratios[0] != 0])) for r in ratios)
+print("maxdev %.3e" % dev)
 """
 
 
 def test_no_pending_cuda_error_after_steps(gpu):
     """Every launch path of a step leaves no CUDA error pending (a failed attribute call,
     for instance, would otherwise surface as the error of a later, unrelated launch), and
-    the three shapes of the delta_nu integrals give bit-identical results.  Run in a fresh
-    process, since the kernels' attributes are set once per process."""
+    the three shapes of the delta_nu integrals agree: the same QAG decisions (a different
+    subdivision would move delta_nu by ~1e-7), sums equal to the last bits that the
+    compiler's FMA contraction may change from kernel to kernel (bar 1e-13).  Run in a
+    fresh process, since the kernels' attributes are set once per process."""
     import os
     import subprocess
     import sys
@@ -132,4 +136,5 @@ def test_no_pending_cuda_error_after_steps(gpu):
                        timeout=600)
     assert r.returncode == 0, r.stderr[-2000:]
     assert "pending 0" in r.stdout, r.stdout[-500:]
-    assert "identical 1" in r.stdout, r.stdout[-500:]
+    dev = float(r.stdout.split("maxdev")[1].split()[0])
+    assert dev < 1e-13, dev
