@@ -686,10 +686,25 @@ static int delta_tot_init(kspace_ctx* c, int nk_in, const double* keff_d, const 
 
 // get_delta_nu_update (delta_tot_table.c:193-250) on device arrays.  Optionally
 // produces the correction table of interface_common.c:134-146.
+// fin: the binning pass's normalisation when it was deferred (see bin_grid): folded into
+// the row-spline kernel of a prepared step, else launched first.
 static int update_device(kspace_ctx* c, double a, int nk_in, const double* keff_d, const double* dcdm_d,
-                         double* dnu_out_d, bool want_corr) {
+                         double* dnu_out_d, bool want_corr, const FinalizeArgs* fin = nullptr) {
     NEED(c->table_ready && c->hubble_ready, KSPACE_ERR_ORDER);
     IntegratorDev& I = c->I;
+    if (fin && fin->active) {
+        const double la = log(a);
+        const bool will_prepare = c->prep_valid && c->init_done && nk_in == c->nk && c->nk >= 2 && c->ia >= 1 &&
+                                  c->prep_Na == c->ia + 1 && c->prep_loga == la &&
+                                  !(la - c->h_scalefact[c->ia - 1] < kFloatAcc) && c->ia < I.namax;
+        if (!will_prepare) {
+            launch_finalize_power(fin->bin_sum, fin->F0sq, fin->count, fin->ksum, fin->compact_bins, nk_in,
+                                  fin->BoxSize, fin->power_out, fin->keff_out, fin->dcdm_out, fin->keffphys_out,
+                                  c->stream);
+            g_launches += 1;
+            fin = nullptr;
+        }
+    }
     if (dcdm_d != I.dcdm)
         CK(cudaMemcpyAsync(I.dcdm, dcdm_d, sizeof(double) * nk_in, cudaMemcpyDeviceToDevice, c->stream));
     if (!c->init_done) {
@@ -734,7 +749,7 @@ static int update_device(kspace_ctx* c, double a, int nk_in, const double* keff_
     if (prepared) {
         CK(cudaStreamWaitEvent(c->stream, c->ev_join, 0));
         launch_integrator_rest(I, c->nk, Na, c->nspec, c->spec_ids, c->qag_warps, c->stream, c->qag_split, prov_row,
-                               true);
+                               true, fin);
     } else {
         launch_delta_nu_combined(I, c->nk, Na, a, loga, c->loga0, c->TimeTransfer, c->fact_valid, c->nspec,
                                  c->spec_ids, c->qag_warps, c->stream, c->qag_split);
@@ -961,9 +976,15 @@ static int bin_grid(kspace_ctx* c, Geo* G, const float* gd, int pmgrid, int slab
         if (c->ar_fn(c->ar_h, nb + 1, c->ar_user) != 0) return KSPACE_ERR_ARG;
         CK(cudaMemcpyAsync(c->bin_sum_d, c->ar_h, sizeof(double) * (nb + 1), cudaMemcpyHostToDevice, c->stream));
     }
-    launch_finalize_power(c->bin_sum_d, c->F0sq_d, G->count_d, G->ksum_d, G->compact_d, G->nk, BoxSize, c->power_d,
-                          c->keffg_d, c->I.dcdm, c->keff_d, c->stream);
-    g_launches += 1;
+    c->fin = FinalizeArgs{c->bin_sum_d, c->F0sq_d, G->count_d, G->ksum_d, G->compact_d, BoxSize, c->power_d,
+                          c->keffg_d, c->I.dcdm, c->keff_d, 1};
+    if (!(prep_time > 0 && c->prep_valid)) {
+        // a prepared step does it in its row-spline kernel instead (update_device)
+        launch_finalize_power(c->bin_sum_d, c->F0sq_d, G->count_d, G->ksum_d, G->compact_d, G->nk, BoxSize,
+                              c->power_d, c->keffg_d, c->I.dcdm, c->keff_d, c->stream);
+        g_launches += 1;
+        c->fin.active = 0;
+    }
     return KSPACE_OK;
 }
 
@@ -1072,7 +1093,8 @@ extern "C" int kspace_gpu_add_nu_power_to_rhogrid(kspace_ctx* c, double Time, do
     st = bin_grid(c, G, gd, pmgrid, slab0, nslab, BoxSize, staged ? &ch : nullptr, Time);
     if (st) return st;
     // the integrator (interface_common.c:125-148)
-    st = update_device(c, Time, G->nk, c->keff_d, c->I.dcdm, c->dnu_out_d, true);
+    st = update_device(c, Time, G->nk, c->keff_d, c->I.dcdm, c->dnu_out_d, true, c->fin.active ? &c->fin : nullptr);
+    c->fin.active = 0;
     if (st) return st;
     c->last_nk = G->nk;
     c->last_BoxSize = BoxSize;

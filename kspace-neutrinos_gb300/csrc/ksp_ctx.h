@@ -89,6 +89,9 @@ struct kspace_ctx {
     bool prep_valid = false;
     int prep_Na = 0;
     double prep_loga = 0;
+    // the binning pass's normalisation, deferred into the row-spline kernel of a prepared
+    // step (active = 0: already done)
+    ksp::FinalizeArgs fin{};
     // profiling
     bool prof = false;
     cudaEvent_t ev[5] = {nullptr, nullptr, nullptr, nullptr, nullptr};

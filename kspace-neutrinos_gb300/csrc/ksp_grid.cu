@@ -452,17 +452,9 @@ __global__ void k_finalize_power(const double* bin_sum, const double* F0sq, cons
                                  double* power_out, double* keff_out, double* dcdm_out, double* keffphys_out) {
     const int c = blockIdx.x * blockDim.x + threadIdx.x;
     if (c >= nk) return;
-    const int b = compact_bins[c];
-    double p = bin_sum[b];
-    p /= *F0sq;
-    const double cnt = (double)count[b];
-    const double ke = ksum[b] / cnt;
-    p /= cnt;
-    if (power_out) power_out[c] = p;
-    if (keff_out) keff_out[c] = ke;
-    const double scale = pow(BoxSize, -3.0);
-    if (dcdm_out) dcdm_out[c] = sqrt(p / scale);
-    if (keffphys_out) keffphys_out[c] = ke * (2 * 3.14159265358979323846 / BoxSize);
+    const FinalizeArgs f{bin_sum, F0sq, count, ksum, compact_bins, BoxSize, power_out, keff_out, dcdm_out,
+                         keffphys_out, 1};
+    finalize_bin(f, c);
 }
 void launch_finalize_power(const double* bin_sum, const double* F0sq, const long long* count, const double* ksum,
                            const int* compact_bins, int nk, double BoxSize, double* power_out, double* keff_out,

@@ -352,12 +352,13 @@ __global__ void k_fs_coeffs(IntegratorDev I, int Nfs, double loga0, double loga)
 // ------------------------------------------------------------------ history splines
 // Forward/back substitution of every history row against the shared factorisation,
 // warp per row (warp-parallel affine scans when the row fits in shared memory).
-__global__ void k_dtot_coeffs(IntegratorDev I, int nk, int Na, int staged, int update_row) {
+__global__ void k_dtot_coeffs(IntegratorDev I, int nk, int Na, int staged, int update_row, FinalizeArgs fin) {
     extern __shared__ __align__(16) double sdc[];
     const int warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
     double* sy = staged ? sdc + (size_t)warp * 2 * I.ld : nullptr;
     double* sc = staged ? sy + I.ld : nullptr;
     for (int ik = blockIdx.x * nw + warp; ik < nk; ik += gridDim.x * nw) {
+        if (fin.active && (threadIdx.x & 31) == 0) finalize_bin(fin, ik);  // this bin's delta_cdm first
         if (update_row >= 0) {  // update_delta_tot (delta_tot_table.c:177-191), as k_update_row
             if ((threadIdx.x & 31) == 0) {
                 const StepScalars& S = *I.sc;
@@ -674,7 +675,16 @@ void launch_integrator_prepare(const IntegratorDev& I, int Na, double a, double 
 // The rest, after the provisional history row: spline coefficients of the rows, the
 // integrals, the species sum.
 void launch_integrator_rest(const IntegratorDev& I, int nk, int Na, int nspec, const int* spec_ids,
-                            int warps_per_block, cudaStream_t st, int qag_split, int update_row, bool defer_combine) {
+                            int warps_per_block, cudaStream_t st, int qag_split, int update_row, bool defer_combine,
+                            const FinalizeArgs* fin) {
+    // a deferred normalisation runs in the row-spline kernel, or on its own without one
+    FinalizeArgs fa{};
+    if (fin && fin->active) {
+        if (Na > 2) fa = *fin;
+        else
+            launch_finalize_power(fin->bin_sum, fin->F0sq, fin->count, fin->ksum, fin->compact_bins, nk, fin->BoxSize,
+                                  fin->power_out, fin->keff_out, fin->dcdm_out, fin->keffphys_out, st);
+    }
     if (update_row >= 0 && Na <= 2) {
         launch_update_row_scalars(I, nk, update_row, st);
         update_row = -1;
@@ -688,7 +698,7 @@ void launch_integrator_rest(const IntegratorDev& I, int nk, int Na, int nspec, c
         // a warp (one row at a time) per block: the latency-bound solves spread over SMs
         const size_t smem = 2 * sizeof(double) * I.ld;
         const int staged = smem <= 200 * 1024;
-        k_dtot_coeffs<<<nk, 32, staged ? smem : 0, st>>>(I, nk, Na, staged, update_row);
+        k_dtot_coeffs<<<nk, 32, staged ? smem : 0, st>>>(I, nk, Na, staged, update_row, fa);
     }
     int wpb = warps_per_block < 1 ? 1 : (warps_per_block > 4 ? 4 : warps_per_block);
     while (wpb > 1 && dnu_qag_smem(I.ld, wpb) > 227 * 1024 - 256) wpb--;

@@ -417,6 +417,39 @@ __device__ __forceinline__ double dnu_task_value(const IntegratorDev& I, const S
 
 // Interpolation table for the grid correction (delta_pow.c:19-37), float, per
 // non-empty bin, plus the bin -> compact index map.
+// K1's normalisation of one compact bin (powerspectrum.c:98-115 + interface_gadget.c:
+// 96-100): P = sum / |F(0)|^2 / count, keff = sum|k| / count (grid units), delta_cdm =
+// sqrt(P L^3), keff in physical units.  k_finalize_power applies it to every bin; the
+// step's row-spline kernel applies it to its bin when the binning pass deferred it.
+struct FinalizeArgs {
+    const double* bin_sum;
+    const double* F0sq;
+    const long long* count;
+    const double* ksum;
+    const int* compact_bins;
+    double BoxSize;
+    double* power_out;
+    double* keff_out;
+    double* dcdm_out;
+    double* keffphys_out;
+    int active;  // 0: nothing to do
+};
+#ifdef __CUDACC__
+__device__ __forceinline__ void finalize_bin(const FinalizeArgs& f, int c) {
+    const int b = f.compact_bins[c];
+    double p = f.bin_sum[b];
+    p /= *f.F0sq;
+    const double cnt = (double)f.count[b];
+    const double ke = f.ksum[b] / cnt;
+    p /= cnt;
+    if (f.power_out) f.power_out[c] = p;
+    if (f.keff_out) f.keff_out[c] = ke;
+    const double scale = pow(f.BoxSize, -3.0);
+    if (f.dcdm_out) f.dcdm_out[c] = sqrt(p / scale);
+    if (f.keffphys_out) f.keffphys_out[c] = ke * (2 * 3.14159265358979323846 / f.BoxSize);
+}
+#endif
+
 struct CorrTable {
     float* xf;   // log k of node j
     float* rn;   // norm * ratio_j
@@ -457,7 +490,7 @@ void launch_integrator_prepare(const IntegratorDev& I, int Na, double a, double 
 // defer_combine: leave the species sum to launch_finish_update(..., combine = true)
 void launch_integrator_rest(const IntegratorDev& I, int nk, int Na, int nspec, const int* spec_ids,
                             int warps_per_block, cudaStream_t st, int qag_split, int update_row = -1,
-                            bool defer_combine = false);
+                            bool defer_combine = false, const FinalizeArgs* fin = nullptr);
 size_t dnu_qag_smem(int ld, int wpb);
 // end of get_delta_nu_update (delta_tot_table.c:226-248) + interface_common.c:134-146:
 // delta_nu_last, committed row, NaN check, clamp, ratio/log k/kspace_prefac, grid table
