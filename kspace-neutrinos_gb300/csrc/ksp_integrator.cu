@@ -524,15 +524,38 @@ __global__ void __launch_bounds__(SPEC ? 256 : 128, SPEC ? 2 : 4)
     uint64_t* bar = reinterpret_cast<uint64_t*>(sm + off);
     __shared__ double s_task[4];  // m/kT, k/(m/kT), (Nfs-1)/(log a - log a0), integrate? of the current task
     const int tid = threadIdx.x;
-    gk61_fill(N, tid, blockDim.x);
-    for (int i = tid; i < Na; i += blockDim.x) knots[i] = I.scalefact[i];
-    if (tid == 0) mbar_init(bar, 1);
-    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
-    __syncthreads();
     const Background* B = I.B;
     const StepScalars& S = *I.sc;
     const int ntask = nspec * nk;
     const unsigned row_bytes = (unsigned)(((Na + 1) & ~1) * sizeof(double));
+    // Thread 0 starts a task: the copies of its history row and spline coefficients, then
+    // the task's divisions while they land.
+    auto start_task = [&](int task) {
+        const int si = task / nk, ik = task % nk;
+        const int mi = si == 0 ? spec_ids.x : (si == 1 ? spec_ids.y : spec_ids.z);
+        const double mnu = B->mnu_J[mi];
+        const bool integ = !S.skip_integral && Na > 1 && mnu / B->kBtnu > 0;
+        if (integ) {
+            asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+            mbar_expect_tx(bar, Na > 2 ? 2 * row_bytes : row_bytes);
+            bulk_g2s(row, I.dtot + (size_t)ik * I.ld, row_bytes, bar);
+            if (Na > 2) bulk_g2s(rc, I.coef + (size_t)ik * I.ld, row_bytes, bar);
+        }
+        const double m = mnu / B->kBtnu;
+        s_task[0] = m;
+        s_task[1] = I.wavenum[ik] / m;
+        s_task[2] = (S.Nfs - 1.) / (S.loga - S.loga0);
+        s_task[3] = integ ? 1.0 : 0.0;
+    };
+    // the first task's copies are in flight while the block fills its tables
+    if (tid == 0) {
+        mbar_init(bar, 1);
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+        if (blockIdx.x < ntask) start_task(blockIdx.x);
+    }
+    gk61_fill(N, tid, blockDim.x);
+    for (int i = tid; i < Na; i += blockDim.x) knots[i] = I.scalefact[i];
+    __syncthreads();
     unsigned phase = 0;
     int my_max = 0;
     long long my_tot = 0;
@@ -540,26 +563,11 @@ __global__ void __launch_bounds__(SPEC ? 256 : 128, SPEC ? 2 : 4)
         const int si = task / nk, ik = task % nk;
         const int mi = si == 0 ? spec_ids.x : (si == 1 ? spec_ids.y : spec_ids.z);
         const double k = I.wavenum[ik];
-        // thread 0 starts the copies of the history row and its spline coefficients, then
-        // forms the task's divisions while they land (the barrier before also ends the
-        // previous task's reads of row / rc and of these scalars)
-        __syncthreads();
-        if (tid == 0) {
-            const double mnu = B->mnu_J[mi];
-            const bool integ = !S.skip_integral && Na > 1 && mnu / B->kBtnu > 0;
-            if (integ) {
-                asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
-                mbar_expect_tx(bar, Na > 2 ? 2 * row_bytes : row_bytes);
-                bulk_g2s(row, I.dtot + (size_t)ik * I.ld, row_bytes, bar);
-                if (Na > 2) bulk_g2s(rc, I.coef + (size_t)ik * I.ld, row_bytes, bar);
-            }
-            const double m = mnu / B->kBtnu;
-            s_task[0] = m;
-            s_task[1] = k / m;
-            s_task[2] = (S.Nfs - 1.) / (S.loga - S.loga0);
-            s_task[3] = integ ? 1.0 : 0.0;
+        if (task != (int)blockIdx.x) {  // later tasks: after the previous task's reads of row / rc
+            __syncthreads();
+            if (tid == 0) start_task(task);
+            __syncthreads();
         }
-        __syncthreads();
         const double mnubykT = s_task[0];
         double integral = 0;
         const bool integrate = s_task[3] != 0.0;
