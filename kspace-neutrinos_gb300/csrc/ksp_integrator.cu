@@ -9,10 +9,15 @@
 //                               cumulative fixed-order Gauss-Legendre sum over the 16*Na
 //                               uniform nodes replaces 16*Na adaptive integrals; spline
 //                               coefficients by the closed-form inverse of tridiag(1,4,1)
-//   k_dtot_coeffs               natural spline of every history row (shared knots)
+//   k_nc_build                  the integrand's bin-independent terms on QAG's right spine
+//   k_dtot_coeffs               natural spline of every history row (shared knots); in a
+//                               prepared step also the binning pass's normalisation and
+//                               the provisional row
 //   k_dnu_qag                   one warp per (species, bin): history row staged into
 //                               shared memory by a TMA bulk copy, then QAG/GK61 of the
 //                               delta_nu time integral (delta_tot_table.c:492-500,592-599)
+//   k_dnu_qag_blk               the same with a block per task (few tasks), one bisection
+//                               level evaluated ahead
 //   k_combine / k_finish        species sum, row commit, NaN check, clamp, ratio table
 #include <cuda_runtime.h>
 #include <stdio.h>
