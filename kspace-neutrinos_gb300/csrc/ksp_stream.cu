@@ -21,6 +21,10 @@
 // rounds the product to float and sums a run (at most 16 modes) in plain FP32.  Both
 // hand each closed run to the CTA's float-pair totals (compensated atomics) and the
 // CTA totals to the global FP64 sums once.
+//
+// The default binning kernel is k_bin_rows (further down): the same per-mode arithmetic
+// over tiles of whole grid rows moved by 1-D bulk copies, 17-mode runs that never cross
+// a row end, and a copy of the CTA's totals per tile row.
 #include <cuda.h>
 #include <cuda_runtime.h>
 #include <stdint.h>
