@@ -13,8 +13,11 @@ namespace ksp {
 static __device__ const double g_jfit[KSP_JFIT_PIECES * KSP_JFIT_STRIDE] = KSP_JFIT_TABLE_INIT;
 
 __device__ __forceinline__ double specialJ_fit_tab(double x) {
-    if (x <= 0.) return 1.;
+    // x <= 0 tested on the bit pattern (+0 and the negatives are the non-positive
+    // integers; a NaN, whatever its sign, goes on as the FP64 compare would let it), on
+    // the integer pipe: an FP64 compare costs a warp the FP64 pipe's full time
     const long long bits = __double_as_longlong(x);
+    if (bits <= 0 && (bits & 0x7fffffffffffffffLL) <= 0x7ff0000000000000LL) return 1.;
     const int e = (int)((bits >> 52) & 0x7ff) - 1023;
     if (e < KSP_JFIT_E0) {  // x < 2^-20: the x^4.1811 term is below 1e-25 relative
         const double x2 = x * x, x4 = x2 * x2, x8 = x4 * x4;
@@ -33,8 +36,8 @@ __device__ __forceinline__ double specialJ_fit_tab(double x) {
 // J and dJ/dx together (the adjoint): the derivative of the piece's polynomial, times
 // du/dx; outside the table the formula and its derivative.
 __device__ __forceinline__ void specialJ_fit_tab_d(double x, double& J, double& Jd) {
-    if (x <= 0.) { J = 1.; Jd = 0.; return; }
     const long long bits = __double_as_longlong(x);
+    if (bits <= 0 && (bits & 0x7fffffffffffffffLL) <= 0x7ff0000000000000LL) { J = 1.; Jd = 0.; return; }
     const int e = (int)((bits >> 52) & 0x7ff) - 1023;
     if (e < KSP_JFIT_E0 || e >= KSP_JFIT_E1) {
         const double x2 = x * x, x4 = x2 * x2, x8 = x4 * x4;
