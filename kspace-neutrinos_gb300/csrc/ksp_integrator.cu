@@ -730,9 +730,10 @@ void launch_integrator_rest(const IntegratorDev& I, int nk, int Na, int nspec, c
             cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
             if (nsm <= 0) nsm = 1;
         }
-        // few tasks: a block of 8 warps per task with look-ahead (split 8) or of 4 warps
-        // without (split 4); many: a warp per task
-        const int split = qag_split > 0 ? qag_split : (ntask < 4 * nsm ? 8 : 1);
+        // a block per task: 8 warps with look-ahead (split 8) below 4 tasks per SM, 4 warps
+        // without above (measured faster than a warp per task, split 1, up to the 1536
+        // tasks of 3 species x 512 bins)
+        const int split = qag_split > 0 ? qag_split : (ntask < 4 * nsm ? 8 : 4);
         const bool spec = split >= 8;
         const size_t bsmem = dnu_qag_blk_smem(I.ld, spec);
         if (split > 1 && bsmem <= 227 * 1024 - 256) {
