@@ -79,11 +79,19 @@ int kspace_gpu_init_omega_nu(kspace_ctx *ctx, const double MNu[3], double TimeTr
                              double tcmb0);
 /* init_hybrid_nu (omega_nu_single.c:230-240; called from interface_common.c:80-81) */
 int kspace_gpu_init_hybrid_nu(kspace_ctx *ctx, double vcrit, double light, double nu_crit_time);
+/* The fields of a host's _hybrid_nu (omega_nu_single.h:51-64) as they are: enabled,
+ * vcrit as a fraction of light speed, nu_crit_time, nufrac_low[3]. */
+int kspace_gpu_set_hybrid(kspace_ctx *ctx, int enabled, double vcrit_frac, double nu_crit_time,
+                          const double *nufrac_low);
 /* Parameters of the host's hubble_function (gadget_defines.h:11), evaluated on the
  * device as H0 sqrt(Omega_nonu/a^3 + (1-Omega0-OmegaLambda)/a^2 + OmegaLambda +
  * Omega_nu(a) [+ Omega_g/a^4]) (delta_tot_table_test.c:33-45, gadget-2/0003 patch:38). */
 int kspace_gpu_set_hubble(kspace_ctx *ctx, double Omega0, double OmegaLambda, double UnitTime_in_s,
                           int include_radiation);
+/* A host hubble_function of another form: n >= 4 samples H[i] = H(a_i) at log a_i =
+ * loga_lo + i * dloga.  log H is interpolated by a natural cubic spline in log a (the
+ * end segments continue past the table); replaces the form set by kspace_gpu_set_hubble. */
+int kspace_gpu_set_hubble_table(kspace_ctx *ctx, double loga_lo, double dloga, int n, const double *H);
 /* Compare the device H(a) with n samples of the host's hubble_function; returns
  * KSPACE_ERR_HUBBLE if any relative difference exceeds rtol. */
 int kspace_gpu_check_hubble(kspace_ctx *ctx, const double *a, const double *H, int n, double rtol,
@@ -128,6 +136,45 @@ int kspace_gpu_total_powerspectrum(kspace_ctx *ctx, int dims, const void *grid, 
  * sqrt(P_cdm); writes delta_nu[nk]. */
 int kspace_gpu_get_delta_nu_update(kspace_ctx *ctx, double a, int nk, const double *keff, const double *P_cdm_sqrt,
                                    double *delta_nu);
+/* delta_tot_init (delta_tot_table.c:79-149) on its own: wavenum = k (not log k) and
+ * dcdm = sqrt(P_cdm) of nk bins (host or device memory).  Truncates a resumed history
+ * after Time, builds delta_nu_init from the transfer table, the first row on a fresh
+ * start, and delta_nu_last. */
+int kspace_gpu_delta_tot_init(kspace_ctx *ctx, int nk, const double *wavenum, const double *dcdm, double Time);
+/* get_delta_nu (delta_tot_table.c:507-611): delta_nu of one mass state of mass mnu (eV)
+ * at scale factor a from the stored rows [0, ia), at the bins' k = wavenum[nk] (host or
+ * device memory); delta_nu: host memory. */
+int kspace_gpu_get_delta_nu(kspace_ctx *ctx, double a, int nk, const double *wavenum, double *delta_nu, double mnu);
+/* get_delta_nu_combined (delta_tot_table.c:153-172): the species-weighted sum of
+ * get_delta_nu over the non-degenerate mass states, from the stored rows. */
+int kspace_gpu_get_delta_nu_combined(kspace_ctx *ctx, double a, int nk, const double *wavenum, double *delta_nu);
+/* update_delta_tot (delta_tot_table.c:177-191): the last row (overwrite != 0) or a new
+ * row at a, from dcdm = sqrt(P_cdm) and delta_nu of the stored bins. */
+int kspace_gpu_update_delta_tot(kspace_ctx *ctx, double a, const double *dcdm, const double *dnu, int overwrite);
+/* The integrator state in the layout of _delta_tot_table (delta_tot_table.h:17-57): nk,
+ * ia, the init flag, scalefact[ia], rows of the history at stride ld doubles (row ik at
+ * delta_tot + ik * ld, columns [0, ia)), delta_nu_init, delta_nu_last, wavenum (nk each;
+ * NULL = unchanged).  Host memory. */
+int kspace_gpu_set_table(kspace_ctx *ctx, int nk, int ia, int init_done, const double *scalefact,
+                         const double *delta_tot, size_t ld, const double *nu_init, const double *nu_last,
+                         const double *wavenum);
+/* Read it back: columns [col0, ia) of scalefact and of every row, the vectors, nk, ia and
+ * the init flag; any output may be NULL. */
+int kspace_gpu_get_table(kspace_ctx *ctx, int col0, int *nk, int *ia, int *init_done, double *scalefact,
+                         double *delta_tot, size_t ld, double *nu_init, double *nu_last, double *wavenum);
+/* specialJ (delta_tot_table.c:457-463; the fit, or the truncated series when qc > 0) and
+ * nufrac_low (omega_nu_single.c:214-228) of n values on the device; ctx may be NULL (the
+ * current device).  fslength (delta_tot_table.c:394-407) of n intervals with the
+ * context's H(a). */
+int kspace_gpu_special_j(kspace_ctx *ctx, const double *x, int n, double qc, double nufrac_low, double *out);
+int kspace_gpu_nufrac_low(kspace_ctx *ctx, const double *qc, int n, double *out);
+int kspace_gpu_fslength(kspace_ctx *ctx, const double *logai, const double *logaf, int n, double light,
+                        double *out);
+/* omega_nu_single (omega_nu_single.c:262-279), get_omegag (:77-81), and the _omega_nu
+ * fields rhocrit, kBtnu, nu_degeneracies[3] and hybnu.nufrac_low[3] (NULL to skip). */
+int kspace_gpu_omega_nu_single(kspace_ctx *ctx, double a, int i, double *out);
+int kspace_gpu_omega_g(kspace_ctx *ctx, double a, double *out);
+int kspace_gpu_background_info(kspace_ctx *ctx, double *rhocrit, double *kBtnu, int *deg, double *nufrac_low);
 /* compute_neutrino_power_from_cdm (interface_common.c:106-123): outputs the
  * interpolation table of delta_nu/delta_cdm (log k, ratio, norm = kspace_prefac). */
 int kspace_gpu_compute_neutrino_power_from_cdm(kspace_ctx *ctx, double Time, const double *keff_in,
@@ -160,11 +207,16 @@ int kspace_gpu_set_jmass(kspace_ctx *ctx, const double MNu[3]);
  * grid_out may equal grid_in.  store_intervals keeps each QAG subdivision. */
 int kspace_gpu_diff_forward(kspace_ctx *ctx, double Time, double BoxSize, const void *grid_in, void *grid_out,
                             int pmgrid, double *pnu_out, int store_intervals);
+/* The count of successful diff_forward calls on the context (read it right after a
+ * forward and hand it to that forward's diff_backward). */
+int kspace_gpu_diff_generation(kspace_ctx *ctx, long long *generation);
 /* Adjoint of the last diff_forward: from dL/dgrid_out and dL/dP_nu, produce dL/dgrid_in,
  * dL/d(history)[nk][ia] (device) and dL/dm per mass state (host, 3).  recompute = 1
- * re-runs each QAG instead of reading the stored subdivision. */
+ * re-runs each QAG instead of reading the stored subdivision.  generation: the
+ * forward's (kspace_gpu_diff_generation); KSPACE_ERR_ORDER if another forward ran on
+ * the context since, whose state the adjoint would otherwise read. */
 int kspace_gpu_diff_backward(kspace_ctx *ctx, const void *gbar_out, const void *grid_in, const double *pnu_bar,
-                             void *gbar_in, double *Dbar, double *mbar, int recompute);
+                             void *gbar_in, double *Dbar, double *mbar, int recompute, long long generation);
 
 /* ---- batches of independent instances ----
  * No counterpart in the reference, which holds one integrator per process.  A batch

@@ -3,9 +3,9 @@
  *
  * These are the reference's own entry points with the reference's signatures; they are
  * implemented by kspace-neutrinos_gb300/dropin/kspace_dropin.c (compile that file into
- * the host program with the host's <mpi.h> and FFTW2 headers, and link
- * libkspace_gb300.so).  Like the reference, the host supplies hubble_function(),
- * terminate(), message() (gadget_defines.h:11,24-25).
+ * the host program with the host's <mpi.h> and FFTW2 headers, together with
+ * dropin/kspace_delta_tot_table.c, and link libkspace_gb300.so).  Like the reference,
+ * the host supplies hubble_function(), terminate(), message() (gadget_defines.h:11,24-25).
  */
 #ifndef KSPACE_NEUTRINOS_DROPIN_H
 #define KSPACE_NEUTRINOS_DROPIN_H
@@ -21,12 +21,10 @@
 #endif
 #endif
 
+#include "kspace_delta_tot_table.h" /* _delta_pow, get_dnudcdm_powerspec, free_d_pow and the integrator API */
+
 #ifdef __cplusplus
 extern "C" {
-#endif
-
-#ifndef NUSPECIES
-#define NUSPECIES 3
 #endif
 
 /* interface_common.h:12-30 */
@@ -39,18 +37,6 @@ extern struct __kspace_params {
     double vcrit;
     double nu_crit_time;
 } kspace_params;
-
-/* delta_pow.h:17-26: the delta_nu/delta_cdm table returned to the host.  The GSL
- * interpolation objects of the reference are not needed: get_dnudcdm_powerspec
- * interpolates linearly in log k as the reference does. */
-typedef struct _delta_pow {
-    double *logkk;
-    double *delta_ratio;
-    void *spline;
-    void *acc;
-    int nbins;
-    double norm;
-} _delta_pow;
 
 /* ---- interface_common.h ---- */
 double OmegaNu(double a);                                   /* :36 */
@@ -77,17 +63,10 @@ void compute_total_power_spectrum(const double Time, const double BoxSize, fftw_
                                   const int pmgrid, int slabstart_y, int nslab_y, MPI_Comm MYMPI_COMM_WORLD); /* :49 */
 int save_total_power(const double Time, const int snapnum, const char *OutputDir); /* :57 */
 
-/* ---- powerspectrum.h / delta_pow.h ---- */
+/* ---- powerspectrum.h ---- */
 int total_powerspectrum(const int dims, fftw_complex *outfield, const int nrbins, const int startslab,
                         const int nslab, double *power, long long int *count, double *keffs,
                         const MPI_Comm MYMPI_COMM_WORLD);   /* powerspectrum.h:30 */
-double get_dnudcdm_powerspec(_delta_pow *d_pow, double kk); /* delta_pow.h:38 */
-void free_d_pow(_delta_pow *d_pow);                         /* delta_pow.h:41 */
-
-/* Host services, as in gadget_defines.h:11,24-25 (defined by the host). */
-double hubble_function(double a);
-void terminate(int ierr, const char *fmt, ...);
-void message(int ierr, const char *fmt, ...);
 
 #ifdef __cplusplus
 }

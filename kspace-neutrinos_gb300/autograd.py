@@ -12,6 +12,11 @@ the history table an input.  Gradients hold every QAG subdivision fixed and the
 background Omega_nu(a), H(a) fixed; the mass gradient is through the free-streaming
 argument of J.  recompute=True re-runs the integrals in the backward pass instead of
 keeping the subdivisions (the memory-light variant).
+
+One forward per backward on an instance: the adjoint reads state the forward leaves in
+the instance, so a second forward on the same instance before the first one's backward
+makes that backward raise KspaceError (code 10003, KSPACE_ERR_ORDER) instead of
+returning the second step's gradients.  Use one instance per step held for backward.
 """
 import numpy as np
 import torch
@@ -27,9 +32,10 @@ class _Fn(torch.autograd.Function):
         nk = history.shape[0]
         pnu = torch.empty(nk, dtype=torch.float64, device=grid.device)
         torch.cuda.synchronize()
-        inst.diff_forward(Time, BoxSize, grid.detach(), out, N, pnu, store_intervals=not recompute)
+        ctx.generation = inst.diff_forward(Time, BoxSize, grid.detach(), out, N, pnu, store_intervals=not recompute)
         ctx.inst = inst
         ctx.recompute = recompute
+        ctx.mass_device = masses.device
         ctx.hist_shape = tuple(history.shape)
         ctx.save_for_backward(grid)
         return out, pnu
@@ -46,8 +52,10 @@ class _Fn(torch.autograd.Function):
         gin = torch.empty_like(grid)
         Dbar = torch.empty(ctx.hist_shape, dtype=torch.float64, device=grid.device)
         torch.cuda.synchronize()
-        mbar = ctx.inst.diff_backward(gout, grid.detach(), gpnu, gin, Dbar, recompute=ctx.recompute)
-        return gin, Dbar, torch.as_tensor(mbar, dtype=torch.float64), None, None, None, None, None
+        mbar = ctx.inst.diff_backward(gout, grid.detach(), gpnu, gin, Dbar, recompute=ctx.recompute,
+                                      generation=ctx.generation)
+        return (gin, Dbar, torch.as_tensor(mbar, dtype=torch.float64, device=ctx.mass_device), None, None, None,
+                None, None)
 
 
 class NeutrinoStep:

@@ -22,26 +22,9 @@
 #include <stdint.h>
 #include "ksp_internal.h"
 #include "ksp_gridutil.cuh"
+#include "ksp_ptx.cuh"
 
 namespace ksp {
-
-__device__ __forceinline__ uint32_t smem_u32a(const void* p) {
-    return static_cast<uint32_t>(__cvta_generic_to_shared(p));
-}
-__device__ __forceinline__ bool mbar_try_wait_a(uint64_t* bar, unsigned phase) {
-    uint32_t ok;
-    asm volatile(
-        "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}\n"
-        : "=r"(ok)
-        : "r"(smem_u32a(bar)), "r"(phase)
-        : "memory");
-    return ok != 0;
-}
-__device__ __forceinline__ bool mbar_wait_bounded_a(uint64_t* bar, unsigned phase) {
-    for (int it = 0; it < (1 << 22); it++)
-        if (mbar_try_wait_a(bar, phase)) return true;
-    return false;
-}
 
 // d specialJ_fit / dx (derivative of the rational fit of delta_tot_table.c:417-428)
 __device__ __forceinline__ double specialJ_fit_deriv(double x) {
@@ -421,7 +404,7 @@ __global__ void __launch_bounds__(128) k_dnu_adj(IntegratorDev I, DnuAdjArgs A, 
     uint64_t* mybar = bars + warp;
     gk61_fill(N, threadIdx.x, blockDim.x);
     for (int i = threadIdx.x; i < Na; i += blockDim.x) knots[i] = I.scalefact[i];
-    if (lane == 0) asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_u32a(mybar)) : "memory");
+    if (lane == 0) asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(ptx::smem_u32(mybar)) : "memory");
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
     __syncthreads();
     const Background* B = I.B;
@@ -447,27 +430,27 @@ __global__ void __launch_bounds__(128) k_dnu_adj(IntegratorDev I, DnuAdjArgs A, 
             __syncwarp();
             if (lane == 0) {
                 asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
-                asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32a(mybar)),
+                asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(ptx::smem_u32(mybar)),
                              "r"(Na > 2 ? 2 * row_bytes : row_bytes)
                              : "memory");
                 asm volatile(
                     "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
-                        smem_u32a(row)),
-                    "l"(I.dtot + (size_t)ik * I.ld), "r"(row_bytes), "r"(smem_u32a(mybar))
+                        ptx::smem_u32(row)),
+                    "l"(I.dtot + (size_t)ik * I.ld), "r"(row_bytes), "r"(ptx::smem_u32(mybar))
                     : "memory");
                 if (Na > 2)
                     asm volatile(
                         "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
-                            smem_u32a(rc)),
-                        "l"(I.coef + (size_t)ik * I.ld), "r"(row_bytes), "r"(smem_u32a(mybar))
+                            ptx::smem_u32(rc)),
+                        "l"(I.coef + (size_t)ik * I.ld), "r"(row_bytes), "r"(ptx::smem_u32(mybar))
                         : "memory");
             }
             for (int i = lane; i < Na; i += 32) { ybar[i] = 0.0; cbar[i] = 0.0; }
-            const bool got = __all_sync(0xffffffffu, mbar_wait_bounded_a(mybar, phase));  // warp-uniform
+            const bool got = __all_sync(0xffffffffu, ptx::mbar_wait_bounded(mybar, phase));  // warp-uniform
             phase ^= 1;
             if (!got) {
                 if (lane == 0) atomicOr(I.status, kStTimeout);
-                mbar_wait_bounded_a(mybar, phase ^ 1);
+                ptx::mbar_wait_bounded(mybar, phase ^ 1);
                 return;
             }
             const KnotSeg ks{I.knot_invh, I.knot_h3, I.knot_ih3};
@@ -607,7 +590,7 @@ __global__ void __launch_bounds__(128) k_dnu_adj_blk(IntegratorDev I, DnuAdjArgs
     uint64_t* bar = reinterpret_cast<uint64_t*>(sm + off);
     gk61_fill(N, tid, blockDim.x);
     for (int i = tid; i < Na; i += blockDim.x) knots[i] = I.scalefact[i];
-    if (tid == 0) asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_u32a(bar)) : "memory");
+    if (tid == 0) asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(ptx::smem_u32(bar)) : "memory");
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
     __syncthreads();
     const Background* B = I.B;
@@ -633,30 +616,30 @@ __global__ void __launch_bounds__(128) k_dnu_adj_blk(IntegratorDev I, DnuAdjArgs
             __syncthreads();  // the previous task's readers of row / rc / wy / wc are done
             if (tid == 0) {
                 asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
-                asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32a(bar)),
+                asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(ptx::smem_u32(bar)),
                              "r"(Na > 2 ? 2 * row_bytes : row_bytes)
                              : "memory");
                 asm volatile(
                     "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
-                        smem_u32a(row)),
-                    "l"(I.dtot + (size_t)ik * I.ld), "r"(row_bytes), "r"(smem_u32a(bar))
+                        ptx::smem_u32(row)),
+                    "l"(I.dtot + (size_t)ik * I.ld), "r"(row_bytes), "r"(ptx::smem_u32(bar))
                     : "memory");
                 if (Na > 2)
                     asm volatile(
                         "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
-                            smem_u32a(rc)),
-                        "l"(I.coef + (size_t)ik * I.ld), "r"(row_bytes), "r"(smem_u32a(bar))
+                            ptx::smem_u32(rc)),
+                        "l"(I.coef + (size_t)ik * I.ld), "r"(row_bytes), "r"(ptx::smem_u32(bar))
                         : "memory");
             }
             for (int i = tid; i < nw * I.ld; i += blockDim.x) {
                 wy[i] = 0.0;
                 wc[i] = 0.0;
             }
-            const bool got = __syncthreads_and(mbar_wait_bounded_a(bar, phase));  // block-uniform
+            const bool got = __syncthreads_and(ptx::mbar_wait_bounded(bar, phase));  // block-uniform
             phase ^= 1;
             if (!got) {
                 if (tid == 0) atomicOr(I.status, kStTimeout);
-                mbar_wait_bounded_a(bar, phase ^ 1);
+                ptx::mbar_wait_bounded(bar, phase ^ 1);
                 return;
             }
             const KnotSeg ks{I.knot_invh, I.knot_h3, I.knot_ih3};

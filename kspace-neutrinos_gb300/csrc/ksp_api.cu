@@ -176,6 +176,7 @@ extern "C" int kspace_gpu_destroy(kspace_ctx* c) {
         cudaFree(g.compact_d);
     }
     if (c->stage_d) cudaFree(c->stage_d);
+    if (c->htab_dev) cudaFree(c->htab_dev);
     if (c->dB) cudaFree(c->dB);
     if (c->status_d) cudaFree(c->status_d);
     if (c->status_h) cudaFreeHost(c->status_h);
@@ -325,16 +326,67 @@ extern "C" int kspace_gpu_init_hybrid_nu(kspace_ctx* c, double vcrit, double lig
     return KSPACE_OK;
 }
 
+// The hybrid-neutrino parameters as a host's _hybrid_nu holds them (omega_nu_single.h:51-64):
+// vcrit as a fraction of light speed, the switch-on time and the particle fractions.
+extern "C" int kspace_gpu_set_hybrid(kspace_ctx* c, int enabled, double vcrit_frac, double nu_crit_time,
+                                     const double* nufrac_low) {
+    NEED(c && nufrac_low, KSPACE_ERR_ARG);
+    NEED(c->bg_ready, KSPACE_ERR_ORDER);
+    Background& B = c->hB;
+    B.hyb_enabled = enabled ? 1 : 0;
+    B.vcrit = vcrit_frac;
+    B.nu_crit_time = nu_crit_time;
+    for (int i = 0; i < kNuSpecies; i++) B.nufrac_low[i] = nufrac_low[i];
+    upload_background(c);
+    CK(cudaStreamSynchronize(c->stream));
+    return KSPACE_OK;
+}
+
 extern "C" int kspace_gpu_set_hubble(kspace_ctx* c, double Omega0, double OmegaLambda, double UnitTime_in_s,
                                      int radiation) {
     NEED(c, KSPACE_ERR_ARG);
     NEED(c->bg_ready, KSPACE_ERR_ORDER);
     Background& B = c->hB;
+    B.htab_n = 0;  // the analytic form
     B.Omega_nonu_H = Omega0 - omega_nu(B, 1);
     B.OmegaLambda = OmegaLambda;
     B.OmegaK = 1.0 - Omega0 - OmegaLambda;
     B.hubble = kHubble * UnitTime_in_s;
     B.radiation = radiation;
+    upload_background(c);
+    CK(cudaStreamSynchronize(c->stream));
+    c->hubble_ready = true;
+    return KSPACE_OK;
+}
+
+// A host H(a) of any form: n >= 4 samples H[i] = H(exp(loga_lo + i * dloga)); log H is
+// interpolated by a natural cubic spline in log a (built on the device), continued by
+// the end segments outside the table.
+extern "C" int kspace_gpu_set_hubble_table(kspace_ctx* c, double loga_lo, double dloga, int n, const double* H) {
+    NEED(c && H && n >= 4 && dloga > 0, KSPACE_ERR_ARG);
+    NEED(c->bg_ready, KSPACE_ERR_ORDER);
+    for (int i = 0; i < n; i++) NEED(H[i] > 0 && isfinite(H[i]), KSPACE_ERR_ARG);
+    CK(cudaSetDevice(c->device));
+    CK(cudaStreamSynchronize(c->stream));
+    if (c->htab_dev) cudaFree(c->htab_dev);
+    c->htab_dev = nullptr;
+    CK(dalloc(&c->htab_dev, 4 * (size_t)n));  // 4 coefficients per segment (n - 1 segments)
+    double* scratch = nullptr;
+    CK(dalloc(&scratch, 2 * (size_t)n));
+    CK(cudaMemcpyAsync(scratch, H, sizeof(double) * n, cudaMemcpyHostToDevice, c->stream));
+    launch_hubble_table(scratch, n, dloga, c->htab_dev, scratch + n, c->stream);
+    g_launches += 1;
+    c->htab_host.assign(4 * (size_t)n, 0.0);
+    CK(cudaMemcpyAsync(c->htab_host.data(), c->htab_dev, sizeof(double) * 4 * (n - 1), cudaMemcpyDeviceToHost,
+                       c->stream));
+    CK(cudaStreamSynchronize(c->stream));
+    cudaFree(scratch);
+    Background& B = c->hB;
+    B.htab_d = c->htab_dev;
+    B.htab_h = c->htab_host.data();
+    B.htab_n = n;
+    B.htab_lo = loga_lo;
+    B.htab_dx = dloga;
     upload_background(c);
     CK(cudaStreamSynchronize(c->stream));
     c->hubble_ready = true;
@@ -746,6 +798,7 @@ static int update_device(kspace_ctx* c, double a, int nk_in, const double* keff_
     c->h_scalefact[c->ia] = loga;
     c->ia++;
     const int Na = c->ia;
+    I.kq = keff_d;  // the integrals at this call's k (delta_tot_table.c:224)
     if (prepared) {
         CK(cudaStreamWaitEvent(c->stream, c->ev_join, 0));
         launch_integrator_rest(I, c->nk, Na, c->nspec, c->spec_ids, c->qag_warps, c->stream, c->qag_split, prov_row,
@@ -754,6 +807,7 @@ static int update_device(kspace_ctx* c, double a, int nk_in, const double* keff_
         launch_delta_nu_combined(I, c->nk, Na, a, loga, c->loga0, c->TimeTransfer, c->fact_valid, c->nspec,
                                  c->spec_ids, c->qag_warps, c->stream, c->qag_split);
     }
+    I.kq = nullptr;
     c->prep_valid = false;
     // keep the row if far enough from the previous one (delta_tot_table.c:229-237)
     const bool commit = a >= exp(c->h_scalefact[Na - 2]) + 0.009;
@@ -782,6 +836,254 @@ extern "C" int kspace_gpu_get_delta_nu_update(kspace_ctx* c, double a, int nk, c
     int st = update_device(c, a, nk, kd, dd, c->dnu_out_d, false);
     if (st) return st;
     CK(cudaMemcpy(delta_nu, c->dnu_out_d, sizeof(double) * nk, cudaMemcpyDeviceToHost));
+    return KSPACE_OK;
+}
+
+// delta_tot_init (delta_tot_table.c:79-149) on its own: wavenum = k (not log k) and
+// dcdm = sqrt(P_cdm) of the nk bins, host or device memory.
+extern "C" int kspace_gpu_delta_tot_init(kspace_ctx* c, int nk, const double* wavenum, const double* dcdm,
+                                         double Time) {
+    NEED(c && wavenum && dcdm && nk > 0, KSPACE_ERR_ARG);
+    NEED(c->table_ready, KSPACE_ERR_ORDER);
+    NEED(nk <= c->I.nk_alloc, KSPACE_ERR_NK_ALLOC);
+    CK(cudaSetDevice(c->device));
+    double* kd = c->io_d;
+    CK(cudaMemcpyAsync(kd, wavenum, sizeof(double) * nk, cudaMemcpyDefault, c->stream));
+    CK(cudaMemcpyAsync(c->I.dcdm, dcdm, sizeof(double) * nk, cudaMemcpyDefault, c->stream));
+    return delta_tot_init(c, nk, kd, c->I.dcdm, Time);
+}
+
+// The integrals of get_delta_nu over the stored rows [0, ia) at scale factor a and the
+// call's k (host or device): nspec mass states spec_ids, species sum into I.dnu.
+static int integrate_stored(kspace_ctx* c, double a, int nk, const double* wavenum, int nspec, const int* spec_ids) {
+    NEED(c->table_ready && c->hubble_ready, KSPACE_ERR_ORDER);
+    NEED(c->transfer_ready || c->init_done || c->ia > 0, KSPACE_ERR_ORDER);
+    NEED(nk > 0 && nk <= c->I.nk_alloc, KSPACE_ERR_NK_ALLOC);
+    NEED(c->ia >= 1, KSPACE_ERR_ORDER);
+    CK(cudaSetDevice(c->device));
+    IntegratorDev& I = c->I;
+    double* kd = c->io_d + 2 * (size_t)I.nk_alloc;
+    CK(cudaMemcpyAsync(kd, wavenum, sizeof(double) * nk, cudaMemcpyDefault, c->stream));
+    CK(cudaMemsetAsync(I.qag_max, 0, sizeof(int), c->stream));
+    CK(cudaMemsetAsync(I.qag_total, 0, sizeof(long long), c->stream));
+    I.kq = kd;
+    // the knot factorisation is rebuilt from the first row: rows may have changed since
+    launch_delta_nu_combined(I, nk, c->ia, a, log(a), c->loga0, c->TimeTransfer, 0, nspec, spec_ids, c->qag_warps,
+                             c->stream, c->qag_split);
+    I.kq = nullptr;
+    g_launches += 8;
+    c->fact_valid = 0;
+    return KSPACE_OK;
+}
+
+// get_delta_nu (delta_tot_table.c:507-611): delta_nu of one mass state of mass mnu (eV)
+// from the stored rows.
+extern "C" int kspace_gpu_get_delta_nu(kspace_ctx* c, double a, int nk, const double* wavenum, double* delta_nu,
+                                       double mnu) {
+    NEED(c && wavenum && delta_nu, KSPACE_ERR_ARG);
+    NEED(c->bg_ready, KSPACE_ERR_ORDER);
+    // the mass enters only through m/kT in J's argument: species slot 0 carries it
+    Background& B = c->hB;
+    const double keep = B.mnu_J[0];
+    B.mnu_J[0] = mnu;
+    CK(cudaMemcpyAsync(&c->dB->mnu_J[0], &B.mnu_J[0], sizeof(double), cudaMemcpyHostToDevice, c->stream));
+    const int ids[3] = {0, 0, 0};
+    int st = integrate_stored(c, a, nk, wavenum, 1, ids);
+    B.mnu_J[0] = keep;
+    if (!st)
+        CK(cudaMemcpyAsync(delta_nu, c->I.dnu_s, sizeof(double) * nk, cudaMemcpyDeviceToHost, c->stream));
+    CK(cudaMemcpyAsync(&c->dB->mnu_J[0], &B.mnu_J[0], sizeof(double), cudaMemcpyHostToDevice, c->stream));
+    const int st2 = sync_status(c);
+    return st ? st : st2;
+}
+
+// get_delta_nu_combined (delta_tot_table.c:153-172) from the stored rows.
+extern "C" int kspace_gpu_get_delta_nu_combined(kspace_ctx* c, double a, int nk, const double* wavenum,
+                                                double* delta_nu) {
+    NEED(c && wavenum && delta_nu, KSPACE_ERR_ARG);
+    int st = integrate_stored(c, a, nk, wavenum, c->nspec, c->spec_ids);
+    if (st) return st;
+    CK(cudaMemcpyAsync(delta_nu, c->I.dnu, sizeof(double) * nk, cudaMemcpyDeviceToHost, c->stream));
+    return sync_status(c);
+}
+
+// update_delta_tot (delta_tot_table.c:177-191): row ia-1 (overwrite) or a new row ia from
+// dcdm = sqrt(P_cdm) and delta_nu of the nk stored bins (host or device memory).
+extern "C" int kspace_gpu_update_delta_tot(kspace_ctx* c, double a, const double* dcdm, const double* dnu,
+                                           int overwrite) {
+    NEED(c && dcdm && dnu, KSPACE_ERR_ARG);
+    NEED(c->table_ready, KSPACE_ERR_ORDER);
+    NEED(overwrite ? c->ia >= 1 : c->ia < c->I.namax, overwrite ? KSPACE_ERR_ORDER : KSPACE_ERR_NAMAX);
+    CK(cudaSetDevice(c->device));
+    const int nk = c->nk;
+    double* dc = c->io_d;
+    double* dn = c->io_d + c->I.nk_alloc;
+    if (nk > 0) {
+        CK(cudaMemcpyAsync(dc, dcdm, sizeof(double) * nk, cudaMemcpyDefault, c->stream));
+        CK(cudaMemcpyAsync(dn, dnu, sizeof(double) * nk, cudaMemcpyDefault, c->stream));
+    }
+    if (!overwrite) c->ia++;
+    const int row = c->ia - 1;
+    c->h_scalefact[row] = log(a);
+    launch_update_row(c->I, nk, row, a, c->h_scalefact[row], dc, dn, c->stream);
+    g_launches += 1;
+    c->fact_valid = 0;
+    return sync_status(c);
+}
+
+// The whole integrator state in the reference's layout (delta_tot_table.h:17-57):
+// scalefact[ia], delta_tot rows of stride ld (row ik at delta_tot + ik * ld), the three
+// per-bin vectors (nk each), and the init flag.  Host memory.
+extern "C" int kspace_gpu_set_table(kspace_ctx* c, int nk, int ia, int init_done, const double* scalefact,
+                                    const double* delta_tot, size_t ld, const double* nu_init,
+                                    const double* nu_last, const double* wavenum) {
+    NEED(c && nk >= 0 && ia >= 0, KSPACE_ERR_ARG);
+    NEED(c->table_ready, KSPACE_ERR_ORDER);
+    IntegratorDev& I = c->I;
+    NEED(nk <= I.nk_alloc && ia <= I.namax, KSPACE_ERR_NK_ALLOC);
+    NEED(ia == 0 || (scalefact && delta_tot && ld >= (size_t)ia), KSPACE_ERR_ARG);
+    CK(cudaSetDevice(c->device));
+    c->nk = nk;
+    c->ia = ia;
+    for (int i = 0; i < ia; i++) c->h_scalefact[i] = scalefact[i];
+    if (ia > 0) {
+        CK(cudaMemcpyAsync(I.scalefact, scalefact, sizeof(double) * ia, cudaMemcpyHostToDevice, c->stream));
+        if (nk > 0)
+            CK(cudaMemcpy2DAsync(I.dtot, sizeof(double) * I.ld, delta_tot, sizeof(double) * ld, sizeof(double) * ia,
+                                 nk, cudaMemcpyHostToDevice, c->stream));
+    }
+    if (nk > 0) {
+        if (nu_init) CK(cudaMemcpyAsync(I.nu_init, nu_init, sizeof(double) * nk, cudaMemcpyHostToDevice, c->stream));
+        if (nu_last) CK(cudaMemcpyAsync(I.nu_last, nu_last, sizeof(double) * nk, cudaMemcpyHostToDevice, c->stream));
+        if (wavenum) CK(cudaMemcpyAsync(I.wavenum, wavenum, sizeof(double) * nk, cudaMemcpyHostToDevice, c->stream));
+    }
+    c->init_done = init_done ? 1 : 0;
+    c->fact_valid = 0;
+    c->prep_valid = false;
+    CK(cudaStreamSynchronize(c->stream));
+    return KSPACE_OK;
+}
+
+// Read the state back: columns [col0, ia) of scalefact and of every row (so a caller that
+// holds the earlier columns copies only what a call may have changed), the vectors, nk,
+// ia and the init flag.  Any output may be NULL.
+extern "C" int kspace_gpu_get_table(kspace_ctx* c, int col0, int* nk, int* ia, int* init_done, double* scalefact,
+                                    double* delta_tot, size_t ld, double* nu_init, double* nu_last,
+                                    double* wavenum) {
+    NEED(c && col0 >= 0, KSPACE_ERR_ARG);
+    NEED(c->table_ready, KSPACE_ERR_ORDER);
+    CK(cudaSetDevice(c->device));
+    CK(cudaStreamSynchronize(c->stream));
+    const IntegratorDev& I = c->I;
+    if (nk) *nk = c->nk;
+    if (ia) *ia = c->ia;
+    if (init_done) *init_done = c->init_done;
+    if (scalefact)
+        for (int i = col0; i < c->ia; i++) scalefact[i] = c->h_scalefact[i];
+    if (delta_tot && c->ia > col0 && c->nk > 0) {
+        NEED(ld >= (size_t)c->ia, KSPACE_ERR_ARG);
+        CK(cudaMemcpy2D(delta_tot + col0, sizeof(double) * ld, I.dtot + col0, sizeof(double) * I.ld,
+                        sizeof(double) * (c->ia - col0), c->nk, cudaMemcpyDeviceToHost));
+    }
+    if (c->nk > 0) {
+        if (nu_init) CK(cudaMemcpy(nu_init, I.nu_init, sizeof(double) * c->nk, cudaMemcpyDeviceToHost));
+        if (nu_last) CK(cudaMemcpy(nu_last, I.nu_last, sizeof(double) * c->nk, cudaMemcpyDeviceToHost));
+        if (wavenum) CK(cudaMemcpy(wavenum, I.wavenum, sizeof(double) * c->nk, cudaMemcpyDeviceToHost));
+    }
+    return KSPACE_OK;
+}
+
+// ------------------------------------------------------------------ scalar functions on the device
+// specialJ, nufrac_low and fslength of n arguments at once, computed by the same device
+// functions the integrator uses.  ctx may be NULL for the first two (current device,
+// default stream); fslength needs the context's H(a).
+template <class F>
+static int device_values(kspace_ctx* c, int nin, const double* in0, const double* in1, int n, double* out, F launch) {
+    NEED(n >= 0 && out, KSPACE_ERR_ARG);
+    if (n == 0) return KSPACE_OK;
+    if (c) CK(cudaSetDevice(c->device));
+    cudaStream_t st = c ? c->stream : 0;
+    double* buf = nullptr;
+    unsigned* status = nullptr;
+    CK(cudaMalloc(&buf, sizeof(double) * (size_t)n * (nin + 1)));
+    if (cudaMalloc(&status, sizeof(unsigned)) != cudaSuccess) {
+        cudaFree(buf);
+        return KSPACE_ERR_CUDA;
+    }
+    cudaError_t e = cudaMemsetAsync(status, 0, sizeof(unsigned), st);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(buf, in0, sizeof(double) * n, cudaMemcpyDefault, st);
+    if (e == cudaSuccess && nin > 1) e = cudaMemcpyAsync(buf + n, in1, sizeof(double) * n, cudaMemcpyDefault, st);
+    if (e == cudaSuccess) {
+        launch(buf, buf + n, buf + (size_t)nin * n, status, st);
+        g_launches += 1;
+        e = cudaGetLastError();
+    }
+    unsigned s = 0;
+    if (e == cudaSuccess) e = cudaMemcpyAsync(out, buf + (size_t)nin * n, sizeof(double) * n, cudaMemcpyDefault, st);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(&s, status, sizeof(unsigned), cudaMemcpyDeviceToHost, st);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+    cudaFree(buf);
+    cudaFree(status);
+    if (e != cudaSuccess) {
+        fprintf(stderr, "kspace_gpu: CUDA error %s\n", cudaGetErrorString(e));
+        return KSPACE_ERR_CUDA;
+    }
+    return map_status(s);
+}
+
+extern "C" int kspace_gpu_special_j(kspace_ctx* c, const double* x, int n, double qc, double nufrac_low, double* out) {
+    NEED(x, KSPACE_ERR_ARG);
+    return device_values(c, 1, x, nullptr, n, out,
+                         [&](const double* a, const double*, double* o, unsigned*, cudaStream_t st) {
+                             launch_special_j(a, n, qc, nufrac_low, o, st);
+                         });
+}
+
+extern "C" int kspace_gpu_nufrac_low(kspace_ctx* c, const double* qc, int n, double* out) {
+    NEED(qc, KSPACE_ERR_ARG);
+    return device_values(c, 1, qc, nullptr, n, out,
+                         [&](const double* a, const double*, double* o, unsigned* status, cudaStream_t st) {
+                             launch_nufrac_low_values(a, n, o, status, st);
+                         });
+}
+
+extern "C" int kspace_gpu_fslength(kspace_ctx* c, const double* logai, const double* logaf, int n, double light,
+                                   double* out) {
+    NEED(c && logai && logaf, KSPACE_ERR_ARG);
+    NEED(c->hubble_ready, KSPACE_ERR_ORDER);
+    const Background* dB = c->dB;
+    return device_values(c, 2, logai, logaf, n, out,
+                         [&](const double* a, const double* b, double* o, unsigned*, cudaStream_t st) {
+                             launch_fslength_values(dB, a, b, n, light, o, st);
+                         });
+}
+
+// omega_nu_single (omega_nu_single.c:262-279), get_omegag (:77-81) and the fields of
+// _omega_nu a host mirror needs (rhocrit, kBtnu, degeneracies, nufrac_low).
+extern "C" int kspace_gpu_omega_nu_single(kspace_ctx* c, double a, int i, double* out) {
+    NEED(c && out && i >= 0 && i < kNuSpecies, KSPACE_ERR_ARG);
+    NEED(c->bg_ready, KSPACE_ERR_ORDER);
+    *out = omega_nu_single(c->hB, a, i);
+    return KSPACE_OK;
+}
+
+extern "C" int kspace_gpu_omega_g(kspace_ctx* c, double a, double* out) {
+    NEED(c && out, KSPACE_ERR_ARG);
+    NEED(c->bg_ready, KSPACE_ERR_ORDER);
+    *out = c->hB.omegag0 / pow(a, 4);  // omega_nu_single.c:77-81
+    return KSPACE_OK;
+}
+
+extern "C" int kspace_gpu_background_info(kspace_ctx* c, double* rhocrit, double* kBtnu, int* deg,
+                                          double* nufrac_low) {
+    NEED(c, KSPACE_ERR_ARG);
+    NEED(c->bg_ready, KSPACE_ERR_ORDER);
+    if (rhocrit) *rhocrit = c->hB.rhocrit;
+    if (kBtnu) *kBtnu = c->hB.kBtnu;
+    for (int i = 0; i < kNuSpecies; i++) {
+        if (deg) deg[i] = c->hB.deg[i];
+        if (nufrac_low) nufrac_low[i] = c->hB.nufrac_low[i];
+    }
     return KSPACE_OK;
 }
 
@@ -1175,12 +1477,23 @@ extern "C" int kspace_gpu_compute_neutrino_power_from_cdm(kspace_ctx* c, double 
 }
 
 // compute_total_power_spectrum (interface_gadget.c:114-144): binning into pmgrid/2 bins
-// for runs without the integrator; saved by kspace_gpu_save_total_power.
+// for runs without the integrator (gadget-2 patch 0004 calls it without InitOmegaNu or
+// allocate_kspace_memory: a context with neither gets bin buffers of its own); saved
+// by kspace_gpu_save_total_power.
 extern "C" int kspace_gpu_compute_total_power_spectrum(kspace_ctx* c, double Time, double BoxSize, const void* grid,
                                                        int pmgrid, int slab0, int nslab) {
     (void)Time;
-    NEED(c && grid, KSPACE_ERR_ARG);
-    NEED(c->table_ready, KSPACE_ERR_ORDER);
+    NEED(c && grid && pmgrid > 1, KSPACE_ERR_ARG);
+    if (!c->table_ready) {
+        // buffers only: a background without neutrinos and a table of pmgrid/2 bins
+        int st = KSPACE_OK;
+        if (!c->bg_ready) {
+            const double zero[3] = {0, 0, 0};
+            st = kspace_gpu_init_omega_nu(c, zero, 0.01, 0.7, 2.7255);
+        }
+        if (!st) st = kspace_gpu_alloc_table(c, pmgrid / 2, 0.01, 1.0, 0.3, 1.0, 1.0);
+        if (st) return st;
+    }
     const int nrbins = pmgrid / 2;
     NEED(nrbins <= c->buf_nb, KSPACE_ERR_NK_ALLOC);
     Geo* G = nullptr;
@@ -1232,9 +1545,18 @@ extern "C" int kspace_gpu_save_total_power(kspace_ctx* c, double Time, int snapn
     fprintf(fd, "# a = %g\n", Time);
     fprintf(fd, "# nbins = %d\n", n);
     for (int i = 0; i < n; i++) {
-        const double d_tot = c->init_done ? get_delta_tot(last[i], dcdm[i], OmegaNua3, Omeganonu, OmegaNu1, partnu)
-                                          : dcdm[i];
-        fprintf(fd, "%g %g\n", keff[i], d_tot * d_tot);
+        if (c->init_done) {
+            // a neutrino run (the library built with KSPACE_NEUTRINOS_2, interface_gadget.c:215-216)
+            const double d_tot = get_delta_tot(last[i], dcdm[i], OmegaNua3, Omeganonu, OmegaNu1, partnu);
+            fprintf(fd, "%g %g\n", keff[i], d_tot * d_tot);
+        } else {
+            // without the integrator (interface_gadget.c:218): the k column is what the
+            // reference writes, exp(log(delta_cdm * 2 pi / BoxSize)): there its keff and
+            // delta_cdm_last share storage (3/2*pmgrid == pmgrid in integer arithmetic,
+            // :118-119), so the stored log k is overwritten with log(delta_cdm 2 pi / L)
+            const double kq = exp(log(dcdm[i] * 2 * kPi / c->last_BoxSize));
+            fprintf(fd, "%g %g\n", kq, dcdm[i] * dcdm[i]);
+        }
     }
     fclose(fd);
     return 0;
@@ -1383,12 +1705,24 @@ extern "C" int kspace_gpu_diff_forward(kspace_ctx* c, double Time, double BoxSiz
     c->diff_box = BoxSize;
     c->diff_store = store_intervals;
     c->diff_pmgrid = pmgrid;
+    c->diff_gen++;
     c->last_nk = c->nk;
     c->last_BoxSize = BoxSize;
     return KSPACE_OK;
 }
 
-// Adjoint of the last kspace_gpu_diff_forward (no other call in between).
+// The number of successful diff_forward calls on the context so far: the generation a
+// diff_backward must name.
+extern "C" int kspace_gpu_diff_generation(kspace_ctx* c, long long* generation) {
+    NEED(c && generation, KSPACE_ERR_ARG);
+    *generation = c->diff_gen;
+    return KSPACE_OK;
+}
+
+// Adjoint of the last kspace_gpu_diff_forward (no other call in between).  generation:
+// the value kspace_gpu_diff_generation gave right after that forward; a later forward
+// on the same context replaces the state the adjoint reads, and the call is refused
+// (KSPACE_ERR_ORDER) instead of returning the later step's gradients.
 //   gbar_out: dL/d grid_out (device c64), grid_in: the forward's input (device),
 //   pnu_bar: dL/dP_nu (device, nk), gbar_in: out dL/d grid_in (device c64),
 //   Dbar: out dL/d history (device, [nk][ia] of the current table), mbar: out
@@ -1396,9 +1730,9 @@ extern "C" int kspace_gpu_diff_forward(kspace_ctx* c, double Time, double BoxSiz
 //   recompute: 1 = re-run every QAG instead of reading the stored subdivisions.
 extern "C" int kspace_gpu_diff_backward(kspace_ctx* c, const void* gbar_out, const void* grid_in,
                                         const double* pnu_bar, void* gbar_in, double* Dbar, double* mbar,
-                                        int recompute) {
+                                        int recompute, long long generation) {
     NEED(c && gbar_out && grid_in && pnu_bar && gbar_in, KSPACE_ERR_ARG);
-    NEED(c->diff_ready, KSPACE_ERR_ORDER);
+    NEED(c->diff_ready && generation == c->diff_gen, KSPACE_ERR_ORDER);
     NEED(recompute || c->diff_store, KSPACE_ERR_ORDER);
     Geo* G = nullptr;
     int st = get_geo(c, c->diff_pmgrid, c->I.nk_alloc, &G);

@@ -42,6 +42,9 @@ struct kspace_ctx {
     Background* dB = nullptr;
     double MNu[3] = {0, 0, 0};
     double bg_a0 = 0.01;
+    // a tabulated host H(a) (Background::htab_*): device coefficients and their host copy
+    double* htab_dev = nullptr;
+    std::vector<double> htab_host;
     int nspec = 0, spec_ids[3] = {0, 0, 0};
     // integrator table
     bool table_ready = false;
@@ -74,6 +77,7 @@ struct kspace_ctx {
     int adj_cap_nb = 0;
     bool diff_ready = false;
     int diff_ia = 0, diff_Na = 0, diff_nk = 0, diff_store = 0;
+    long long diff_gen = 0;  // counts successful diff_forward calls
     double diff_time = 0, diff_box = 0;
     int diff_pmgrid = 0;
     // the delta_cdm-independent integrator work of a step, run on a side stream while the

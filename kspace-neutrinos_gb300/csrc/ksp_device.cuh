@@ -64,6 +64,14 @@ struct Background {
     double Omega_nonu_H, OmegaLambda, OmegaK, hubble;
     int radiation;
     RhoTable tab[kNuSpecies];
+    // A host H(a) of another form, tabulated: log H as a natural cubic spline in log a on
+    // htab_n uniform knots from htab_lo with spacing htab_h, 4 coefficients per segment
+    // (device copy for kernels, host copy for host-side evaluation); htab_n = 0: the
+    // analytic form above.
+    const double* htab_d;
+    const double* htab_h;
+    int htab_n;
+    double htab_lo, htab_dx;
 };
 
 // ------------------------------------------------------------------ splines
@@ -193,9 +201,24 @@ KSP_HD double omega_nu_single(const Background& B, double a, int i) {
     return om - part;
 }
 
+// log H at log a from the tabulated spline (the end segments continue past the table)
+KSP_HD double hubble_tab_log(const Background& B, double la) {
+#ifdef __CUDA_ARCH__
+    const double* t = B.htab_d;
+#else
+    const double* t = B.htab_h;
+#endif
+    int i = (int)floor((la - B.htab_lo) / B.htab_dx);
+    i = i < 0 ? 0 : (i > B.htab_n - 2 ? B.htab_n - 2 : i);
+    const double dx = la - (B.htab_lo + i * B.htab_dx);
+    const double* c = t + 4 * i;
+    return c[0] + dx * (c[1] + dx * (c[2] + dx * c[3]));
+}
+
 // delta_tot_table_test.c:33-45 (+ curvature, gadget-2/0003 patch:38); Omega_g as
 // omega_nu_single.c:77-81.
 KSP_HD double hubble(const Background& B, double a, double loga = NAN) {
+    if (B.htab_n > 0) return exp(hubble_tab_log(B, loga == loga ? loga : log(a)));
     const double a3 = a * a * a;
     double om = B.Omega_nonu_H / a3 + B.OmegaLambda;
     if (B.OmegaK != 0.0) om += B.OmegaK / (a * a);
@@ -239,6 +262,7 @@ __device__ __forceinline__ double rho_nu_ia(const RhoTable& T, double a, double 
 // The fslength integrand 1/(a^2 H(a)) at a = e^x (delta_tot_table.c:378-383) with H as
 // hubble() forms it, 1/a computed once (one exp, one sqrt, two divisions per node).
 __device__ __forceinline__ double fsl_integrand(const Background& B, double x) {
+    if (B.htab_n > 0) return exp(-2.0 * x - hubble_tab_log(B, x));
     const double a = exp(x);
     const double ia = 1.0 / a;
     const double ia2 = ia * ia, ia3 = ia2 * ia;

@@ -16,51 +16,9 @@
 #include <stdint.h>
 #include "ksp_internal.h"
 #include "ksp_gridutil.cuh"
+#include "ksp_ptx.cuh"
 
 namespace ksp {
-
-// ------------------------------------------------------------------ helpers
-__device__ __forceinline__ uint32_t smem_addr(const void* p) {
-    return static_cast<uint32_t>(__cvta_generic_to_shared(p));
-}
-__device__ __forceinline__ void mbar_init_(uint64_t* bar, unsigned count) {
-    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_addr(bar)), "r"(count) : "memory");
-}
-__device__ __forceinline__ void mbar_expect_tx_(uint64_t* bar, unsigned bytes) {
-    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_addr(bar)), "r"(bytes)
-                 : "memory");
-}
-__device__ __forceinline__ bool mbar_try_wait_(uint64_t* bar, unsigned phase) {
-    uint32_t ok;
-    asm volatile(
-        "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}\n"
-        : "=r"(ok)
-        : "r"(smem_addr(bar)), "r"(phase)
-        : "memory");
-    return ok != 0;
-}
-__device__ __forceinline__ bool mbar_wait_bounded_(uint64_t* bar, unsigned phase) {
-    for (int it = 0; it < (1 << 22); it++)
-        if (mbar_try_wait_(bar, phase)) return true;
-    return false;
-}
-__device__ __forceinline__ void tma_load_2d(void* dst, const CUtensorMap* map, uint64_t* bar, int x, int y) {
-    asm volatile(
-        "cp.async.bulk.tensor.2d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%3, %4}], [%2];" ::
-            "r"(smem_addr(dst)),
-        "l"(reinterpret_cast<uint64_t>(map)), "r"(smem_addr(bar)), "r"(x), "r"(y)
-        : "memory");
-}
-__device__ __forceinline__ void tma_store_2d(const CUtensorMap* map, const void* src, int x, int y) {
-    asm volatile("cp.async.bulk.tensor.2d.global.shared::cta.bulk_group [%0, {%2, %3}], [%1];" ::"l"(
-                     reinterpret_cast<uint64_t>(map)),
-                 "r"(smem_addr(src)), "r"(x), "r"(y)
-                 : "memory");
-}
-__device__ __forceinline__ void bulk_commit() { asm volatile("cp.async.bulk.commit_group;" ::: "memory"); }
-__device__ __forceinline__ void bulk_wait_read_le1() { asm volatile("cp.async.bulk.wait_group.read 1;" ::: "memory"); }
-__device__ __forceinline__ void bulk_wait_all() { asm volatile("cp.async.bulk.wait_group 0;" ::: "memory"); }
-__device__ __forceinline__ void fence_async_smem() { asm volatile("fence.proxy.async.shared::cta;" ::: "memory"); }
 
 // ------------------------------------------------------------------ shared-memory layout
 struct SmemPlan {
@@ -101,7 +59,7 @@ k_bin_power_tma(const __grid_constant__ CUtensorMap tmap, GridArgs g, const int*
     __shared__ long long s_rowbase;
     __shared__ int s_zbase;
     const SmemPlan P = plan_smem(ROWS, STAGES, g.nrbins, 2 * g.nz, NW);
-    const uint32_t base_u = smem_addr(sm_raw);
+    const uint32_t base_u = ptx::smem_u32(sm_raw);
     unsigned char* stage0 = sm_raw + ((1024 - (base_u & 1023)) & 1023);
     float* s_hist = reinterpret_cast<float*>(sm_raw + P.hist_off);  // per warp: nrbins high, nrbins low parts
     int* s_thr = reinterpret_cast<int*>(sm_raw + P.thr_off);
@@ -120,7 +78,7 @@ k_bin_power_tma(const __grid_constant__ CUtensorMap tmap, GridArgs g, const int*
     }
     if (tid == 0) {
         s_abort = 0;
-        for (int st = 0; st < STAGES; st++) mbar_init_(&bars[st], 1);
+        for (int st = 0; st < STAGES; st++) ptx::mbar_init(&bars[st], 1);
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
     }
     __syncthreads();
@@ -128,8 +86,8 @@ k_bin_power_tma(const __grid_constant__ CUtensorMap tmap, GridArgs g, const int*
     if (tid == 0) {
         for (int k = 0; k < STAGES && k < my_n; k++) {
             const int tile = blockIdx.x + k * gridDim.x;
-            mbar_expect_tx_(&bars[k], ROWS * 128);
-            tma_load_2d(stage0 + (size_t)k * ROWS * 128, &tmap, &bars[k], 0, tile * ROWS);
+            ptx::mbar_expect_tx(&bars[k], ROWS * 128);
+            ptx::tma_load_2d(stage0 + (size_t)k * ROWS * 128, &tmap, &bars[k], 0, tile * ROWS);
         }
     }
     BinPairAcc2 acc;
@@ -138,7 +96,7 @@ k_bin_power_tma(const __grid_constant__ CUtensorMap tmap, GridArgs g, const int*
         const int st = k % STAGES;
         const int tile = blockIdx.x + k * gridDim.x;
         if (tid == 0) {
-            if (!mbar_wait_bounded_(&bars[st], (k / STAGES) & 1)) s_abort = 1;
+            if (!ptx::mbar_wait_bounded(&bars[st], (k / STAGES) & 1)) s_abort = 1;
             const long long m = (long long)tile * ROWS * 16;
             s_rowbase = m / g.nz;
             s_zbase = (int)(m - s_rowbase * g.nz);
@@ -186,8 +144,8 @@ k_bin_power_tma(const __grid_constant__ CUtensorMap tmap, GridArgs g, const int*
         __syncthreads();
         if (tid == 0 && k + STAGES < my_n) {
             const int nt = blockIdx.x + (k + STAGES) * gridDim.x;
-            mbar_expect_tx_(&bars[st], ROWS * 128);
-            tma_load_2d(stage0 + (size_t)st * ROWS * 128, &tmap, &bars[st], 0, nt * ROWS);
+            ptx::mbar_expect_tx(&bars[st], ROWS * 128);
+            ptx::tma_load_2d(stage0 + (size_t)st * ROWS * 128, &tmap, &bars[st], 0, nt * ROWS);
         }
     }
     if (s_abort) {
@@ -195,7 +153,7 @@ k_bin_power_tma(const __grid_constant__ CUtensorMap tmap, GridArgs g, const int*
         if (tid == 0) {
             atomicOr(status, kStTimeout);
             for (int kk = k; kk < my_n && kk < k + STAGES; kk++)
-                mbar_wait_bounded_(&bars[kk % STAGES], (kk / STAGES) & 1);
+                ptx::mbar_wait_bounded(&bars[kk % STAGES], (kk / STAGES) & 1);
         }
         return;
     }
@@ -275,7 +233,7 @@ k_correct_tma(const __grid_constant__ CUtensorMap tmap, GridArgs g, const int* _
     __shared__ long long s_rowbase;
     __shared__ int s_zbase;
     const SmemPlan P = plan_smem(ROWS, STAGES, g.nrbins, 3 * g.nk + g.nrbins);
-    const uint32_t base_u = smem_addr(sm_raw);
+    const uint32_t base_u = ptx::smem_u32(sm_raw);
     unsigned char* stage0 = sm_raw + ((1024 - (base_u & 1023)) & 1023);
     int* s_thr = reinterpret_cast<int*>(sm_raw + P.thr_off);
     float* s_tab = reinterpret_cast<float*>(sm_raw + P.tab_off);
@@ -292,7 +250,7 @@ k_correct_tma(const __grid_constant__ CUtensorMap tmap, GridArgs g, const int* _
     }
     if (tid == 0) {
         s_abort = 0;
-        for (int st = 0; st < STAGES; st++) mbar_init_(&bars[st], 1);
+        for (int st = 0; st < STAGES; st++) ptx::mbar_init(&bars[st], 1);
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
     }
     __syncthreads();
@@ -301,8 +259,8 @@ k_correct_tma(const __grid_constant__ CUtensorMap tmap, GridArgs g, const int* _
     if (tid == 0) {
         for (int k = 0; k < STAGES - 1 && k < my_n; k++) {
             const int tile = blockIdx.x + k * gridDim.x;
-            mbar_expect_tx_(&bars[k], ROWS * 128);
-            tma_load_2d(stage0 + (size_t)k * ROWS * 128, &tmap, &bars[k], 0, tile * ROWS);
+            ptx::mbar_expect_tx(&bars[k], ROWS * 128);
+            ptx::tma_load_2d(stage0 + (size_t)k * ROWS * 128, &tmap, &bars[k], 0, tile * ROWS);
         }
     }
     unsigned flags = 0;
@@ -312,7 +270,7 @@ k_correct_tma(const __grid_constant__ CUtensorMap tmap, GridArgs g, const int* _
         const int st = k % STAGES;
         const int tile = blockIdx.x + k * gridDim.x;
         if (tid == 0) {
-            if (!mbar_wait_bounded_(&bars[st], (k / STAGES) & 1)) s_abort = 1;
+            if (!ptx::mbar_wait_bounded(&bars[st], (k / STAGES) & 1)) s_abort = 1;
             const long long m = (long long)tile * ROWS * 16;
             s_rowbase = m / g.nz;
             s_zbase = (int)(m - s_rowbase * g.nz);
@@ -349,17 +307,17 @@ k_correct_tma(const __grid_constant__ CUtensorMap tmap, GridArgs g, const int* _
                 *vp = v;
             }
         }
-        fence_async_smem();
+        ptx::fence_async_smem();
         __syncthreads();
         if (tid == 0) {
-            tma_store_2d(&tmap, stage0 + (size_t)st * ROWS * 128, 0, tile * ROWS);
-            bulk_commit();
+            ptx::tma_store_2d(&tmap, stage0 + (size_t)st * ROWS * 128, 0, tile * ROWS);
+            ptx::bulk_commit();
             if (k + STAGES - 1 < my_n) {
                 const int s2 = (k + STAGES - 1) % STAGES;
                 const int nt = blockIdx.x + (k + STAGES - 1) * gridDim.x;
-                bulk_wait_read_le1();  // the store issued from stage s2 one iteration ago has been read
-                mbar_expect_tx_(&bars[s2], ROWS * 128);
-                tma_load_2d(stage0 + (size_t)s2 * ROWS * 128, &tmap, &bars[s2], 0, nt * ROWS);
+                ptx::bulk_wait_read_le1();  // the store issued from stage s2 one iteration ago has been read
+                ptx::mbar_expect_tx(&bars[s2], ROWS * 128);
+                ptx::tma_load_2d(stage0 + (size_t)s2 * ROWS * 128, &tmap, &bars[s2], 0, nt * ROWS);
             }
         }
     }
@@ -367,9 +325,9 @@ k_correct_tma(const __grid_constant__ CUtensorMap tmap, GridArgs g, const int* _
         if (s_abort) {
             atomicOr(status, kStTimeout);
             for (int kk = k; kk < my_n && kk < k + STAGES - 1; kk++)
-                mbar_wait_bounded_(&bars[kk % STAGES], (kk / STAGES) & 1);
+                ptx::mbar_wait_bounded(&bars[kk % STAGES], (kk / STAGES) & 1);
         }
-        bulk_wait_all();
+        ptx::bulk_wait_all();
     }
     if (s_abort) return;
     // trailing modes (fewer than 16) by CTA 0

@@ -22,42 +22,9 @@
 #include <cuda_runtime.h>
 #include <stdio.h>
 #include "ksp_internal.h"
+#include "ksp_ptx.cuh"
 
 namespace ksp {
-
-// ------------------------------------------------------------------ small PTX helpers
-__device__ __forceinline__ uint32_t smem_u32(const void* p) {
-    return static_cast<uint32_t>(__cvta_generic_to_shared(p));
-}
-__device__ __forceinline__ void mbar_init(uint64_t* bar, unsigned count) {
-    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(count) : "memory");
-}
-__device__ __forceinline__ void mbar_expect_tx(uint64_t* bar, unsigned bytes) {
-    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)), "r"(bytes)
-                 : "memory");
-}
-__device__ __forceinline__ bool mbar_try_wait(uint64_t* bar, unsigned phase) {
-    uint32_t ok;
-    asm volatile(
-        "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}\n"
-        : "=r"(ok)
-        : "r"(smem_u32(bar)), "r"(phase)
-        : "memory");
-    return ok != 0;
-}
-// Bounded wait: gives up after ~2^22 polls (each poll may suspend for a while).
-__device__ __forceinline__ bool mbar_wait_bounded(uint64_t* bar, unsigned phase) {
-    for (int it = 0; it < (1 << 22); it++)
-        if (mbar_try_wait(bar, phase)) return true;
-    return false;
-}
-__device__ __forceinline__ void bulk_g2s(void* dst, const void* src, unsigned bytes, uint64_t* bar) {
-    asm volatile(
-        "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
-            smem_u32(dst)),
-        "l"(src), "r"(bytes), "r"(smem_u32(bar))
-        : "memory");
-}
 
 // ------------------------------------------------------------------ background tables
 struct RhoIntegrand {  // omega_nu_single.c:89-96
@@ -118,6 +85,39 @@ void launch_background_tables(Background* dB, double a0, cudaStream_t st, unsign
     cudaFreeAsync(scratch, st);
 }
 
+// Natural cubic spline of log H on n uniform knots (spacing h), as per-segment
+// polynomial coefficients (y_i, b_i, c_i, d_i): one thread (a one-time set-up).
+__global__ void k_hubble_table(const double* H, int n, double h, double* coef, double* m) {
+    if (threadIdx.x != 0 || blockIdx.x != 0) return;
+    // second derivatives: m[i-1] + 4 m[i] + m[i+1] = 6 (y[i+1] - 2 y[i] + y[i-1]) / h^2,
+    // m[0] = m[n-1] = 0 (Thomas algorithm; coef[4i+1] holds the modified diagonal ratio)
+    double* cp = coef;  // scratch for the forward sweep, overwritten below
+    m[0] = 0;
+    m[n - 1] = 0;
+    double prev_c = 0, prev_d = 0;
+    for (int i = 1; i < n - 1; i++) {
+        const double r = 6.0 * (log(H[i + 1]) - 2.0 * log(H[i]) + log(H[i - 1])) / (h * h);
+        const double den = 4.0 - prev_c;
+        const double ci = 1.0 / den;
+        const double di = (r - prev_d) / den;
+        cp[4 * i] = ci;
+        cp[4 * i + 1] = di;
+        prev_c = ci;
+        prev_d = di;
+    }
+    for (int i = n - 2; i >= 1; i--) m[i] = cp[4 * i + 1] - cp[4 * i] * m[i + 1];
+    for (int i = 0; i < n - 1; i++) {
+        const double y0 = log(H[i]), y1 = log(H[i + 1]);
+        coef[4 * i] = y0;
+        coef[4 * i + 1] = (y1 - y0) / h - h * (2.0 * m[i] + m[i + 1]) / 6.0;
+        coef[4 * i + 2] = 0.5 * m[i];
+        coef[4 * i + 3] = (m[i + 1] - m[i]) / (6.0 * h);
+    }
+}
+void launch_hubble_table(const double* H, int n, double h, double* coef, double* scratch, cudaStream_t st) {
+    k_hubble_table<<<1, 32, 0, st>>>(H, n, h, coef, scratch);
+}
+
 __global__ void k_spline1(const double* x, const double* y, double* c, double* scratch, int n) {
     if (threadIdx.x == 0 && blockIdx.x == 0) natural_spline_coeffs(x, y, n, c, scratch);
 }
@@ -147,6 +147,34 @@ __global__ void k_nufrac_low(Background* B, double light, double vcrit, unsigned
 }
 void launch_nufrac_low(Background* dB, double light, double vcrit, cudaStream_t st, unsigned* status) {
     k_nufrac_low<<<1, 32 * kNuSpecies, 0, st>>>(dB, light, vcrit, status);
+}
+
+// nufrac_low(qc) of n momenta (omega_nu_single.c:214-228): a warp per value
+__global__ void k_nufrac_low_values(const double* qc, int n, double* out, unsigned* status) {
+    __shared__ Gk61Nodes N;
+    __shared__ QagList L[4];
+    gk61_fill(N, threadIdx.x, blockDim.x);
+    __syncthreads();
+    const int w = threadIdx.x >> 5;
+    const int i = blockIdx.x * 4 + w;
+    if (i >= n) return;
+    QagResult r = qag_warp(FermiDirac{}, N, L[w], 0.0, qc[i], 0.0, 1e-6, 100);
+    if ((threadIdx.x & 31) == 0) {
+        out[i] = r.result / (1.5 * kZeta3);
+        if (!r.ok) atomicOr(status, kStGsl);
+    }
+}
+void launch_nufrac_low_values(const double* qc, int n, double* out, unsigned* status, cudaStream_t st) {
+    if (n > 0) k_nufrac_low_values<<<(n + 3) / 4, 128, 0, st>>>(qc, n, out, status);
+}
+
+// specialJ of n arguments (the device function the integrator uses)
+__global__ void k_special_j(const double* x, int n, double qc, double nfl, double* out) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) out[i] = specialJ(x[i], qc, nfl);
+}
+void launch_special_j(const double* x, int n, double qc, double nufrac_low, double* out, cudaStream_t st) {
+    if (n > 0) k_special_j<<<(n + 127) / 128, 128, 0, st>>>(x, n, qc, nufrac_low, out);
 }
 
 // ------------------------------------------------------------------ history rows
@@ -422,7 +450,7 @@ __global__ void __launch_bounds__(128) k_dnu_qag(IntegratorDev I, int nk, int Na
 
     gk61_fill(N, threadIdx.x, blockDim.x);
     for (int i = threadIdx.x; i < Na; i += blockDim.x) knots[i] = I.scalefact[i];
-    if (lane == 0) mbar_init(mybar, 1);
+    if (lane == 0) ptx::mbar_init(mybar, 1);
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
     __syncthreads();
 
@@ -436,7 +464,7 @@ __global__ void __launch_bounds__(128) k_dnu_qag(IntegratorDev I, int nk, int Na
     for (int task = blockIdx.x * nw + warp; task < ntask; task += gridDim.x * nw) {
         const int si = task / nk, ik = task % nk;
         const int mi = si == 0 ? spec_ids.x : (si == 1 ? spec_ids.y : spec_ids.z);
-        const double k = I.wavenum[ik];
+        const double k = I.kq ? I.kq[ik] : I.wavenum[ik];
         // the task's divisions on lane 0
         double mnubykT = 0, kom = 0, fsi = 0;
         if (lane == 0) {
@@ -455,16 +483,16 @@ __global__ void __launch_bounds__(128) k_dnu_qag(IntegratorDev I, int nk, int Na
             if (lane == 0) {
                 // order this warp's earlier generic reads of the buffers before the async writes
                 asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
-                mbar_expect_tx(mybar, Na > 2 ? 2 * row_bytes : row_bytes);
-                bulk_g2s(row, I.dtot + (size_t)ik * I.ld, row_bytes, mybar);
-                if (Na > 2) bulk_g2s(rc, I.coef + (size_t)ik * I.ld, row_bytes, mybar);
+                ptx::mbar_expect_tx(mybar, Na > 2 ? 2 * row_bytes : row_bytes);
+                ptx::bulk_g2s(row, I.dtot + (size_t)ik * I.ld, row_bytes, mybar);
+                if (Na > 2) ptx::bulk_g2s(rc, I.coef + (size_t)ik * I.ld, row_bytes, mybar);
             }
-            const bool got = __all_sync(0xffffffffu, mbar_wait_bounded(mybar, phase));  // warp-uniform
+            const bool got = __all_sync(0xffffffffu, ptx::mbar_wait_bounded(mybar, phase));  // warp-uniform
             phase ^= 1;
             if (!got) {
                 if (lane == 0) atomicOr(I.status, kStTimeout);
                 // wait (bounded) for the copy still in flight before leaving
-                mbar_wait_bounded(mybar, phase ^ 1);
+                ptx::mbar_wait_bounded(mybar, phase ^ 1);
                 return;
             }
             const KnotSeg ks{I.knot_invh, I.knot_h3, I.knot_ih3};
@@ -542,19 +570,19 @@ __global__ void __launch_bounds__(SPEC ? 256 : 128, SPEC ? 2 : 4)
         const bool integ = !S.skip_integral && Na > 1 && mnu / B->kBtnu > 0;
         if (integ) {
             asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
-            mbar_expect_tx(bar, Na > 2 ? 2 * row_bytes : row_bytes);
-            bulk_g2s(row, I.dtot + (size_t)ik * I.ld, row_bytes, bar);
-            if (Na > 2) bulk_g2s(rc, I.coef + (size_t)ik * I.ld, row_bytes, bar);
+            ptx::mbar_expect_tx(bar, Na > 2 ? 2 * row_bytes : row_bytes);
+            ptx::bulk_g2s(row, I.dtot + (size_t)ik * I.ld, row_bytes, bar);
+            if (Na > 2) ptx::bulk_g2s(rc, I.coef + (size_t)ik * I.ld, row_bytes, bar);
         }
         const double m = mnu / B->kBtnu;
         s_task[0] = m;
-        s_task[1] = I.wavenum[ik] / m;
+        s_task[1] = (I.kq ? I.kq[ik] : I.wavenum[ik]) / m;
         s_task[2] = (S.Nfs - 1.) / (S.loga - S.loga0);
         s_task[3] = integ ? 1.0 : 0.0;
     };
     // the first task's copies are in flight while the block fills its tables
     if (tid == 0) {
-        mbar_init(bar, 1);
+        ptx::mbar_init(bar, 1);
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
         if (blockIdx.x < ntask) start_task(blockIdx.x);
     }
@@ -567,7 +595,7 @@ __global__ void __launch_bounds__(SPEC ? 256 : 128, SPEC ? 2 : 4)
     for (int task = blockIdx.x; task < ntask; task += gridDim.x) {
         const int si = task / nk, ik = task % nk;
         const int mi = si == 0 ? spec_ids.x : (si == 1 ? spec_ids.y : spec_ids.z);
-        const double k = I.wavenum[ik];
+        const double k = I.kq ? I.kq[ik] : I.wavenum[ik];
         if (task != (int)blockIdx.x) {  // later tasks: after the previous task's reads of row / rc
             __syncthreads();
             if (tid == 0) start_task(task);
@@ -577,11 +605,11 @@ __global__ void __launch_bounds__(SPEC ? 256 : 128, SPEC ? 2 : 4)
         double integral = 0;
         const bool integrate = s_task[3] != 0.0;
         if (integrate) {
-            const bool got = __syncthreads_and(mbar_wait_bounded(bar, phase));  // block-uniform
+            const bool got = __syncthreads_and(ptx::mbar_wait_bounded(bar, phase));  // block-uniform
             phase ^= 1;
             if (!got) {
                 if (tid == 0) atomicOr(I.status, kStTimeout);
-                mbar_wait_bounded(bar, phase ^ 1);
+                ptx::mbar_wait_bounded(bar, phase ^ 1);
                 return;
             }
             const KnotSeg ks{I.knot_invh, I.knot_h3, I.knot_ih3};
@@ -648,6 +676,55 @@ static void gl_nodes(int n, double* X, double* Wt) {
         X[i] = x;
         Wt[i] = 2 / ((1 - x * x) * dp * dp);
     }
+}
+
+// fslength(logai, logaf) = light * int_{logai}^{logaf} dlna / (a^2 H(a)) (delta_tot_table.c:378-407)
+// for n intervals, a warp each: the interval is cut into segments of at most 0.01 in
+// log a, each integrated with the 8-point Gauss-Legendre rule (the integrand is smooth on
+// a scale of ~1 in log a, so the rule error is far below double rounding); lanes take
+// segments in turn and the warp sums them.  0 where logai >= logaf, as the reference.
+struct GL8 {
+    double x[8], w[8];
+};
+__global__ void k_fslength_values(const Background* B, const double* lai, const double* laf, int n, double light,
+                                  GL8 gl, double* out) {
+    const int lane = threadIdx.x & 31;
+    const int i = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
+    if (i >= n) return;
+    const double a0 = lai[i], a1 = laf[i];
+    double acc = 0;
+    if (a0 < a1) {
+        const int nseg = (int)ceil((a1 - a0) / 0.01);
+        const double h = (a1 - a0) / nseg;
+        for (int sgi = lane; sgi < nseg; sgi += 32) {
+            const double c = a0 + (sgi + 0.5) * h;
+            double sseg = 0;
+            for (int q = 0; q < 8; q++) {
+                const double la = c + 0.5 * h * gl.x[q];
+                const double a = exp(la);
+                sseg += gl.w[q] / (a * (a * hubble(*B, a, la)));
+            }
+            acc += 0.5 * h * sseg;
+        }
+    }
+    for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
+    if (lane == 0) out[i] = a0 < a1 ? light * acc : 0.0;
+}
+void launch_fslength_values(const Background* dB, const double* logai, const double* logaf, int n, double light,
+                            double* out, cudaStream_t st) {
+    static GL8 gl;
+    static bool have = false;
+    if (!have) {
+        double X[4], Wt[4];  // the positive half; nodes come in +-x pairs
+        gl_nodes(8, X, Wt);
+        for (int q = 0; q < 4; q++) {
+            gl.x[2 * q] = X[q];
+            gl.x[2 * q + 1] = -X[q];
+            gl.w[2 * q] = gl.w[2 * q + 1] = Wt[q];
+        }
+        have = true;
+    }
+    if (n > 0) k_fslength_values<<<(n + 3) / 4, 128, 0, st>>>(dB, logai, logaf, n, light, gl, out);
 }
 static GL4 gl4_host() {
     GL4 g;

@@ -34,6 +34,8 @@ struct IntegratorDev {
     double* nu_init;                 // [nk_alloc]
     double* nu_last;                 // [nk_alloc]
     double* wavenum;                 // [nk_alloc]
+    const double* kq;                // k of the bins of the current call (the reference integrates at
+                                     // the wavenum argument, delta_tot_table.c:526,593); null = wavenum
     double* dcdm;                    // [nk_alloc] sqrt(P_cdm) of the current call
     double* dnu_s;                   // [kNuSpecies][nk_alloc] per-species delta_nu
     double* dnu;                     // [nk_alloc] combined
@@ -468,6 +470,15 @@ void launch_background_tables(Background* dB, double a0, cudaStream_t st, unsign
 void launch_spline_coeffs_1thread(const double* x, const double* y, double* c, double* scratch, int n,
                                   cudaStream_t st);
 void launch_nufrac_low(Background* dB, double light, double vcrit, cudaStream_t st, unsigned* status);
+// natural cubic spline of log H on n uniform knots of spacing h: coef[4 (n-1)], scratch[n]
+void launch_hubble_table(const double* H, int n, double h, double* coef, double* scratch, cudaStream_t st);
+// nufrac_low (omega_nu_single.c:214-228) of n momenta, a warp each
+void launch_nufrac_low_values(const double* qc, int n, double* out, unsigned* status, cudaStream_t st);
+// specialJ (delta_tot_table.c:457-463) of n arguments
+void launch_special_j(const double* x, int n, double qc, double nufrac_low, double* out, cudaStream_t st);
+// fslength (delta_tot_table.c:394-407) of n intervals [logai, logaf], a warp each
+void launch_fslength_values(const Background* dB, const double* logai, const double* logaf, int n, double light,
+                            double* out, cudaStream_t st);
 // update_delta_tot (delta_tot_table.c:177-191) for row `row` at scale factor a
 void launch_update_row(const IntegratorDev& I, int nk, int row, double a, double loga, const double* dcdm,
                        const double* dnu, cudaStream_t st);

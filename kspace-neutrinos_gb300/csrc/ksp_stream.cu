@@ -28,10 +28,7 @@
 #include <cuda.h>
 #include <cuda_runtime.h>
 #include <stdint.h>
-#include <map>
 #include <mutex>
-#include <set>
-#include <tuple>
 #include "ksp_internal.h"
 #include "ksp_gridutil.cuh"
 #include "ksp_ptx.cuh"
@@ -865,45 +862,72 @@ int sm_count_s() {
 // shared memory on the current device, memoised: the occupancy query and the attribute
 // call cost host microseconds, and at every step the device waits for the first launch.
 // The kernel's dynamic shared-memory limit is raised once per device to the largest any
-// of these passes asks for (220 KB); each launch still asks for its own size.
+// of these passes asks for (220 KB); each launch still asks for its own size.  The memo
+// is a fixed table (no host allocation: the allocation-free entry point runs through
+// here): 64 (kernel, device, threads, smem) results, replaced round-robin, and the
+// kernels whose shared-memory limit was raised.
 constexpr int kMaxSmemPass = 220 * 1024;
+struct OccEntry {
+    const void* kern;
+    int dev, threads, n;
+    size_t smem;
+};
 template <typename K>
 int resident_blocks(K kern, int threads, size_t smem) {
     static std::mutex m;
-    static std::map<std::tuple<const void*, int, int, size_t>, int> memo;
-    static std::set<std::pair<const void*, int>> raised;
+    static OccEntry memo[64];
+    static int memo_n = 0, memo_next = 0;
+    static std::pair<const void*, int> raised[64];
+    static int raised_n = 0;
     int dev = 0;
     if (cudaGetDevice(&dev) != cudaSuccess) return 0;
     const void* kp = reinterpret_cast<const void*>(kern);
     std::lock_guard<std::mutex> lock(m);
-    const auto key = std::make_tuple(kp, dev, threads, smem);
-    const auto it = memo.find(key);
-    if (it != memo.end()) return it->second;
-    if (raised.insert(std::make_pair(kp, dev)).second)
+    for (int i = 0; i < memo_n; i++)
+        if (memo[i].kern == kp && memo[i].dev == dev && memo[i].threads == threads && memo[i].smem == smem)
+            return memo[i].n;
+    bool done = false;
+    for (int i = 0; i < raised_n && !done; i++) done = raised[i].first == kp && raised[i].second == dev;
+    if (!done) {
         cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, kMaxSmemPass);
+        if (raised_n < 64) raised[raised_n++] = std::make_pair(kp, dev);
+    }
     int n = 0;
     if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, kern, threads, smem) != cudaSuccess) n = 0;
-    memo[key] = n;
+    memo[memo_next] = OccEntry{kp, dev, threads, n, smem};
+    memo_next = (memo_next + 1) % 64;
+    if (memo_n < 64) memo_n++;
     return n;
 }
 
 // The 2-D tensor map of a grid pointer, memoised per device (a handful of grids and slab
-// chunks recur at every step); at most 64 are kept.
+// chunks recur at every step) in a fixed table of 64, replaced round-robin.
+struct TmapEntry {
+    int dev, rows;
+    const void* grid;
+    long long nrows16;
+    CUtensorMap map;
+};
 bool grid_tmap_cached(CUtensorMap* map, const void* grid, long long nrows16, int rows) {
     static std::mutex m;
-    static std::map<std::tuple<int, const void*, long long, int>, CUtensorMap> memo;
+    static TmapEntry memo[64];
+    static int memo_n = 0, memo_next = 0;
     int dev = 0;
     if (cudaGetDevice(&dev) != cudaSuccess) return false;
-    const auto key = std::make_tuple(dev, grid, nrows16, rows);
     std::lock_guard<std::mutex> lock(m);
-    const auto it = memo.find(key);
-    if (it != memo.end()) {
-        *map = it->second;
-        return true;
-    }
+    for (int i = 0; i < memo_n; i++)
+        if (memo[i].dev == dev && memo[i].grid == grid && memo[i].nrows16 == nrows16 && memo[i].rows == rows) {
+            *map = memo[i].map;
+            return true;
+        }
     if (!make_grid_tmap(map, grid, nrows16, rows)) return false;
-    if (memo.size() >= 64) memo.clear();
-    memo[key] = *map;
+    memo[memo_next].dev = dev;
+    memo[memo_next].rows = rows;
+    memo[memo_next].grid = grid;
+    memo[memo_next].nrows16 = nrows16;
+    memo[memo_next].map = *map;
+    memo_next = (memo_next + 1) % 64;
+    if (memo_n < 64) memo_n++;
     return true;
 }
 

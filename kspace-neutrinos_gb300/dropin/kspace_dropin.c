@@ -16,9 +16,9 @@
 #include <string.h>
 #include "kspace_neutrinos_dropin.h"
 #include "kspace_gpu.h"
+#include "kspace_hubble_match.h"
 
 #define KSP_LIGHTCGS 2.99792458e10
-#define KSP_HUBBLE 3.24077929e-18
 /* gadget_defines.h:47-49 (parameter types of the P-Gadget3 reader) */
 #define KSP_REAL 1
 #define KSP_STRING 2
@@ -132,46 +132,13 @@ static void load_transfer(double BoxSize, double UnitLength_in_cm, MPI_Comm comm
     free(buf);
 }
 
-/* The host owns H(a).  Identify OmegaLambda, curvature and the radiation term of the
- * host's hubble_function against the device model, then verify it at 64 points. */
-static void match_hubble(double Omega0, double UnitTime_in_s)
+/* The host owns H(a): identify it with the device model (kspace_hubble_match.h). */
+static void match_hubble(double Omega0, double UnitTime_in_s, double TimeMax)
 {
-    const double H0 = KSP_HUBBLE * UnitTime_in_s;
-    int best = -1;
-    double best_err = 1e300;
-    /* candidates: flat (OmegaLambda = 1 - Omega0) or curvature with OmegaLambda from
-     * H(1); radiation on or off */
-    for (int rad = 1; rad >= 0; rad--) {
-        for (int flat = 1; flat >= 0; flat--) {
-            double OL = 1 - Omega0;
-            if (!flat) {
-                /* H(1)^2/H0^2 = Omega0 + OmegaK + OmegaL + rad*Og = 1 + rad*Og when OmegaK = 1-Omega0-OmegaL;
-                 * the curvature cannot be read from H(1): use H(0.5). */
-                const double h1 = hubble_function(0.5) / H0;
-                check(kspace_gpu_set_hubble(g_ctx, Omega0, 1 - Omega0, UnitTime_in_s, rad), "set_hubble");
-                double hm = 0;
-                kspace_gpu_hubble(g_ctx, 0.5, &hm);
-                hm /= H0;
-                /* with OmegaK = 1 - Omega0 - OL: h^2 = flat_h^2 + (1-Omega0-OL)(1/a^2 - 1) at a = 0.5 */
-                OL = 1 - Omega0 - (h1 * h1 - hm * hm) / 3.0;
-            }
-            check(kspace_gpu_set_hubble(g_ctx, Omega0, OL, UnitTime_in_s, rad), "set_hubble");
-            double a[64], H[64], err = 0;
-            for (int i = 0; i < 64; i++) {
-                a[i] = exp(log(kspace_params.TimeTransfer / 2) + i * (log(2.0) - log(kspace_params.TimeTransfer / 2)) / 63);
-                H[i] = hubble_function(a[i]);
-            }
-            kspace_gpu_check_hubble(g_ctx, a, H, 64, 1e-12, &err);
-            if (err < best_err) {
-                best_err = err;
-                best = rad * 2 + flat;
-            }
-            if (err < 1e-12)
-                return;
-        }
-    }
-    terminate(10004, "hubble_function is not of the form H0 sqrt(Om/a^3 + Ok/a^2 + OL + Onu(a) [+ Og/a^4]) "
-                     "(best relative difference %g, case %d)\n", best_err, best);
+    double err = 0;
+    if (kspace_match_hubble(g_ctx, Omega0, UnitTime_in_s, kspace_params.TimeTransfer, TimeMax, &err) != KSPACE_OK)
+        terminate(10004, "hubble_function is not of the form H0 sqrt(Om/a^3 + Ok/a^2 + OL + Onu(a) [+ Og/a^4]) "
+                         "(best relative difference %g)\n", err);
 }
 
 /* interface_common.c:77-102 */
@@ -184,7 +151,7 @@ void allocate_kspace_memory(const int nk_in, const int ThisTask, const double Bo
     if (kspace_params.hybrid_neutrinos_on)
         check(kspace_gpu_init_hybrid_nu(g_ctx, kspace_params.vcrit, KSP_LIGHTCGS / 1e5, kspace_params.nu_crit_time),
               "init_hybrid_nu");
-    match_hubble(Omega0, UnitTime_in_s);
+    match_hubble(Omega0, UnitTime_in_s, TimeMax);
     check(kspace_gpu_alloc_table(g_ctx, nk_in, kspace_params.TimeTransfer, TimeMax, Omega0, UnitTime_in_s,
                                  UnitLength_in_cm), "allocate_delta_tot_table");
     load_transfer(BoxSize, UnitLength_in_cm, comm);
@@ -232,6 +199,9 @@ void compute_total_power_spectrum(const double Time, const double BoxSize, fftw_
     g_comm = comm;
     int nranks = 1;
     MPI_Comm_size(comm, &nranks);
+    MPI_Comm_rank(comm, &g_rank);
+    if (!g_ctx) /* a run without the neutrino module (gadget-2 patch 0004) */
+        check(kspace_gpu_create(&g_ctx, pick_device()), "kspace_gpu_create");
     check(kspace_gpu_set_allreduce(g_ctx, nranks > 1 ? allreduce_sum : NULL, &g_comm), "set_allreduce");
     check(kspace_gpu_compute_total_power_spectrum(g_ctx, Time, BoxSize, fft_of_rhogrid, pmgrid, slabstart_y,
                                                   nslab_y), "compute_total_power_spectrum");
@@ -240,6 +210,8 @@ void compute_total_power_spectrum(const double Time, const double BoxSize, fftw_
 /* interface_gadget.c:196-224 */
 int save_total_power(const double Time, const int snapnum, const char *OutputDir)
 {
+    if (!g_ctx)
+        terminate(10003, "save_total_power before any power spectrum was computed\n");
     return kspace_gpu_save_total_power(g_ctx, Time, snapnum, OutputDir);
 }
 
@@ -275,32 +247,6 @@ _delta_pow compute_neutrino_power_from_cdm(const double Time, const double keff_
           "compute_neutrino_power_from_cdm");
     return d;
 }
-
-/* delta_pow.c:19-37 */
-double get_dnudcdm_powerspec(_delta_pow *d_pow, double kk)
-{
-    const double *x = d_pow->logkk, *y = d_pow->delta_ratio;
-    const int n = d_pow->nbins;
-    if (kk < x[0] && kk > x[0] - log(2))
-        kk = x[0];
-    if (kk < x[0] - log(2)) {
-        fprintf(stderr, "trying to extract a k= %g < min stored = %g \n", kk, x[0]);
-        kk = x[0];
-    }
-    if (kk > x[n - 1])
-        kk = x[n - 1];
-    int lo = 0, hi = n - 1;
-    while (hi > lo + 1) {
-        const int mid = (lo + hi) / 2;
-        if (x[mid] > kk)
-            hi = mid;
-        else
-            lo = mid;
-    }
-    return d_pow->norm * (y[lo] + (kk - x[lo]) * ((y[lo + 1] - y[lo]) / (x[lo + 1] - x[lo])));
-}
-
-void free_d_pow(_delta_pow *d_pow) { (void)d_pow; }
 
 /* interface_common.c:41-52,150-197 */
 void save_nu_state(char *savedir)

@@ -67,7 +67,8 @@ _SIGS = {
     "kspace_gpu_set_vectors": (_i, [_vp, _PD, _PD, _PD, _i]),
     "kspace_gpu_set_jmass": (_i, [_vp, _PD]),
     "kspace_gpu_diff_forward": (_i, [_vp, _d, _d, _vp, _vp, _i, _vp, _i]),
-    "kspace_gpu_diff_backward": (_i, [_vp, _vp, _vp, _vp, _vp, _vp, _PD, _i]),
+    "kspace_gpu_diff_backward": (_i, [_vp, _vp, _vp, _vp, _vp, _vp, _PD, _i, C.c_longlong]),
+    "kspace_gpu_diff_generation": (_i, [_vp, _PLL]),
     "kspace_gpu_batch_create": (_i, [C.POINTER(_vp), C.POINTER(_vp), _i]),
     "kspace_gpu_batch_destroy": (_i, [_vp]),
     "kspace_gpu_batch_bind_grid": (_i, [_vp, _i, _vp, _i, _d]),
@@ -79,6 +80,20 @@ _SIGS = {
     "kspace_gpu_batch_autotune": (_i, [_vp, _PD, _vp, _i, _PI, C.POINTER(C.c_float)]),
     "kspace_gpu_batch_last_ms": (_i, [_vp, C.POINTER(C.c_float)]),
     "kspace_gpu_bin_power_noalloc": (_i, [_i, _vp, _i, _i, _i, _vp, _vp]),
+    "kspace_gpu_set_hybrid": (_i, [_vp, _i, _d, _d, _PD]),
+    "kspace_gpu_set_hubble_table": (_i, [_vp, _d, _d, _i, _PD]),
+    "kspace_gpu_delta_tot_init": (_i, [_vp, _i, _PD, _PD, _d]),
+    "kspace_gpu_get_delta_nu": (_i, [_vp, _d, _i, _PD, _PD, _d]),
+    "kspace_gpu_get_delta_nu_combined": (_i, [_vp, _d, _i, _PD, _PD]),
+    "kspace_gpu_update_delta_tot": (_i, [_vp, _d, _PD, _PD, _i]),
+    "kspace_gpu_set_table": (_i, [_vp, _i, _i, _i, _PD, _PD, C.c_size_t, _PD, _PD, _PD]),
+    "kspace_gpu_get_table": (_i, [_vp, _i, _PI, _PI, _PI, _PD, _PD, C.c_size_t, _PD, _PD, _PD]),
+    "kspace_gpu_special_j": (_i, [_vp, _PD, _i, _d, _d, _PD]),
+    "kspace_gpu_nufrac_low": (_i, [_vp, _PD, _i, _PD]),
+    "kspace_gpu_fslength": (_i, [_vp, _PD, _PD, _i, _d, _PD]),
+    "kspace_gpu_omega_nu_single": (_i, [_vp, _d, _i, _PD]),
+    "kspace_gpu_omega_g": (_i, [_vp, _d, _PD]),
+    "kspace_gpu_background_info": (_i, [_vp, _PD, _PD, _PI, _PD]),
 }
 
 _lib = None
@@ -209,6 +224,10 @@ class KspaceNeutrinos:
         _check(self.L.kspace_gpu_set_hubble(self.h, Omega0, OmegaLambda, UnitTime_in_s, int(include_radiation)),
                "set_hubble")
 
+    def set_hubble_table(self, loga_lo, dloga, H):
+        h = _f64(H)
+        _check(self.L.kspace_gpu_set_hubble_table(self.h, loga_lo, dloga, len(h), _pd(h)), "set_hubble_table")
+
     def check_hubble(self, a, H, rtol=1e-12):
         a = _f64(a)
         H = _f64(H)
@@ -235,6 +254,36 @@ class KspaceNeutrinos:
         v = _d()
         _check(self.L.kspace_gpu_hubble(self.h, a, C.byref(v)), "hubble")
         return v.value
+
+    def set_hybrid(self, enabled, vcrit_frac, nu_crit_time, nufrac_low):
+        f = _f64(nufrac_low)
+        _check(self.L.kspace_gpu_set_hybrid(self.h, int(enabled), vcrit_frac, nu_crit_time, _pd(f)), "set_hybrid")
+
+    def omega_nu_single(self, a, i):
+        v = _d()
+        _check(self.L.kspace_gpu_omega_nu_single(self.h, a, i, C.byref(v)), "omega_nu_single")
+        return v.value
+
+    def omegag(self, a):
+        v = _d()
+        _check(self.L.kspace_gpu_omega_g(self.h, a, C.byref(v)), "get_omegag")
+        return v.value
+
+    def background_info(self):
+        rc, kb = _d(), _d()
+        deg = (C.c_int * 3)()
+        nfl = np.zeros(3)
+        _check(self.L.kspace_gpu_background_info(self.h, C.byref(rc), C.byref(kb), deg, _pd(nfl)),
+               "background_info")
+        return dict(rhocrit=rc.value, kBtnu=kb.value, deg=list(deg), nufrac_low=nfl)
+
+    def fslength(self, logai, logaf, light):
+        """fslength (delta_tot_table.c:394-407) of arrays of intervals, on the device."""
+        a = np.atleast_1d(_f64(logai))
+        b = np.atleast_1d(_f64(logaf))
+        out = np.zeros(len(a))
+        _check(self.L.kspace_gpu_fslength(self.h, _pd(a), _pd(b), len(a), light, _pd(out)), "fslength")
+        return out
 
     # ---- table (allocate_kspace_memory, interface_common.c:77-102)
     def alloc_table(self, nk_alloc, TimeTransfer, TimeMax, Omega0, UnitTime_in_s, UnitLength_in_cm):
@@ -323,6 +372,28 @@ class KspaceNeutrinos:
                "get_delta_nu_update")
         return out
 
+    def delta_tot_init(self, keff, P_cdm_sqrt, Time):
+        k = _f64(keff)
+        d = _f64(P_cdm_sqrt)
+        _check(self.L.kspace_gpu_delta_tot_init(self.h, len(k), _pd(k), _pd(d), Time), "delta_tot_init")
+
+    def get_delta_nu(self, a, wavenum, mnu):
+        k = _f64(wavenum)
+        out = np.zeros(len(k))
+        _check(self.L.kspace_gpu_get_delta_nu(self.h, a, len(k), _pd(k), _pd(out), mnu), "get_delta_nu")
+        return out
+
+    def get_delta_nu_combined(self, a, wavenum):
+        k = _f64(wavenum)
+        out = np.zeros(len(k))
+        _check(self.L.kspace_gpu_get_delta_nu_combined(self.h, a, len(k), _pd(k), _pd(out)), "get_delta_nu_combined")
+        return out
+
+    def update_delta_tot(self, a, P_cdm_sqrt, delta_nu, overwrite):
+        d = _f64(P_cdm_sqrt)
+        n = _f64(delta_nu)
+        _check(self.L.kspace_gpu_update_delta_tot(self.h, a, _pd(d), _pd(n), int(overwrite)), "update_delta_tot")
+
     def compute_neutrino_power_from_cdm(self, Time, keff, P_cdm, Nmodes):
         k = _f64(keff)
         p = _f64(P_cdm)
@@ -376,14 +447,23 @@ class KspaceNeutrinos:
             _check(self.L.kspace_gpu_set_jmass(self.h, _pd(m)), "set_jmass")
 
     def diff_forward(self, Time, BoxSize, grid_in, grid_out, pmgrid, pnu_out, store_intervals=True):
+        """One differentiable step; returns its generation (for diff_backward)."""
         _check(self.L.kspace_gpu_diff_forward(self.h, Time, BoxSize, grid_in.data_ptr(), grid_out.data_ptr(),
                                               pmgrid, pnu_out.data_ptr(), int(store_intervals)), "diff_forward")
+        g = C.c_longlong()
+        _check(self.L.kspace_gpu_diff_generation(self.h, C.byref(g)), "diff_generation")
+        return g.value
 
-    def diff_backward(self, gbar_out, grid_in, pnu_bar, gbar_in, Dbar, recompute=False):
+    def diff_backward(self, gbar_out, grid_in, pnu_bar, gbar_in, Dbar, recompute=False, generation=None):
+        """Adjoint of the forward of that generation (default: the last forward)."""
+        if generation is None:
+            g = C.c_longlong()
+            _check(self.L.kspace_gpu_diff_generation(self.h, C.byref(g)), "diff_generation")
+            generation = g.value
         mbar = np.zeros(3)
         _check(self.L.kspace_gpu_diff_backward(self.h, gbar_out.data_ptr(), grid_in.data_ptr(), pnu_bar.data_ptr(),
                                                gbar_in.data_ptr(), Dbar.data_ptr() if Dbar is not None else None,
-                                               _pd(mbar), int(recompute)), "diff_backward")
+                                               _pd(mbar), int(recompute), generation), "diff_backward")
         return mbar
 
     # ---- diagnostics
@@ -413,6 +493,24 @@ class KspaceNeutrinos:
 
     def launch_count(self):
         return int(self.L.kspace_gpu_launch_count(self.h))
+
+
+def special_j(x, qc=-1.0, nufrac_low=0.0, device_ctx=None):
+    """specialJ (delta_tot_table.c:457-463) of an array on the device."""
+    L = load_library()
+    xx = np.atleast_1d(_f64(x))
+    out = np.zeros(len(xx))
+    _check(L.kspace_gpu_special_j(device_ctx, _pd(xx), len(xx), qc, nufrac_low, _pd(out)), "specialJ")
+    return out
+
+
+def nufrac_low(qc, device_ctx=None):
+    """nufrac_low (omega_nu_single.c:214-228) of an array on the device."""
+    L = load_library()
+    q = np.atleast_1d(_f64(qc))
+    out = np.zeros(len(q))
+    _check(L.kspace_gpu_nufrac_low(device_ctx, _pd(q), len(q), _pd(out)), "nufrac_low")
+    return out
 
 
 def _buf_ptr(x):

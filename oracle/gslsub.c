@@ -74,7 +74,7 @@ void gsl_interp_accel_free(gsl_interp_accel *a) { free(a); }
 gsl_interp *gsl_interp_alloc(const gsl_interp_type *T, size_t n)
 {
     if (n < T->min_size) {
-        gslsub_error("insufficient number of points for interpolation type", __FILE__, __LINE__, GSL_EINVAL);
+        gslsub_error("too few knots for this interpolant", __FILE__, __LINE__, GSL_EINVAL);
         return NULL;
     }
     gsl_interp *p = (gsl_interp *)calloc(1, sizeof(gsl_interp));
@@ -131,12 +131,12 @@ int gsl_interp_init(gsl_interp *interp, const double xa[], const double ya[], si
 {
     size_t i;
     if (size != interp->size) {
-        gslsub_error("data must match size of interpolation object", __FILE__, __LINE__, GSL_EINVAL);
+        gslsub_error("knot count differs from the allocated interpolant", __FILE__, __LINE__, GSL_EINVAL);
         return GSL_EINVAL;
     }
     for (i = 1; i < size; i++) {
         if (!(xa[i - 1] < xa[i])) {
-            gslsub_error("x values must be strictly increasing", __FILE__, __LINE__, GSL_EINVAL);
+            gslsub_error("knots are not in strictly ascending order", __FILE__, __LINE__, GSL_EINVAL);
             return GSL_EINVAL;
         }
     }
@@ -165,7 +165,7 @@ double gsl_interp_eval(const gsl_interp *interp, const double xa[], const double
                        gsl_interp_accel *a)
 {
     if (x < interp->xmin || x > interp->xmax) {
-        gslsub_error("interpolation error", __FILE__, __LINE__, GSL_EDOM);
+        gslsub_error("query outside the knot range", __FILE__, __LINE__, GSL_EDOM);
         return NAN;
     }
     const size_t i = find_segment(xa, interp->size, x);
@@ -234,7 +234,7 @@ static void gk61(const gsl_function *f, double a, double b, double *result, doub
 gsl_integration_workspace *gsl_integration_workspace_alloc(size_t n)
 {
     if (n == 0) {
-        gslsub_error("workspace length n must be positive integer", __FILE__, __LINE__, GSL_EDOM);
+        gslsub_error("integration workspace needs at least one interval", __FILE__, __LINE__, GSL_EDOM);
         return NULL;
     }
     gsl_integration_workspace *w = (gsl_integration_workspace *)calloc(1, sizeof(*w));
@@ -305,15 +305,15 @@ int gsl_integration_qag(const gsl_function *f, double a, double b, double epsabs
     *result = 0;
     *abserr = 0;
     if (key != GSL_INTEG_GAUSS61) {
-        gslsub_error("only the 61-point rule is provided by this subset", __FILE__, __LINE__, GSL_EINVAL);
+        gslsub_error("this subset has the 61-point rule only", __FILE__, __LINE__, GSL_EINVAL);
         return GSL_EINVAL;
     }
     if (limit > w->limit) {
-        gslsub_error("iteration limit exceeds available workspace", __FILE__, __LINE__, GSL_EINVAL);
+        gslsub_error("subdivision limit larger than the workspace", __FILE__, __LINE__, GSL_EINVAL);
         return GSL_EINVAL;
     }
     if (epsabs <= 0 && (epsrel < 50 * DBL_EPSILON || epsrel < 0.5e-28)) {
-        gslsub_error("tolerance cannot be achieved with given epsabs and epsrel", __FILE__, __LINE__, GSL_EBADTOL);
+        gslsub_error("requested tolerances are unreachable (epsabs <= 0 and epsrel too small)", __FILE__, __LINE__, GSL_EBADTOL);
         return GSL_EBADTOL;
     }
     g_total_qag_calls++;
@@ -333,7 +333,7 @@ int gsl_integration_qag(const gsl_function *f, double a, double b, double epsabs
     if (err0 <= round_off && err0 > tol) {
         *result = res0;
         *abserr = err0;
-        gslsub_error("cannot reach tolerance because of roundoff error on first attempt", __FILE__, __LINE__, GSL_EROUND);
+        gslsub_error("first rule evaluation already dominated by rounding: tolerance unreachable", __FILE__, __LINE__, GSL_EROUND);
         return GSL_EROUND;
     } else if ((err0 <= tol && err0 != rasc0) || err0 == 0.0) {
         *result = res0;
@@ -342,7 +342,7 @@ int gsl_integration_qag(const gsl_function *f, double a, double b, double epsabs
     } else if (limit == 1) {
         *result = res0;
         *abserr = err0;
-        gslsub_error("a maximum of one iteration was insufficient", __FILE__, __LINE__, GSL_EMAXITER);
+        gslsub_error("tolerance not met and the subdivision limit is one", __FILE__, __LINE__, GSL_EMAXITER);
         return GSL_EMAXITER;
     }
     area = res0;
@@ -399,14 +399,14 @@ int gsl_integration_qag(const gsl_function *f, double a, double b, double epsabs
     if (errsum <= tol)
         return GSL_SUCCESS;
     if (error_type == 2) {
-        gslsub_error("roundoff error prevents tolerance from being achieved", __FILE__, __LINE__, GSL_EROUND);
+        gslsub_error("rounding errors grew too large to meet the tolerance", __FILE__, __LINE__, GSL_EROUND);
         return GSL_EROUND;
     }
     if (error_type == 3) {
-        gslsub_error("bad integrand behavior found in the integration interval", __FILE__, __LINE__, GSL_ESING);
+        gslsub_error("integrand too irregular: an interval became too narrow to split", __FILE__, __LINE__, GSL_ESING);
         return GSL_ESING;
     }
-    gslsub_error("maximum number of subdivisions reached", __FILE__, __LINE__, GSL_EMAXITER);
+    gslsub_error("subdivision limit reached before the tolerance was met", __FILE__, __LINE__, GSL_EMAXITER);
     return GSL_EMAXITER;
 }
 

@@ -234,6 +234,10 @@ int ref_add_nu_power_to_rhogrid(double Time, double BoxSize, fftw_complex *grid,
 {
     GUARDED(add_nu_power_to_rhogrid(Time, BoxSize, grid, pmgrid, slab0, nslab, MPI_COMM_WORLD));
 }
+int ref_compute_total_power_spectrum(double Time, double BoxSize, fftw_complex *grid, int pmgrid, int slab0, int nslab)
+{
+    GUARDED(compute_total_power_spectrum(Time, BoxSize, grid, pmgrid, slab0, nslab, MPI_COMM_WORLD));
+}
 int ref_compute_neutrino_power_from_cdm(double Time, const double *keff, const double *P, const long *Nmodes, int nk,
                                         double *logk_out, double *ratio_out, double *norm_out, int *nbins_out)
 {

@@ -183,14 +183,15 @@ class StepRef:
             res.append(float(np.sum(wb * (out - f["out"]) * (out + f["out"]))) + dE)
         return (res[0] - res[1]) / (2 * h)
 
-    def fd_mass(self, x, D, mJ, wb, f, rel=1e-6):
+    def fd_mass(self, x, D, mJ, wb, f, rel=1e-6, i=0):
+        """d L / d (mass of mass state i inside J)."""
         a2u = self._a2u(x)
         m0 = np.asarray(mJ, dtype=np.float64)
-        h = rel * m0[0]
+        h = rel * m0[i]
         res = []
         for sgn in (1, -1):
             mm = m0.copy()
-            mm[0] += sgn * h
+            mm[i] += sgn * h
             out = np.maximum(self.dnu(f["dc"], D, mm), 0)
             dE, _ = self._dE(a2u, f["su"], (out - f["out"]) / f["dc"])
             res.append(float(np.sum(wb * (out - f["out"]) * (out + f["out"]))) + dE)

@@ -15,6 +15,8 @@ ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 ORACLE_DIR = os.path.join(ROOT, "oracle")
 ORACLE_SO = os.path.join(ORACLE_DIR, "liboracle.so")
 REF_SO = os.path.join(ORACLE_DIR, "_ref", "libkspace_ref.so")
+# the same sources built with -DKSPACE_NEUTRINOS_2 (the Gadget-2 neutrino-run switch)
+REF_NU2_SO = os.path.join(ORACLE_DIR, "_ref", "libkspace_ref_nu2.so")
 
 d = C.c_double
 i32 = C.c_int
@@ -31,8 +33,8 @@ def _p(a, ct=C.c_double):
 def build_oracle():
     """Build liboracle.so (and the reference build when its sources are present)."""
     subprocess.run(["make", "-s", "-C", ORACLE_DIR], check=True)
-    if os.path.isdir("/root/reference") and not os.path.exists(REF_SO):
-        subprocess.run(["make", "-s", "-C", ORACLE_DIR, "ref"], check=True)
+    if not os.path.exists(REF_SO):
+        subprocess.run(["make", "-s", "-C", ORACLE_DIR, "ref-if-present"], check=True)
 
 
 def _sig(lib, name, res, args):
@@ -224,16 +226,17 @@ class Oracle:
 
 
 class RefLib:
-    """The unmodified reference C (oracle/_ref/libkspace_ref.so)."""
-    _lib = None
+    """The unmodified reference C (oracle/_ref/libkspace_ref.so, or another build of the
+    same sources given by path)."""
+    _libs = {}
 
     @staticmethod
-    def available():
-        return os.path.exists(REF_SO)
+    def available(path=REF_SO):
+        return os.path.exists(path)
 
-    def __init__(self):
-        if RefLib._lib is None:
-            L = C.CDLL(REF_SO)
+    def __init__(self, path=REF_SO):
+        if path not in RefLib._libs:
+            L = C.CDLL(path)
             _sig(L, "ref_omnu_new", vp, [])
             _sig(L, "ref_omnu_free", None, [vp])
             _sig(L, "ref_init_omega_nu", i32, [vp, PD, d, d, d])
@@ -283,6 +286,7 @@ class RefLib:
             _sig(L, "ref_OmegaNu_nopart", d, [d])
             _sig(L, "ref_allocate_kspace_memory", i32, [i32, d, d, d, d, C.c_char_p, d])
             _sig(L, "ref_add_nu_power_to_rhogrid", i32, [d, d, vp, i32, i32, i32])
+            _sig(L, "ref_compute_total_power_spectrum", i32, [d, d, vp, i32, i32, i32])
             _sig(L, "ref_compute_neutrino_power_from_cdm", i32,
                  [d, PD, PD, C.POINTER(C.c_long), i32, PD, PD, PD, PI])
             _sig(L, "ref_save_nu_state", i32, [C.c_char_p])
@@ -295,8 +299,8 @@ class RefLib:
             _sig(L, "ref_set_hubble_global", None, [d, d, d, i32, d, d])
             _sig(L, "ref_set_verbose", None, [i32])
             _sig(L, "ref_last_terminate_message", C.c_char_p, [])
-            RefLib._lib = L
-        self.L = RefLib._lib
+            RefLib._libs[path] = L
+        self.L = RefLib._libs[path]
 
     def omnu(self, MNu, a0=0.01, h=0.7, tcmb0=2.7255):
         o = self.L.ref_omnu_new()

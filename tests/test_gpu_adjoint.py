@@ -33,18 +33,19 @@ def setup(oracle, gpu, N, nb, Na, masses, seed=0):
     return c, ref, k, a
 
 
-def gpu_grads(k, c, a, wb, recompute):
+def gpu_grads(k, c, a, wb, recompute, mass_device="cpu"):
     import torch
     from autograd import NeutrinoStep
     step = NeutrinoStep(k, c["scalefact"], a, c["L"], recompute=recompute)
     grid = torch.as_tensor(c["grid"]).cuda().requires_grad_(True)
     hist = torch.as_tensor(c["delta_tot"]).cuda().requires_grad_(True)
-    m = torch.tensor(c["MNu"], dtype=torch.float64, requires_grad=True)
+    m = torch.tensor(c["MNu"], dtype=torch.float64, device=mass_device, requires_grad=True)
     out, pnu = step(grid, hist, m)
     w = torch.as_tensor(wb).cuda()
     loss = (w * pnu).sum() + 0.5 * torch.view_as_real(out).pow(2).sum()
     loss.backward()
-    return (grid.grad.detach().cpu().numpy(), hist.grad.detach().cpu().numpy(), m.grad.detach().numpy(),
+    assert m.grad.device == m.device
+    return (grid.grad.detach().cpu().numpy(), hist.grad.detach().cpu().numpy(), m.grad.detach().cpu().numpy(),
             out.detach().cpu().numpy(), pnu.detach().cpu().numpy())
 
 
@@ -94,4 +95,43 @@ def test_gradients(gpu, oracle, N, nb, Na):
     assert np.array_equal(xg2, xg)
     assert np.max(np.abs(Dg2 - Dg)) <= 1e-14 * np.max(np.abs(Dg))
     assert abs(mg2[0] - mg[0]) <= 1e-14 * abs(mg[0])
+    k.close()
+
+
+def test_mass_gradient_three_mass_states(gpu, oracle):
+    """Non-degenerate masses (0.02, 0.03, 0.06 eV: three mass states): the gradient with
+    respect to each mass against the FP64 reference adjoint and central differences,
+    with the masses on the GPU."""
+    c, ref, k, a = setup(oracle, gpu, 64, 48, 24, (0.02, 0.03, 0.06), seed=5)
+    wb = np.random.default_rng(7).random(c["nk"])
+    xg, Dg, mg, _, _ = gpu_grads(k, c, a, wb, recompute=False, mass_device="cuda")
+    x = c["grid"].astype(np.complex128)
+    mJ = np.array(c["MNu"])
+    adj = ref.adjoint(x, c["delta_tot"], mJ, wb)
+    for i in range(3):
+        assert abs(mg[i] / adj["mbar"][i] - 1) < 1e-5, (i, mg[i], adj["mbar"][i])
+        fd = ref.fd_mass(x, c["delta_tot"], mJ, wb, adj["f"], i=i)
+        assert abs(fd / mg[i] - 1) < 1e-5, (i, fd, mg[i])
+    k.close()
+
+
+def test_second_forward_before_backward_is_refused(gpu, oracle):
+    """The adjoint reads the state the last forward left in the instance: a backward
+    whose forward was followed by another one is refused (KSPACE_ERR_ORDER) rather than
+    computed from the second step."""
+    import torch
+    from autograd import NeutrinoStep
+    c, ref, k, a = setup(oracle, gpu, 32, 32, 10, (0.1, 0.1, 0.1))
+    step = NeutrinoStep(k, c["scalefact"], a, c["L"])
+    grid = torch.as_tensor(c["grid"]).cuda().requires_grad_(True)
+    hist = torch.as_tensor(c["delta_tot"]).cuda()
+    m = torch.tensor(c["MNu"], dtype=torch.float64)
+    out1, p1 = step(grid, hist, m)
+    out2, p2 = step(grid, hist * 1.01, m)
+    with pytest.raises(gpu.KspaceError) as e:
+        out1.abs().pow(2).sum().backward()
+    assert e.value.code == 10003
+    # the latest forward's backward still works
+    out2.abs().pow(2).sum().backward()
+    assert torch.isfinite(torch.view_as_real(grid.grad)).all()
     k.close()

@@ -33,7 +33,8 @@ def test_pm_harness_matches_oracle(gpu, oracle, tmp_path):
     pkg = os.path.join(ROOT, "kspace-neutrinos_gb300")
     subprocess.run(["gcc", "-O2", "-I" + os.path.join(ROOT, "include"), "-I" + os.path.join(ROOT, "oracle", "shim"),
                     "-o", exe, os.path.join(ROOT, "tests", "dropin", "pm_harness.c"),
-                    os.path.join(pkg, "dropin", "kspace_dropin.c"), "-L" + pkg, "-lkspace_gb300",
+                    os.path.join(pkg, "dropin", "kspace_dropin.c"),
+                    os.path.join(pkg, "dropin", "kspace_delta_tot_table.c"), "-L" + pkg, "-lkspace_gb300",
                     "-Wl,-rpath," + pkg, "-lm"], check=True)
     tf = str(tmp_path / "transfer.dat")
     sf_path = str(tmp_path / "state.txt")

@@ -66,8 +66,10 @@ def test_integrator_step(gpu, oracle, cfg):
     k.close()
 
 
-@pytest.mark.parametrize("N,nb,Na", [(16, 16, 6), (32, 32, 12), (64, 48, 24)])
+@pytest.mark.parametrize("N,nb,Na", [(16, 16, 6), (32, 32, 12), (64, 48, 24), (128, 128, 32)])
 def test_full_step(gpu, oracle, N, nb, Na):
+    """(128, 128, 32) is the small plain-method configuration: N=128 grid, 128 bins, a
+    32-row history to a=0.5, 3 x 0.1 eV."""
     import torch
     c = cases.make_case(N, nb, Na, 0.5, (0.1, 0.1, 0.1))
     bg, s = cases.oracle_state(oracle, c)

@@ -41,6 +41,13 @@ def test_noalloc_matches_total_powerspectrum(gpu, N, nb):
     assert st == 0, st
     p = _power_from_sums(out.cpu().numpy(), nb, count_full)
     assert np.max(np.abs(p / power - 1)) <= 1e-12
+    # warmed up: a further call takes no device memory (free memory unchanged)
+    torch.cuda.synchronize()
+    free0, _ = torch.cuda.mem_get_info()
+    st = L.kspace_gpu_bin_power_noalloc(N, grid.data_ptr(), nb, 0, N, out.data_ptr(), None)
+    torch.cuda.synchronize()
+    free1, _ = torch.cuda.mem_get_info()
+    assert st == 0 and free1 == free0, (free0, free1)
     # beyond the fixed scratch: refused, nothing launched
     sums = np.zeros(5001)
     assert L.kspace_gpu_bin_power_noalloc(N, grid.data_ptr(), 5000, 0, N, sums.ctypes.data, None) == 10002
