@@ -3,15 +3,18 @@
 
 One "step" = add_nu_power_to_rhogrid on a synthetic r2c grid: bin the grid into the
 power spectrum (K1), advance delta_nu over the stored delta_tot history (K2), multiply
-every mode by the neutrino correction (K3).  Default workload: N=512 grid
-(512x512x257 complex64), 256 log k bins, 256-row history from a=0.01 to a=1.0,
-3 degenerate 0.1 eV neutrinos, box 512 Mpc/h.
+every mode by the neutrino correction (K3).  Default workload: the precision
+configuration, an N=1024 grid (1024x1024x513 complex64, 4.3 GB), 512 log k bins, a
+512-row history from a=0.01 to a=1.0, three neutrino mass states of 0.02, 0.03 and
+0.06 eV, box 512 Mpc/h.  The N=512 configuration (512x512x257, 256 bins, 256-row
+history, 3 x 0.1 eV) is measured too and reported under "n512".
 
   python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gb300|reference]
 
 Prints one JSON line.  value = grid modes processed per second (whole job) with the
 grid resident in HBM; e2e = the same through the C ABI with the grid in pinned host
-memory (host->device and device->host copies inside the timed region).
+memory (host->device and device->host copies inside the timed region), beside the
+plain copy bandwidth of the host link.
 """
 import argparse
 import json
@@ -158,6 +161,29 @@ class ClockSampler:
                 "reasons": sorted(reasons), "samples": len(sm)}
 
 
+_HOST_GRIDS = {}
+
+
+def host_grid(N, L, seed):
+    """The seeded numpy grid, generated once per process (4.3 GB at N=1024)."""
+    key = (N, L, seed)
+    if key not in _HOST_GRIDS:
+        _HOST_GRIDS.clear()
+        _HOST_GRIDS[key] = W.make_grid(N, L, seed=seed)
+    return _HOST_GRIDS[key]
+
+
+def bench_config(cfg):
+    """The workload description printed by both arms (the same dict)."""
+    N = cfg["N"]
+    gbytes = 8 * N * N * (N // 2 + 1)
+    return {"workload": cfg["name"], "N": N, "nbins": cfg["nbins"], "history_rows": cfg["Na"],
+            "masses_eV": list(cfg["MNu"]), "box_mpc_h": cfg["L"], "grid_bytes": gbytes,
+            "l2": ("grid (%.0f MB) larger than L2 (129 MB): no flush" % (gbytes / 1e6)) if gbytes >= 160e6 else
+                  ("grid (%.0f MB) smaller than L2 (129 MB): L2 flushed (256 MB write) before each separately "
+                   "timed step" % (gbytes / 1e6))}
+
+
 def setup_workload(cfg, device_grid=True, seed=0):
     N, nb, L = cfg["N"], cfg["nbins"], cfg["L"]
     count, keff_grid = W.geometry(N, nb)
@@ -179,6 +205,76 @@ def step_times(cfg, w, steps):
     by 0.001 (provisional row dropped), so each timed step does the same work."""
     a0 = cfg["a_end"] + 0.01
     return [a0 + 0.001 * i for i in range(steps)]
+
+
+def plain_steps(k, cfg, grid, slab0, nslab, stream, a_list, warmup, steps, world=1):
+    """Device-timed steps with the grid resident in HBM: returns (seconds, stage ms [4],
+    launches per step).  A grid smaller than L2 is timed step by step after an L2 flush."""
+    import torch
+    N, L = cfg["N"], cfg["L"]
+    for i in range(warmup):
+        k.add_nu_power_to_rhogrid(a_list[i], L, grid, N, slab0, nslab)
+    torch.cuda.synchronize()
+    k.set_profiling(True)
+    launches0 = k.launch_count()
+    stage = np.zeros(4)
+    ev0 = torch.cuda.Event(enable_timing=True)
+    ev1 = torch.cuda.Event(enable_timing=True)
+    if world > 1:
+        import torch.distributed as dist
+        dist.barrier()
+    torch.cuda.synchronize()
+    bytes_grid = 8 * grid.numel()
+    flush = torch.empty(32 * 1024 * 1024, dtype=torch.float64, device="cuda") if bytes_grid < 160e6 else None
+    if flush is None:
+        ev0.record(stream)
+        for i in range(steps):
+            k.add_nu_power_to_rhogrid(a_list[warmup + i], L, grid, N, slab0, nslab)
+            stage += np.array(k.stage_times())
+        ev1.record(stream)
+        torch.cuda.synchronize()
+        t_dev = ev0.elapsed_time(ev1) / 1e3
+    else:
+        t_dev = 0.0
+        for i in range(steps):
+            with torch.cuda.stream(stream):
+                flush.zero_()
+            ev0.record(stream)
+            k.add_nu_power_to_rhogrid(a_list[warmup + i], L, grid, N, slab0, nslab)
+            ev1.record(stream)
+            torch.cuda.synchronize()
+            t_dev += ev0.elapsed_time(ev1) / 1e3
+            stage += np.array(k.stage_times())
+    launches = (k.launch_count() - launches0) / steps
+    k.set_profiling(False)
+    return t_dev, stage / steps, launches
+
+
+def link_bandwidth(nbytes, reps=3):
+    """Plain pinned-memory copies of nbytes each way over the host link (cudaMemcpyAsync
+    through torch), best of reps: the ceiling of an end-to-end step that moves the grid
+    up and back."""
+    import torch
+    h = torch.empty(nbytes // 4, dtype=torch.float32, pin_memory=True)
+    d = torch.empty(nbytes // 4, dtype=torch.float32, device="cuda")
+    ev0 = torch.cuda.Event(enable_timing=True)
+    ev1 = torch.cuda.Event(enable_timing=True)
+    best_up, best_down = 1e30, 1e30
+    for _ in range(reps):
+        torch.cuda.synchronize()
+        ev0.record()
+        d.copy_(h, non_blocking=True)
+        ev1.record()
+        torch.cuda.synchronize()
+        best_up = min(best_up, ev0.elapsed_time(ev1) / 1e3)
+        ev0.record()
+        h.copy_(d, non_blocking=True)
+        ev1.record()
+        torch.cuda.synchronize()
+        best_down = min(best_down, ev0.elapsed_time(ev1) / 1e3)
+    del h, d
+    return {"h2d_gbs": nbytes / best_up / 1e9, "d2h_gbs": nbytes / best_down / 1e9,
+            "up_and_down_ms": 1e3 * (best_up + best_down)}
 
 
 def run_gb300(args, cfg):
@@ -217,54 +313,20 @@ def run_gb300(args, cfg):
     G = nslab * N * nz
     bytes_grid = 8 * G
     a_list = step_times(cfg, None, nsteps)
-    # warm-up (includes the integrator initialisation and one committed row)
-    for i in range(args.warmup):
-        k.add_nu_power_to_rhogrid(a_list[i], L, grid, N, slab0, nslab)
-    torch.cuda.synchronize()
-    k.set_profiling(True)
-    launches0 = k.launch_count()
-    stage = np.zeros(4)
-    ev0 = torch.cuda.Event(enable_timing=True)
-    ev1 = torch.cuda.Event(enable_timing=True)
-    if world > 1:
-        dist.barrier()
-    torch.cuda.synchronize()
-    # A grid smaller than L2 (129 MB) would stay cached between steps: then each step is
-    # timed on its own, after a write of a 256 MB buffer flushes L2 (outside the timing).
-    flush = torch.empty(32 * 1024 * 1024, dtype=torch.float64, device="cuda") if bytes_grid < 160e6 else None
     with clock_sampler(local) as clk:
-        if flush is None:
-            ev0.record(stream)
-            for i in range(args.steps):
-                k.add_nu_power_to_rhogrid(a_list[args.warmup + i], L, grid, N, slab0, nslab)
-                stage += np.array(k.stage_times())
-            ev1.record(stream)
-            torch.cuda.synchronize()
-            t_dev = ev0.elapsed_time(ev1) / 1e3
-        else:
-            t_dev = 0.0
-            for i in range(args.steps):
-                with torch.cuda.stream(stream):
-                    flush.zero_()
-                ev0.record(stream)
-                k.add_nu_power_to_rhogrid(a_list[args.warmup + i], L, grid, N, slab0, nslab)
-                ev1.record(stream)
-                torch.cuda.synchronize()
-                t_dev += ev0.elapsed_time(ev1) / 1e3
-                stage += np.array(k.stage_times())
-    launches = k.launch_count() - launches0
+        t_dev, stage, launches = plain_steps(k, cfg, grid, slab0, nslab, stream, a_list, args.warmup, args.steps,
+                                             world)
     if world > 1:
         tt = torch.tensor([t_dev], device="cuda")
         dist.all_reduce(tt, op=dist.ReduceOp.MAX)
         t_dev = float(tt.item())
     ms_per_step = 1e3 * t_dev / args.steps
-    value = world * G * args.steps / t_dev if world > 1 else G * args.steps / t_dev
-    if world > 1:
-        value = N * N * nz * args.steps / t_dev
-    k.set_profiling(False)
+    value = N * N * nz * args.steps / t_dev
     # e2e through the C ABI with host buffers (pinned)
     host = torch.empty((nslab, N, nz), dtype=torch.complex64, pin_memory=True)
     host.copy_(grid.cpu())
+    del grid
+    torch.cuda.empty_cache()
     a_e2e = [a_list[-1] + 0.001 * (i + 1) for i in range(args.warmup + args.steps)]
     for i in range(args.warmup):
         k.add_nu_power_to_rhogrid(a_e2e[i], L, host.numpy(), N, slab0, nslab)
@@ -277,10 +339,12 @@ def run_gb300(args, cfg):
         tt = torch.tensor([t_e2e], device="cuda")
         dist.all_reduce(tt, op=dist.ReduceOp.MAX)
         t_e2e = float(tt.item())
-    e2e_value = (N * N * nz if world > 1 else G) * args.steps / t_e2e
+    e2e_value = N * N * nz * args.steps / t_e2e
+    del host
+    link = link_bandwidth(bytes_grid) if rank == 0 else None
     # roofline of the dominant grid kernel
     hbm, peak_kind = peaks()
-    k1_ms, k2_ms, k3_ms = stage[0] / args.steps, stage[1] / args.steps, stage[2] / args.steps
+    k1_ms, k2_ms, k3_ms = stage[0], stage[1], stage[2]
     k1_gbs = bytes_grid / (k1_ms * 1e-3) / 1e9 if k1_ms > 0 else None
     k3_gbs = 2 * bytes_grid / (k3_ms * 1e-3) / 1e9 if k3_ms > 0 else None
     tma = int(os.environ.get("KSPACE_GPU_TMA", "5"))
@@ -293,11 +357,13 @@ def run_gb300(args, cfg):
     traffic, traffic_note = None, None
     try:
         with open(os.path.join(ROOT, "profiles", "traffic.json")) as f:
-            traffic = json.load(f).get(dom["kernel"].split()[0])
-        if traffic is not None and bytes_grid != 538968064:
-            # captured on the N=512 grid; DRAM bytes scale with the grid
-            traffic = traffic * bytes_grid / 538968064
-            traffic_note = "ncu capture at N=512 scaled by the grid size"
+            tj = json.load(f)
+        ref_bytes = tj.get("captured_grid_bytes", 538968064)
+        traffic = tj.get(dom["kernel"].split()[0])
+        if traffic is not None and bytes_grid != ref_bytes:
+            # captured on a smaller grid; DRAM bytes scale with the grid
+            traffic = traffic * bytes_grid / ref_bytes
+            traffic_note = "ncu capture at %d grid bytes scaled by the grid size" % ref_bytes
     except Exception:
         pass
     res = {
@@ -305,34 +371,65 @@ def run_gb300(args, cfg):
         "warmup": args.warmup, "ms_per_step": ms_per_step, "higher_is_better": True,
         "scaling": "strong" if world > 1 else "weak", "vs_baseline": None, "dtype": "c64 grid / f64 integrator",
         "data": "synthetic (seeded Gaussian modes with the configured P(k); no dataset)",
-        "config": {"workload": cfg["name"], "N": N, "nbins": nb, "history_rows": cfg["Na"],
-                   "masses_eV": list(cfg["MNu"]), "box_mpc_h": L, "grid_bytes": bytes_grid,
-                   "l2": ("grid (%.0f MB) larger than L2 (129 MB): no flush" % (bytes_grid / 1e6)) if flush is None
-                   else ("grid (%.0f MB) smaller than L2 (129 MB): L2 flushed (256 MB write) before each "
-                         "separately timed step" % (bytes_grid / 1e6)),
-                   "parallelism": "slabs" if world > 1 else "single GPU"},
+        "config": bench_config(cfg),
+        "parallelism": "slabs over %d ranks" % world if world > 1 else "single GPU",
         "hbm_gbs_step": 3 * bytes_grid / (ms_per_step * 1e-3) / 1e9,
-        "stage_ms": {"binning_K1": k1_ms, "integrator_K2": k2_ms, "correction_K3": k3_ms},
+        "hbm_frac_step": 3 * bytes_grid / (ms_per_step * 1e-3) / 1e9 / hbm,
+        "stage_ms": {"binning_K1": k1_ms, "integrator_K2": k2_ms, "correction_K3": k3_ms, "whole_call": stage[3]},
         "stage_gbs": {"K1": k1_gbs, "K3": k3_gbs},
+        "stage_frac": {"K1": (k1_gbs / hbm) if k1_gbs else None, "K3": (k3_gbs / hbm) if k3_gbs else None},
         "roofline": {"bound": "hbm", "kernel": dom["kernel"], "achieved": dom["gbs"], "peak": hbm,
                      "peak_kind": peak_kind, "unit": "GB/s", "frac": (dom["gbs"] / hbm) if dom["gbs"] else None,
                      "traffic": traffic, "traffic_note": traffic_note, "algorithmic_bytes_per_launch": dom["bytes"]},
         "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": bytes_grid,
                 "d2h_bytes_per_step": bytes_grid, "ms_per_step": 1e3 * t_e2e / args.steps},
-        "gpu_launches": launches,
+        "gpu_launches": int(round(launches * args.steps)),
         "clocks": clk.summary(),
     }
+    if link:
+        res["e2e"]["link"] = link
+        res["e2e"]["frac_of_link"] = link["up_and_down_ms"] / res["e2e"]["ms_per_step"]
     if rank == 0 and not args.no_cpu_baseline:
         res["cpu_baseline"] = cpu_baseline(cfg, wl, args.cpu_threads, sample_steps=1)
-    if rank == 0 and world == 1 and not args.no_extras:
-        mx, tot = k.qag_stats()
-        res["integrator"] = {"qag_max_intervals": mx, "qag_total_intervals_last_step": tot}
-        res["fwd_adjoint"] = fwd_adjoint()
-        res["errors"] = errors_vs_oracle(cfg, wl, args.cpu_threads or os.cpu_count() or 1)
     k.close()
+    if rank == 0 and world == 1 and not args.no_extras:
+        res["errors"] = errors_vs_oracle(cfg, wl, args.cpu_threads or os.cpu_count() or 1)
+        if cfg["name"] != "cfg1_n512":
+            res["n512"] = n512_steps(args)
+        res["fwd_adjoint"] = fwd_adjoint()
     if world > 1:
         dist.destroy_process_group()
     return res if rank == 0 else None
+
+
+def n512_steps(args):
+    """The N=512 configuration (512x512x257, 256 bins, 256-row history, 3 x 0.1 eV):
+    device-timed steps and stage times, as for the main workload."""
+    import torch
+    import kspace_gpu as kg
+    cfg = dict(W.CONFIGS["cfg1_n512"])
+    cfg["name"] = "cfg1_n512"
+    N, nb, L = cfg["N"], cfg["nbins"], cfg["L"]
+    wl = setup_workload(cfg)
+    nsteps = args.warmup + args.steps
+    k = kg.make_instance(cfg["MNu"], 0.01, 0.7, 0.3, nb, time_max(cfg, 2 * nsteps + 2), wl["logk"], wl["T"],
+                         UnitLength_in_cm=W.UNIT_LENGTH_MPC)
+    k.set_nu_state(wl["sf"], wl["dt"])
+    stream = torch.cuda.Stream()
+    k.set_stream(stream)
+    grid = W.make_grid_torch(N, L, seed=1, device="cuda")
+    with clock_sampler(0) as clk:
+        t_dev, stage, _ = plain_steps(k, cfg, grid, 0, N, stream, step_times(cfg, None, nsteps), args.warmup,
+                                      args.steps)
+    k.close()
+    hbm, _ = peaks()
+    gb = 8 * grid.numel()
+    ms = 1e3 * t_dev / args.steps
+    return {"config": bench_config(cfg), "value": N * N * (N // 2 + 1) / (ms * 1e-3), "unit": UNIT,
+            "ms_per_step": ms, "hbm_frac_step": 3 * gb / (ms * 1e-3) / 1e9 / hbm,
+            "stage_ms": {"binning_K1": stage[0], "integrator_K2": stage[1], "correction_K3": stage[2]},
+            "stage_frac": {"K1": gb / (stage[0] * 1e-3) / 1e9 / hbm, "K3": 2 * gb / (stage[2] * 1e-3) / 1e9 / hbm},
+            "clocks": clk.summary()}
 
 
 def fwd_adjoint(steps=5, warmup=3):
@@ -400,9 +497,10 @@ def fwd_adjoint(steps=5, warmup=3):
 
 
 def errors_vs_oracle(cfg, wl, threads):
-    """One step on a fresh instance and the oracle (the reference algorithm in C), and on
-    the all-FP64 oracle (double |F|^2 and window, exact delta_nu integral): max relative
-    differences of P(k), delta_nu/delta_cdm and the corrected grid."""
+    """One step on a fresh instance and on the oracle (the reference algorithm in C), and
+    on the all-FP64 oracle (double |F|^2 and window, exact delta_nu integral): per-bin
+    mode counts (bit for bit) and max relative differences of P(k), delta_nu,
+    delta_nu/delta_cdm and the corrected grid."""
     import torch
     import kspace_gpu as kg
     sys.path.insert(0, os.path.join(ROOT, "tests"))
@@ -411,16 +509,21 @@ def errors_vs_oracle(cfg, wl, threads):
     N, nb, L = cfg["N"], cfg["nbins"], cfg["L"]
     TimeMax = time_max(cfg, 4)
     a = cfg["a_end"] + 0.01
-    g = W.make_grid(N, L, seed=1)
+    g = host_grid(N, L, 1)
     k = kg.make_instance(cfg["MNu"], 0.01, 0.7, 0.3, nb, TimeMax, wl["logk"], wl["T"],
                          UnitLength_in_cm=W.UNIT_LENGTH_MPC)
     k.set_nu_state(wl["sf"], wl["dt"])
     gd = torch.as_tensor(g).cuda()
+    nk_g, p_g, c_g, _ = k.total_powerspectrum(N, gd, nb)
     k.add_nu_power_to_rhogrid(a, L, gd, N)
     lc = k.last_correction()
     gg = gd.cpu().numpy()
+    del gd
     k.close()
-    res = {}
+    torch.cuda.empty_cache()
+    nk_o, p_o, c_o, _ = O.total_powerspectrum(g, N, nb, nthreads=threads)
+    res = {"counts_equal": bool(nk_g == nk_o and np.array_equal(c_g, c_o)), "nk": int(nk_o),
+           "modes_binned": int(c_o.sum())}
     for name, exact in (("vs_reference_oracle", 0), ("vs_fp64_oracle", 1)):
         bg = O.bg(cfg["MNu"], a0=0.01, h=0.7, Omega0=0.3, UnitTime_in_s=W.UNIT_TIME)
         s = O.state(bg, nb, 0.01, TimeMax, Omega0=0.3, UnitTime_in_s=W.UNIT_TIME, UnitLength_in_cm=W.UNIT_LENGTH_MPC)
@@ -434,11 +537,15 @@ def errors_vs_oracle(cfg, wl, threads):
             st, out = O.add_nu_power_to_rhogrid(s, a, L, go, N, nthreads=threads, nk_alloc=nb)
         assert st == 0, st
         m = out["ratio"] != 0
+        dnu_g = lc["ratio"] * lc["dcdm"]
         res[name] = {
             "P_k": float(np.max(np.abs((lc["dcdm"] / out["dcdm"]) ** 2 - 1))),
+            "delta_nu": float(np.max(np.abs(dnu_g[m] / out["dnu"][m] - 1))),
             "delta_nu_over_delta_cdm": float(np.max(np.abs(lc["ratio"][m] / out["ratio"][m] - 1))),
             "corrected_grid": float(np.max(np.abs(gg - go) / np.maximum(np.abs(go), 1e-30))),
         }
+        del go
+    res["bars"] = {"counts": "bit-exact", "P_k": 1e-6, "corrected_grid": 1e-6, "delta_nu": 1e-10}
     return res
 
 
@@ -454,7 +561,7 @@ def cpu_baseline(cfg, wl, threads, sample_steps=1):
     s = O.state(bg, nb, 0.01, TimeMax, Omega0=0.3, UnitTime_in_s=W.UNIT_TIME, UnitLength_in_cm=W.UNIT_LENGTH_MPC)
     O.set_transfer(s, wl["logk"], wl["T"])
     assert O.set_nu_state(s, wl["sf"], wl["dt"]) == 0
-    g = W.make_grid(N, L, seed=1)
+    g = host_grid(N, L, 1).copy()
     # initialisation call (delta_nu_last) is not timed, as on the GPU
     st, _ = O.add_nu_power_to_rhogrid(s, cfg["a_end"] + 0.01, L, g, N, nthreads=threads, nk_alloc=nb)
     assert st == 0, st
@@ -490,7 +597,7 @@ def run_reference(args, cfg):
     s = O.state(bg, nb, 0.01, TimeMax, Omega0=0.3, UnitTime_in_s=W.UNIT_TIME, UnitLength_in_cm=W.UNIT_LENGTH_MPC)
     O.set_transfer(s, wl["logk"], wl["T"])
     assert O.set_nu_state(s, wl["sf"], wl["dt"]) == 0
-    g = W.make_grid(N, L, seed=1)
+    g = host_grid(N, L, 1).copy()
     a_list = step_times(cfg, None, nsteps)
     for i in range(args.warmup):
         st, _ = O.add_nu_power_to_rhogrid(s, a_list[i], L, g, N, nthreads=threads, nk_alloc=nb)
@@ -504,7 +611,7 @@ def run_reference(args, cfg):
     return {"metric": METRIC, "value": v, "unit": UNIT, "impl": "reference", "n_gpus": 0, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": 1e3 * dt / args.steps, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "c64 grid / f64 integrator", "data": "synthetic",
-            "config": {"workload": cfg["name"], "N": N, "nbins": nb, "history_rows": cfg["Na"]},
+            "config": bench_config(cfg),
             "cpu_baseline": {"value": v, "unit": UNIT, "cores": threads, "kind": "port",
                              "sample": "the full N=%d step, %d timed steps, binning/multiply split over %d threads "
                                        "as MPI slabs" % (N, args.steps, threads)},
@@ -659,7 +766,7 @@ def main():
     ap.add_argument("--steps", type=int, default=20)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
-    ap.add_argument("--config", default="cfg1_n512", choices=sorted(W.CONFIGS) + ["batch"])
+    ap.add_argument("--config", default="cfg2_n1024", choices=sorted(W.CONFIGS) + ["batch"])
     ap.add_argument("--batch-m", type=int, default=W.BATCH["M"])
     ap.add_argument("--autotune", type=int, default=1)
     ap.add_argument("--cpu-threads", type=int, default=0)

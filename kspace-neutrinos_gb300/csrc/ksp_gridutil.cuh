@@ -2,6 +2,7 @@
 // correction K3 and their adjoints): mode coordinates, the exact log bin of integer
 // k^2, the CIC window factor and the correction interpolation.
 #pragma once
+#include <stdlib.h>
 #include <cuda.h>
 #include <cuda_runtime.h>
 #include <stdint.h>
@@ -48,6 +49,7 @@ struct GridArgs {
     float c1;       // binsperunit * ln2 / 2: bin ~ c1 * log2(k^2)
     float lnscale;  // log(2 pi / BoxSize) (K3)
     FastDiv fd_nz, fd_N;
+    int first_wait;  // poll limit of the binning pass's first bounded wait (2^22; a test may shorten it)
 };
 
 __device__ __forceinline__ int kval(int n, int N) { return n <= N / 2 ? n : n - N; }
@@ -426,6 +428,20 @@ __device__ __forceinline__ float corr_delta(int k2, const GridArgs& g, const Cor
 }
 
 
+// The poll limit of the first bounded wait of the default binning pass: 2^22, or, for
+// the test of the expiry path (a wait that runs out ends the pass with
+// KSPACE_ERR_TIMEOUT after draining its copies, with no fault), the value of
+// KSPACE_GPU_TEST_FIRST_WAIT read once per process.
+inline int first_wait_limit() {
+    static int v = -1;
+    if (v < 0) {
+        const char* e = getenv("KSPACE_GPU_TEST_FIRST_WAIT");
+        v = e ? atoi(e) : (1 << 22);
+        if (v < 0) v = 0;
+    }
+    return v;
+}
+
 inline GridArgs make_grid_args(const GridGeom& g, int nk, float lnscale) {
     GridArgs a;
     a.N = g.N;
@@ -440,6 +456,7 @@ inline GridArgs make_grid_args(const GridGeom& g, int nk, float lnscale) {
     a.lnscale = lnscale;
     a.fd_nz = make_fastdiv((uint32_t)a.nz);
     a.fd_N = make_fastdiv((uint32_t)g.N);
+    a.first_wait = first_wait_limit();
     return a;
 }
 

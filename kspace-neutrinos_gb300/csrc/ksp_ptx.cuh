@@ -36,6 +36,12 @@ __device__ __forceinline__ bool mbar_wait_bounded(uint64_t* bar, unsigned phase)
         if (mbar_try_wait(bar, phase)) return true;
     return false;
 }
+// the same with a given poll limit (0: report expiry without polling)
+__device__ __forceinline__ bool mbar_wait_bounded_n(uint64_t* bar, unsigned phase, int limit) {
+    for (int it = 0; it < limit; it++)
+        if (mbar_try_wait(bar, phase)) return true;
+    return false;
+}
 // global -> shared bulk copy; 16-byte aligned addresses, size a multiple of 16
 __device__ __forceinline__ void bulk_g2s(void* dst, const void* src, unsigned bytes, uint64_t* bar) {
     asm volatile(

@@ -753,7 +753,7 @@ __global__ void __launch_bounds__(WARPS * 32)
     int s = 0;
     unsigned phase = 0;
     for (; k < my_n; k++) {
-        const bool got = ptx::mbar_wait_bounded(&gbar[s], phase);
+        const bool got = ptx::mbar_wait_bounded_n(&gbar[s], phase, k == 0 ? g.first_wait : (1 << 22));
         const bool all = T.wg == 1 ? __all_sync(kFull, got) : named_and(1 + grp, gsz, got);
         if (!all) {
             ok = false;

@@ -133,3 +133,52 @@ def test_nan_correction_factor_gives_5(gpu):
     ratio[nk // 2] = 0.01
     k.apply_delta_pow(c["L"], g, 16, nb, logk, ratio, 0.01)  # still usable
     k.close()
+
+
+_EXPIRED_WAIT = r"""
+import ctypes, os, sys
+sys.path[:0] = [sys.argv[1], sys.argv[1] + "/tests", sys.argv[1] + "/kspace-neutrinos_gb300"]
+import torch
+import cases, kspace_gpu as kg
+import workloads as W
+rt = None
+for name in ("libcudart.so.13", "libcudart.so"):
+    try:
+        rt = ctypes.CDLL(name)
+        break
+    except OSError:
+        pass
+N, nb = 64, 48
+g = torch.as_tensor(W.make_grid(N, seed=4)).cuda()
+k = kg.KspaceNeutrinos()
+k.init_omega_nu((0.1, 0.1, 0.1), 0.01, 0.7)
+k.alloc_table(nb, 0.01, 1.0, 0.3, cases.UT, cases.UL)
+try:
+    k.total_powerspectrum(N, g, nb)
+    print("status 0")
+except kg.KspaceError as e:
+    print("status", e.code)
+torch.cuda.synchronize()
+print("pending", rt.cudaPeekAtLastError() if rt else 0)
+x = torch.arange(10, device="cuda", dtype=torch.float64).sum().item()  # the device is still usable
+print("after", x)
+k.close()
+"""
+
+
+def test_expired_bounded_wait_returns_timeout(gpu):
+    """The first bounded wait of the binning pass given no polls (KSPACE_GPU_TEST_FIRST_WAIT=0,
+    read once per process): the wait reports expiry, the warps stop, the group's leader
+    waits (bounded) for its copies still in flight, the kernel returns and the call gives
+    KSPACE_ERR_TIMEOUT (10005); no trap, no pending CUDA error, the device stays usable."""
+    import os
+    import subprocess
+    import sys
+    root = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+    env = dict(os.environ, KSPACE_GPU_TEST_FIRST_WAIT="0")
+    r = subprocess.run([sys.executable, "-c", _EXPIRED_WAIT, root], capture_output=True, text=True, timeout=600,
+                       env=env)
+    assert r.returncode == 0, r.stderr[-2000:]
+    assert "status 10005" in r.stdout, r.stdout
+    assert "pending 0" in r.stdout, r.stdout
+    assert "after 45.0" in r.stdout, r.stdout
