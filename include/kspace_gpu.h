@@ -271,8 +271,8 @@ int kspace_gpu_batch_last_ms(kspace_batch *batch, float *ms);
  * or device) receives sum w |F|^2 W^4 per bin, not normalised, and |F(0)|^2 last;
  * divide by |F(0)|^2 and the mode counts for the power.  grid: device memory.  Limits:
  * nrbins <= 4096, dims <= 4096 (KSPACE_ERR_ARG beyond).  Scratch is one fixed device
- * array shared by all calls: overlapping calls race.  The first call on a device sets
- * up the scratch address; make it before any stream capture.  cuda_stream: a
+ * array shared by all calls: overlapping calls race.  The first call on a device looks
+ * up the scratch address.  cuda_stream: a
  * cudaStream_t (NULL = the default stream); returns after the sums are in bin_sums. */
 int kspace_gpu_bin_power_noalloc(int dims, const void *grid, int nrbins, int startslab, int nslab,
                                  double *bin_sums, void *cuda_stream);

@@ -404,8 +404,8 @@ __global__ void __launch_bounds__(128) k_dnu_adj(IntegratorDev I, DnuAdjArgs A, 
     uint64_t* mybar = bars + warp;
     gk61_fill(N, threadIdx.x, blockDim.x);
     for (int i = threadIdx.x; i < Na; i += blockDim.x) knots[i] = I.scalefact[i];
-    if (lane == 0) asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(ptx::smem_u32(mybar)) : "memory");
-    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    if (lane == 0) ptx::mbar_init(mybar, 1);
+    ptx::mbar_init_fence();
     __syncthreads();
     const Background* B = I.B;
     const StepScalars& S = *I.sc;
@@ -429,21 +429,10 @@ __global__ void __launch_bounds__(128) k_dnu_adj(IntegratorDev I, DnuAdjArgs A, 
         if (integrate) {
             __syncwarp();
             if (lane == 0) {
-                asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
-                asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(ptx::smem_u32(mybar)),
-                             "r"(Na > 2 ? 2 * row_bytes : row_bytes)
-                             : "memory");
-                asm volatile(
-                    "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
-                        ptx::smem_u32(row)),
-                    "l"(I.dtot + (size_t)ik * I.ld), "r"(row_bytes), "r"(ptx::smem_u32(mybar))
-                    : "memory");
-                if (Na > 2)
-                    asm volatile(
-                        "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
-                            ptx::smem_u32(rc)),
-                        "l"(I.coef + (size_t)ik * I.ld), "r"(row_bytes), "r"(ptx::smem_u32(mybar))
-                        : "memory");
+                ptx::fence_async_smem();
+                ptx::mbar_expect_tx(mybar, Na > 2 ? 2 * row_bytes : row_bytes);
+                ptx::bulk_g2s(row, I.dtot + (size_t)ik * I.ld, row_bytes, mybar);
+                if (Na > 2) ptx::bulk_g2s(rc, I.coef + (size_t)ik * I.ld, row_bytes, mybar);
             }
             for (int i = lane; i < Na; i += 32) { ybar[i] = 0.0; cbar[i] = 0.0; }
             const bool got = __all_sync(0xffffffffu, ptx::mbar_wait_bounded(mybar, phase));  // warp-uniform
@@ -590,8 +579,8 @@ __global__ void __launch_bounds__(128) k_dnu_adj_blk(IntegratorDev I, DnuAdjArgs
     uint64_t* bar = reinterpret_cast<uint64_t*>(sm + off);
     gk61_fill(N, tid, blockDim.x);
     for (int i = tid; i < Na; i += blockDim.x) knots[i] = I.scalefact[i];
-    if (tid == 0) asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(ptx::smem_u32(bar)) : "memory");
-    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    if (tid == 0) ptx::mbar_init(bar, 1);
+    ptx::mbar_init_fence();
     __syncthreads();
     const Background* B = I.B;
     const StepScalars& S = *I.sc;
@@ -615,21 +604,10 @@ __global__ void __launch_bounds__(128) k_dnu_adj_blk(IntegratorDev I, DnuAdjArgs
         if (integrate) {
             __syncthreads();  // the previous task's readers of row / rc / wy / wc are done
             if (tid == 0) {
-                asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
-                asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(ptx::smem_u32(bar)),
-                             "r"(Na > 2 ? 2 * row_bytes : row_bytes)
-                             : "memory");
-                asm volatile(
-                    "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
-                        ptx::smem_u32(row)),
-                    "l"(I.dtot + (size_t)ik * I.ld), "r"(row_bytes), "r"(ptx::smem_u32(bar))
-                    : "memory");
-                if (Na > 2)
-                    asm volatile(
-                        "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
-                            ptx::smem_u32(rc)),
-                        "l"(I.coef + (size_t)ik * I.ld), "r"(row_bytes), "r"(ptx::smem_u32(bar))
-                        : "memory");
+                ptx::fence_async_smem();
+                ptx::mbar_expect_tx(bar, Na > 2 ? 2 * row_bytes : row_bytes);
+                ptx::bulk_g2s(row, I.dtot + (size_t)ik * I.ld, row_bytes, bar);
+                if (Na > 2) ptx::bulk_g2s(rc, I.coef + (size_t)ik * I.ld, row_bytes, bar);
             }
             for (int i = tid; i < nw * I.ld; i += blockDim.x) {
                 wy[i] = 0.0;

@@ -79,7 +79,7 @@ k_bin_power_tma(const __grid_constant__ CUtensorMap tmap, GridArgs g, const int*
     if (tid == 0) {
         s_abort = 0;
         for (int st = 0; st < STAGES; st++) ptx::mbar_init(&bars[st], 1);
-        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+        ptx::mbar_init_fence();
     }
     __syncthreads();
     const int my_n = blockIdx.x < ntiles ? (ntiles - 1 - blockIdx.x) / gridDim.x + 1 : 0;
@@ -251,7 +251,7 @@ k_correct_tma(const __grid_constant__ CUtensorMap tmap, GridArgs g, const int* _
     if (tid == 0) {
         s_abort = 0;
         for (int st = 0; st < STAGES; st++) ptx::mbar_init(&bars[st], 1);
-        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+        ptx::mbar_init_fence();
     }
     __syncthreads();
     CorrSmem T{s_thr, s_cmap, s_tab, s_tab + g.nk, s_tab + 2 * g.nk};

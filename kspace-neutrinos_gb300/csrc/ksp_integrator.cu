@@ -451,7 +451,7 @@ __global__ void __launch_bounds__(128) k_dnu_qag(IntegratorDev I, int nk, int Na
     gk61_fill(N, threadIdx.x, blockDim.x);
     for (int i = threadIdx.x; i < Na; i += blockDim.x) knots[i] = I.scalefact[i];
     if (lane == 0) ptx::mbar_init(mybar, 1);
-    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    ptx::mbar_init_fence();
     __syncthreads();
 
     const Background* B = I.B;
@@ -482,7 +482,7 @@ __global__ void __launch_bounds__(128) k_dnu_qag(IntegratorDev I, int nk, int Na
             __syncwarp();
             if (lane == 0) {
                 // order this warp's earlier generic reads of the buffers before the async writes
-                asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+                ptx::fence_async_smem();
                 ptx::mbar_expect_tx(mybar, Na > 2 ? 2 * row_bytes : row_bytes);
                 ptx::bulk_g2s(row, I.dtot + (size_t)ik * I.ld, row_bytes, mybar);
                 if (Na > 2) ptx::bulk_g2s(rc, I.coef + (size_t)ik * I.ld, row_bytes, mybar);
@@ -569,7 +569,7 @@ __global__ void __launch_bounds__(SPEC ? 256 : 128, SPEC ? 2 : 4)
         const double mnu = B->mnu_J[mi];
         const bool integ = !S.skip_integral && Na > 1 && mnu / B->kBtnu > 0;
         if (integ) {
-            asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+            ptx::fence_async_smem();
             ptx::mbar_expect_tx(bar, Na > 2 ? 2 * row_bytes : row_bytes);
             ptx::bulk_g2s(row, I.dtot + (size_t)ik * I.ld, row_bytes, bar);
             if (Na > 2) ptx::bulk_g2s(rc, I.coef + (size_t)ik * I.ld, row_bytes, bar);
@@ -583,7 +583,7 @@ __global__ void __launch_bounds__(SPEC ? 256 : 128, SPEC ? 2 : 4)
     // the first task's copies are in flight while the block fills its tables
     if (tid == 0) {
         ptx::mbar_init(bar, 1);
-        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+        ptx::mbar_init_fence();
         if (blockIdx.x < ntask) start_task(blockIdx.x);
     }
     gk61_fill(N, tid, blockDim.x);

@@ -14,8 +14,7 @@
 // requests are refused with KSPACE_ERR_ARG and a message on stderr.  The scratch is
 // about 57 KB.  Calls share the scratch, so calls that overlap (from two host threads, or
 // queued on two streams at once) race; serialise them.  The first call on a device
-// looks up the scratch address (cudaGetSymbolAddress) with that device current; make
-// that first call before any stream capture begins.
+// looks up the scratch address (cudaGetSymbolAddress) with that device current.
 #include <cuda_runtime.h>
 #include <math.h>
 #include <stdio.h>
