@@ -151,6 +151,9 @@ CONFIGS = {
     "cfg1_n512": dict(N=512, nbins=256, Na=256, a_end=1.0, MNu=(0.1, 0.1, 0.1), L=512.0),
     "cfg2_n1024": dict(N=1024, nbins=512, Na=512, a_end=1.0, MNu=(0.02, 0.03, 0.06), L=512.0),
     "cfg3_n256": dict(N=256, nbins=128, Na=128, a_end=1.0, MNu=(0.05, 0.05, 0.05), L=512.0),
+    # a smaller grid with the N=1024 workload's kernel shapes (two warps per row-pair tile in
+    # the binning pass), for full ncu captures that stay within a few GB of device memory
+    "prof_n768": dict(N=768, nbins=384, Na=256, a_end=1.0, MNu=(0.02, 0.03, 0.06), L=512.0),
     # profiling case: grid larger than L2 (227 MB) but small enough for multi-pass captures
     "prof_n384": dict(N=384, nbins=192, Na=64, a_end=1.0, MNu=(0.1, 0.1, 0.1), L=512.0),
 }
