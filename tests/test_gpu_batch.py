@@ -1,4 +1,4 @@
-"""Batched integration against the single-instance path.
+"""Batched integration against the single-instance path and the oracle.
 
 Instances with different masses, cosmologies, history lengths and bin counts -- two of
 them bound to grids of different sizes -- are advanced together through the batch ABI
@@ -7,6 +7,8 @@ through kspace_gpu_get_delta_nu_update / kspace_gpu_add_nu_power_to_rhogrid.  Th
 calls mix committed rows, dropped provisional rows and the same-scale-factor shortcut.
 delta_nu must agree to 1e-12 relative (the bar for batching is 1e-10), the corrected
 grids to 1e-6.  A tuning run in between (dry steps) must leave every state unchanged.
+Three free instances (one, two and three mass states) are also driven through the
+oracle's get_delta_nu_update with the same inputs: delta_nu within 1e-10.
 """
 import math
 
@@ -55,7 +57,20 @@ def schedule(M):
     return calls
 
 
-def test_batch_matches_single_instances(gpu):
+def oracle_instance(oracle, p):
+    """The oracle state of instance p (the inputs build_instance gives the library)."""
+    ut = UL / 1e5
+    bg = oracle.bg(p["MNu"], a0=0.01, h=p["h"], Omega0=p["Omega0"], UnitTime_in_s=ut)
+    s = oracle.state(bg, p["nk"], 0.01, 0.01 + (p["Na"] + 20) / 100.0, Omega0=p["Omega0"], UnitTime_in_s=ut,
+                     UnitLength_in_cm=UL)
+    logk, T = W.transfer_table(float(sum(p["MNu"])))
+    oracle.set_transfer(s, logk, T)
+    sf, dt = W.history(p["k"], p["Na"], p["a_end"])
+    assert oracle.set_nu_state(s, sf, dt) == 0
+    return s
+
+
+def test_batch_matches_single_instances(gpu, oracle):
     import torch
     M = 18
     ps = make_params(M, seed=3)
@@ -78,6 +93,9 @@ def test_batch_matches_single_instances(gpu):
     keff_pool = np.concatenate([kph[i] for i in range(M) if i not in grid_N])
     dcdm0 = np.concatenate([np.sqrt(W.spectrum(kph[i])) for i in range(M) if i not in grid_N])
     calls = schedule(M)
+    oracle_ids = (2, 3, 5)  # one, three and two mass states
+    ostates = {i: oracle_instance(oracle, ps[i]) for i in oracle_ids}
+    worst_oracle = 0.0
     B.init(calls[0], nk, keff_pool, dcdm0)
     off = B.offsets
     assert list(B.nk[2:]) == [len(kph[i]) for i in range(2, M)]
@@ -118,6 +136,13 @@ def test_batch_matches_single_instances(gpu):
             assert np.array_equal(got == 0, ref == 0)
             worst = max(worst, err)
             assert err <= 1e-12, (ci, i, err)
+            if i in ostates:
+                st, ro = oracle.get_delta_nu_update(ostates[i], a[i], kph[i], dcdm[off[i]:off[i + 1]])
+                assert st == 0
+                nzo = np.abs(ro) > 0
+                eo = cases.rel_err(got[nzo], ro[nzo])
+                worst_oracle = max(worst_oracle, eo)
+                assert eo <= 1e-10, (ci, i, eo)
     # the twins' history tables equal the batch's
     for i in range(M):
         s1 = batch_insts[i].table_info()
@@ -129,7 +154,7 @@ def test_batch_matches_single_instances(gpu):
     B.close()
     for k in batch_insts + twins:
         k.close()
-    print("worst batch/single relative difference", worst)
+    print("worst batch/single relative difference", worst, "batch/oracle", worst_oracle)
 
 
 def test_batch_errors(gpu):
