@@ -808,9 +808,11 @@ void launch_integrator_rest(const IntegratorDev& I, int nk, int Na, int nspec, c
             if (nsm <= 0) nsm = 1;
         }
         // a block per task: 8 warps with look-ahead (split 8) below 4 tasks per SM, 4 warps
-        // without above (measured faster than a warp per task, split 1, up to the 1536
-        // tasks of 3 species x 512 bins)
-        const int split = qag_split > 0 ? qag_split : (ntask < 4 * nsm ? 8 : 4);
+        // without up to 6 tasks per SM, 2 warps from there (at 128 registers a thread, 4
+        // blocks of 4 warps fit an SM: 1221 tasks of 3 species x 407 bins take two waves
+        // of 4-warp blocks and one of 2-warp blocks, measured 0.211 against 0.223 ms; a
+        // warp per task, split 1, 0.231 ms)
+        const int split = qag_split > 0 ? qag_split : (ntask < 4 * nsm ? 8 : (ntask < 6 * nsm ? 4 : 2));
         const bool spec = split >= 8;
         const size_t bsmem = dnu_qag_blk_smem(I.ld, spec);
         if (split > 1 && bsmem <= 227 * 1024 - 256) {
