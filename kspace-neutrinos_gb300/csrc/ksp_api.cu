@@ -171,6 +171,7 @@ extern "C" int kspace_gpu_destroy(kspace_ctx* c) {
         cudaFree(g.g.thresh);
         cudaFree(g.g.w1);
         cudaFree(g.g.cmap);
+        if (g.g.runtab) cudaFree(g.g.runtab);
         cudaFree(g.count_d);
         cudaFree(g.ksum_d);
         cudaFree(g.compact_d);
@@ -1165,6 +1166,8 @@ static int get_geo(kspace_ctx* c, int N, int nrbins, Geo** out) {
     CK(cudaMemcpy(G.count_d, G.count.data(), sizeof(long long) * nrbins, cudaMemcpyHostToDevice));
     CK(cudaMemcpy(G.ksum_d, G.ksum.data(), sizeof(double) * nrbins, cudaMemcpyHostToDevice));
     if (G.nk) CK(cudaMemcpy(G.compact_d, G.compact.data(), sizeof(int) * G.nk, cudaMemcpyHostToDevice));
+    if (build_run_table(g, c->stream) < 0) return KSPACE_ERR_CUDA;
+    g_launches += g.runtab ? 1 : 0;
     c->geos[key] = G;
     *out = &c->geos[key];
     return KSPACE_OK;

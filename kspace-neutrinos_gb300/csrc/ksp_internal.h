@@ -527,7 +527,12 @@ struct GridGeom {
     float* w1;                      // device [N/2+1]: 1-D inverse CIC window (float)
     int* cmap;                      // device [nrbins]: bin -> compact index (-1 empty)
     float bin_c1;                   // binsperunit * ln2 / 2 (approximate bin estimate)
+    unsigned* runtab = nullptr;     // device run table of the binning pass (or null)
+    int run_Rp = 0;                 // its row length: runs of 17 modes per grid row, rounded up to 4
 };
+// the run table of a geometry (ksp_stream.cu): 0 built, 1 not applicable (2^15 bins or
+// more, or over 1 GiB), -1 error
+int build_run_table(GridGeom& g, cudaStream_t st);
 // histogram of weighted mode counts over integer k^2 for the slab range
 void launch_k2_histogram(int N, int slab0, int nslab, unsigned long long* hist, cudaStream_t st);
 // K1: per-bin sum of w |F|^2 W^4 (double), and |F(0)|^2 when slab0 == 0

@@ -170,6 +170,29 @@ __device__ __forceinline__ void bin_step_slots(float re, float im, float iwxy, f
     d += 2;
 }
 
+// The same step with the crossing read from the run's bit mask (the run table): no k^2,
+// no threshold load.
+template <bool EXACT>
+__device__ __forceinline__ void bin_step_bit(float re, float im, float iwxy, float2 w, bool c,
+                                             typename SpillOf<EXACT>::type*& sp, float& h, float& l) {
+    float phi, plo;
+    mode_value<EXACT>(re, im, iwxy, w, phi, plo);
+    sp += c ? 32 : 0;
+    const float h0 = c ? 0.f : h;
+    if constexpr (EXACT) {
+        const float l0 = c ? 0.f : l;
+        const float s = __fadd_rn(h0, phi);
+        const float bb = __fsub_rn(s, h0);
+        const float e = __fadd_rn(__fsub_rn(h0, __fsub_rn(s, bb)), __fsub_rn(phi, bb));
+        h = s;
+        l = __fadd_rn(l0, __fadd_rn(e, plo));
+        *sp = make_float2(h, l);
+    } else {
+        h = __fadd_rn(h0, phi);
+        *sp = h;
+    }
+}
+
 __device__ __forceinline__ void add_pair(float* H, float* L, int b, float hi, float lo) {
     if (hi != 0.f || lo != 0.f) pair_atomic_add(H, L, b, hi, lo);
 }
@@ -615,13 +638,15 @@ struct RowTiling {
     int tile_bytes;   // trows * nz * 8
     int stage_bytes;  // tile + read-past slack, 128-byte multiple
     int copies;       // copies of the CTA's bin totals: tile row r adds to copy r % copies
+    int Rp;           // run-table row length (R rounded up to 4), 0 without the run table
+    int tab_bytes;    // run-table rows at the start of a stage: trows * Rp * 4
 };
 
 // floats from one copy of the bin totals ({H[nrbins]}, {L[nrbins]}) to the next: 2 nrbins
 // padded to 16 modulo 32, so that a bin sits in opposite half-banks of neighbouring copies
 __host__ __device__ inline int totals_stride(int nrbins) { return 2 * nrbins + ((48 - (2 * nrbins) % 32) % 32); }
 
-inline RowTiling make_row_tiling(int nz) {
+inline RowTiling make_row_tiling(int nz, bool table) {
     RowTiling t;
     t.R = (nz + kRun - 1) / kRun;
     int pairs = 32 / (2 * t.R);
@@ -629,7 +654,9 @@ inline RowTiling make_row_tiling(int nz) {
     t.trows = 2 * pairs;
     t.wg = (t.trows * t.R + 31) / 32;
     t.tile_bytes = t.trows * nz * 8;
-    t.stage_bytes = (t.tile_bytes + kRun * 8 + 127) & ~127;
+    t.Rp = table ? (t.R + 3) & ~3 : 0;
+    t.tab_bytes = t.trows * t.Rp * 4;
+    t.stage_bytes = (t.tab_bytes + t.tile_bytes + kRun * 8 + 127) & ~127;
     t.copies = 1;
     return t;
 }
@@ -672,11 +699,34 @@ __device__ __forceinline__ bool named_and(int id, int nthreads, bool v) {
     return out != 0;
 }
 
-template <int WARPS, int STAGES, bool EXACT>
+// One tile into a stage: its rows and, with the run table, the table rows of each of its
+// row pairs (|kx|, min |ky|, then min |ky| + 1: one 16-byte aligned copy per pair), all on
+// one mbarrier.
+__device__ __forceinline__ void issue_row_tile(const GridArgs& g, const RowTiling& T, const unsigned* runtab,
+                                               const unsigned char* gsrc, unsigned char* dst, uint64_t* bar,
+                                               long long r0, long long nrows) {
+    const long long nr = nrows - r0 < T.trows ? nrows - r0 : T.trows;
+    const unsigned bytes = (unsigned)(nr * g.nz * 8);
+    const unsigned tbytes = (unsigned)((nr / 2) * 2 * T.Rp * 4);
+    ptx::mbar_expect_tx(bar, bytes + tbytes);
+    ptx::bulk_g2s(dst + T.tab_bytes, gsrc + r0 * g.nz * 8, bytes, bar);
+    for (int p = 0; 2 * p < nr && T.Rp; p++) {
+        const uint32_t row0 = (uint32_t)(r0 + 2 * p);
+        const uint32_t il = fdiv(row0, g.fd_N);
+        const int j0 = (int)(row0 - il * (uint32_t)g.N);
+        const int kx = kval(g.slab0 + (int)il, g.N), ky0 = kval(j0, g.N), ky1 = kval(j0 + 1, g.N);
+        const int ax = kx < 0 ? -kx : kx, ay0 = ky0 < 0 ? -ky0 : ky0, ay1 = ky1 < 0 ? -ky1 : ky1;
+        const int aymin = ay0 < ay1 ? ay0 : ay1;
+        ptx::bulk_g2s(dst + (size_t)p * 2 * T.Rp * 4, runtab + ((size_t)ax * (g.half + 1) + aymin) * T.Rp,
+                      (unsigned)(2 * T.Rp * 4), bar);
+    }
+}
+
+template <int WARPS, int STAGES, bool EXACT, bool TAB>
 __global__ void __launch_bounds__(WARPS * 32)
     k_bin_rows(GridArgs g, RowTiling T, const int* __restrict__ thresh, const float* __restrict__ w1g,
                const float* __restrict__ grid, double* bin_sum, double* F0sq, unsigned* status, long long ntiles,
-               long long nrows) {
+               long long nrows, const unsigned* __restrict__ runtab) {
     typedef typename SpillOf<EXACT>::type Spill;
     extern __shared__ unsigned char sm_raw[];
     __shared__ int s_gap;
@@ -741,13 +791,8 @@ __global__ void __launch_bounds__(WARPS * 32)
     const long long my_n = gg < ntiles ? (ntiles - 1 - gg) / TG + 1 : 0;
     const unsigned char* gsrc = reinterpret_cast<const unsigned char*>(grid);
     if (leader)
-        for (int s = 0; s < STAGES && s < my_n; s++) {
-            const long long t = gg + s * TG;
-            const long long r0 = t * T.trows;
-            const unsigned bytes = (unsigned)((nrows - r0 < T.trows ? nrows - r0 : T.trows) * g.nz * 8);
-            ptx::mbar_expect_tx(&gbar[s], bytes);
-            ptx::bulk_g2s(gstage + s * T.stage_bytes, gsrc + r0 * g.nz * 8, bytes, &gbar[s]);
-        }
+        for (int s = 0; s < STAGES && s < my_n; s++)
+            issue_row_tile(g, T, runtab, gsrc, gstage + s * T.stage_bytes, &gbar[s], (gg + s * TG) * T.trows, nrows);
     bool ok = true;
     long long k = 0;
     int s = 0;
@@ -759,17 +804,44 @@ __global__ void __launch_bounds__(WARPS * 32)
             ok = false;
             break;
         }
-        const unsigned char* tb = gstage + s * T.stage_bytes;
+        const unsigned char* tb = gstage + s * T.stage_bytes + T.tab_bytes;
         const long long pr64 = (gg + k * TG) * T.trows + row_t;
         const bool valid = lane_ok && pr64 < nrows;
         const int pr = (int)(valid ? pr64 : 0);
         const int il = (int)fdiv((uint32_t)pr, g.fd_N);
-        const int kx = kval(g.slab0 + il, g.N), ky = kval(pr - il * g.N, g.N);
+        const int jy = pr - il * g.N;
+        const int kx = kval(g.slab0 + il, g.N), ky = kval(jy, g.N);
         const int kxy2 = kx * kx + ky * ky;
         int k2 = kxy2 + z0 * z0;
         const float iwxy = __fmul_rn(s_wt[kx < 0 ? -kx : kx].x, s_wt[ky < 0 ? -ky : ky].x);
-        const bool fast = valid && k2 >= ksafe;
-        if (fast) {
+        unsigned e = 1u;
+        if (TAB && valid) {
+            // the run's table entry: b_start << 17 | crossing bits | slow bit (the pair's
+            // rows are |ky| ascending in the stage)
+            const int kyp = kval(row_t & 1 ? jy - 1 : jy + 1, g.N);
+            const int ay = ky < 0 ? -ky : ky, ayp = kyp < 0 ? -kyp : kyp;
+            const unsigned* et = reinterpret_cast<const unsigned*>(gstage + s * T.stage_bytes) +
+                                 (row_t >> 1) * 2 * T.Rp;
+            e = et[(ay < ayp ? 0 : T.Rp) + (run - row_t * T.R)];
+        }
+        const bool fast = TAB ? valid && (e & 1u) == 0 : valid && k2 >= ksafe;
+        if (TAB && fast) {
+            const int b = (int)(e >> 17);
+            Spill* sp = my_spill;
+            float h = 0.f, l = 0.f;
+            const float2* vp = reinterpret_cast<const float2*>(tb + lane_off);
+#pragma unroll
+            for (int i = 0; i < kRun; i++) {
+                const float2 v = vp[i];  // past the row end: weight 0 (table entries past nz)
+                bin_step_bit<EXACT>(v.x, v.y, iwxy, wz[i], i > 0 && ((e >> i) & 1u), sp, h, l);
+            }
+            const int nsp = (int)(sp - my_spill) >> 5;
+            for (int q = 0; q <= nsp; q++) {
+                const Spill v = my_spill[32 * q];
+                if constexpr (EXACT) add_pair(s_H, s_L, b + q, v.x, v.y);
+                else add_pair(s_H, s_L, b + q, v, 0.f);
+            }
+        } else if (fast) {
             const int b = bin_of(k2, g.c1, s_thr, g.nrbins);
             const int* tq = s_thr + b + 1;
             int tnext = *tq;
@@ -813,12 +885,9 @@ __global__ void __launch_bounds__(WARPS * 32)
         }
         if (T.wg == 1) __syncwarp();
         else named_sync(1 + grp, gsz);
-        if (leader && k + STAGES < my_n) {
-            const long long r0 = (gg + (k + STAGES) * TG) * T.trows;
-            const unsigned bytes = (unsigned)((nrows - r0 < T.trows ? nrows - r0 : T.trows) * g.nz * 8);
-            ptx::mbar_expect_tx(&gbar[s], bytes);
-            ptx::bulk_g2s(gstage + s * T.stage_bytes, gsrc + r0 * g.nz * 8, bytes, &gbar[s]);
-        }
+        if (leader && k + STAGES < my_n)
+            issue_row_tile(g, T, runtab, gsrc, gstage + s * T.stage_bytes, &gbar[s], (gg + (k + STAGES) * TG) * T.trows,
+                           nrows);
         if (++s == STAGES) {
             s = 0;
             phase ^= 1;
@@ -963,15 +1032,15 @@ int run_bin_stream(const GridGeom& g, const GridArgs& a, const float* grid, doub
     return cudaPeekAtLastError() == cudaSuccess ? 0 : -2;
 }
 
-template <int WARPS, int STAGES, bool EXACT>
+template <int WARPS, int STAGES, bool EXACT, bool TAB>
 int run_bin_rows(const GridGeom& g, const GridArgs& a, const float* grid, double* bin_sum, double* F0sq,
                  unsigned* status, cudaStream_t st) {
     if ((reinterpret_cast<uintptr_t>(grid) & 15) != 0) return -1;
-    RowTiling T = make_row_tiling(a.nz);
+    RowTiling T = make_row_tiling(a.nz, TAB);
     if (WARPS % T.wg != 0) return -1;
     const long long nrows = (long long)g.nslab * g.N;
     if (nrows <= 0) return -1;
-    auto kern = k_bin_rows<WARPS, STAGES, EXACT>;
+    auto kern = k_bin_rows<WARPS, STAGES, EXACT, TAB>;
     auto blocks_per_sm = [&](const RowTiling& t) -> int {
         const StreamPlan p = plan_bin_rows(WARPS, STAGES, g.nrbins, a.nz, EXACT, t);
         return p.total > (size_t)kMaxSmemPass ? 0 : resident_blocks(kern, WARPS * 32, p.total);
@@ -994,8 +1063,18 @@ int run_bin_rows(const GridGeom& g, const GridArgs& a, const float* grid, double
     long long n = (long long)sm_count_s() * per_sm;
     const long long need = (ntiles + groups - 1) / groups;
     if (n > need) n = need > 0 ? need : 1;
-    kern<<<(int)n, WARPS * 32, P.total, st>>>(a, T, g.thresh, g.w1, grid, bin_sum, F0sq, status, ntiles, nrows);
+    kern<<<(int)n, WARPS * 32, P.total, st>>>(a, T, g.thresh, g.w1, grid, bin_sum, F0sq, status, ntiles, nrows,
+                                              g.runtab);
     return cudaPeekAtLastError() == cudaSuccess ? 0 : -2;
+}
+
+// the exact variant reads bin crossings from the geometry's run table when it has one
+template <int WARPS, int STAGES, bool EXACT>
+int run_bin_rows_any(const GridGeom& g, const GridArgs& a, const float* grid, double* bin_sum, double* F0sq,
+                     unsigned* status, cudaStream_t st) {
+    if (EXACT && g.runtab && g.run_Rp == ((a.nz + kRun - 1) / kRun + 3) / 4 * 4)
+        return run_bin_rows<WARPS, STAGES, EXACT, EXACT>(g, a, grid, bin_sum, F0sq, status, st);
+    return run_bin_rows<WARPS, STAGES, EXACT, false>(g, a, grid, bin_sum, F0sq, status, st);
 }
 
 template <int WARPS, int STAGES>
@@ -1012,7 +1091,70 @@ int run_corr_stream(const GridArgs& a, float* grid, CorrTable corr, unsigned* st
     return cudaPeekAtLastError() == cudaSuccess ? 0 : -2;
 }
 
+// Run table of a geometry: for |kx|, |ky| in [0, N/2] and run r (modes z = 17r .. 17r+16
+// of a grid row), entry = b_start << 17 | bit i (i = 1..16) set where mode i opens the next
+// bin | bit 0 "slow".  Slow: the run holds the k = 0 mode (excluded, powerspectrum.c:65)
+// or skips a bin between two consecutive modes (low k, a bin narrower than one k^2 step).
+// Rows of Rp = R rounded up to 4 entries (16-byte rows); entries past R are slow.
+__global__ void k_run_table(const int* __restrict__ thr, int nrbins, float c1, int half, int nz, int R, int Rp,
+                            unsigned* __restrict__ tab) {
+    const long long n = (long long)(half + 1) * (half + 1) * Rp;
+    for (long long e = (long long)blockIdx.x * blockDim.x + threadIdx.x; e < n;
+         e += (long long)gridDim.x * blockDim.x) {
+        const int r = (int)(e % Rp);
+        const long long q = e / Rp;
+        if (r >= R) {
+            tab[e] = 1u;
+            continue;
+        }
+        const int ay = (int)(q % (half + 1)), ax = (int)(q / (half + 1));
+        const int kxy2 = ax * ax + ay * ay;
+        unsigned mask = 0;
+        int bprev = -1, bstart = 0;
+        bool slow = false;
+        for (int i = 0; i < kRun; i++) {
+            const int z = kRun * r + i;
+            if (z >= nz) break;
+            const int k2 = kxy2 + z * z;
+            if (k2 == 0) {
+                slow = true;
+                continue;
+            }
+            const int b = bin_of(k2, c1, thr, nrbins);
+            if (bprev < 0) {
+                bstart = b;
+            } else if (b != bprev) {
+                if (b - bprev > 1) slow = true;
+                mask |= 1u << i;
+            }
+            bprev = b;
+        }
+        tab[e] = ((unsigned)bstart << 17) | mask | (slow ? 1u : 0u);
+    }
+}
+
 }  // namespace
+
+int build_run_table(GridGeom& g, cudaStream_t st) {
+    g.runtab = nullptr;
+    g.run_Rp = 0;
+    const int half = g.N / 2, nz = half + 1;
+    const int R = (nz + kRun - 1) / kRun, Rp = (R + 3) & ~3;
+    const size_t n = (size_t)(half + 1) * (half + 1) * Rp;
+    if (g.nrbins >= (1 << 15) || n * sizeof(unsigned) > (size_t(1) << 30)) return 1;
+    unsigned* tab = nullptr;
+    if (cudaMalloc(&tab, n * sizeof(unsigned)) != cudaSuccess) return -1;
+    long long blocks = ((long long)n + 255) / 256;
+    if (blocks > 8LL * sm_count_s()) blocks = 8LL * sm_count_s();
+    k_run_table<<<(int)blocks, 256, 0, st>>>(g.thresh, g.nrbins, g.bin_c1, half, nz, R, Rp, tab);
+    if (cudaPeekAtLastError() != cudaSuccess) {
+        cudaFree(tab);
+        return -1;
+    }
+    g.runtab = tab;
+    g.run_Rp = Rp;
+    return 0;
+}
 
 int launch_bin_stream(const GridGeom& g, const GridArgs& a, const float* grid, double* bin_sum, double* F0sq,
                       unsigned* status, int warps, int stages, bool exact, cudaStream_t st) {
@@ -1032,12 +1174,12 @@ int launch_bin_rows(const GridGeom& g, const GridArgs& a, const float* grid, dou
     if (a.N >= 32768) return -1;
 #define KSP_BR(W, S)                                                                            \
     if (warps == W && stages == S)                                                              \
-        return exact ? run_bin_rows<W, S, true>(g, a, grid, bin_sum, F0sq, status, st)          \
-                     : run_bin_rows<W, S, false>(g, a, grid, bin_sum, F0sq, status, st);
+        return exact ? run_bin_rows_any<W, S, true>(g, a, grid, bin_sum, F0sq, status, st)      \
+                     : run_bin_rows_any<W, S, false>(g, a, grid, bin_sum, F0sq, status, st);
     KSP_BR(4, 2) KSP_BR(4, 3) KSP_BR(8, 2) KSP_BR(8, 3)
 #undef KSP_BR
-    return exact ? run_bin_rows<8, 2, true>(g, a, grid, bin_sum, F0sq, status, st)
-                 : run_bin_rows<8, 2, false>(g, a, grid, bin_sum, F0sq, status, st);
+    return exact ? run_bin_rows_any<8, 2, true>(g, a, grid, bin_sum, F0sq, status, st)
+                 : run_bin_rows_any<8, 2, false>(g, a, grid, bin_sum, F0sq, status, st);
 }
 
 int launch_correct_stream(const GridArgs& a, float* grid, CorrTable corr, unsigned* status, int warps, int stages,
