@@ -825,21 +825,36 @@ __global__ void __launch_bounds__(WARPS * 32)
             e = et[(ay < ayp ? 0 : T.Rp) + (run - row_t * T.R)];
         }
         const bool fast = TAB ? valid && (e & 1u) == 0 : valid && k2 >= ksafe;
-        if (TAB && fast) {
+        if constexpr (TAB) {
             const int b = (int)(e >> 17);
-            Spill* sp = my_spill;
-            float h = 0.f, l = 0.f;
-            const float2* vp = reinterpret_cast<const float2*>(tb + lane_off);
+            const int nsp = fast ? __popc(e & 0x1fffeu) : 0;  // the run's closed bins
+            if (fast) {
+                Spill* sp = my_spill;
+                float h = 0.f, l = 0.f;
+                const float2* vp = reinterpret_cast<const float2*>(tb + lane_off);
 #pragma unroll
-            for (int i = 0; i < kRun; i++) {
-                const float2 v = vp[i];  // past the row end: weight 0 (table entries past nz)
-                bin_step_bit<EXACT>(v.x, v.y, iwxy, wz[i], i > 0 && ((e >> i) & 1u), sp, h, l);
+                for (int i = 0; i < kRun; i++) {
+                    const float2 v = vp[i];  // past the row end: weight 0 (table entries past nz)
+                    bin_step_bit<EXACT>(v.x, v.y, iwxy, wz[i], i > 0 && ((e >> i) & 1u), sp, h, l);
+                }
             }
-            const int nsp = (int)(sp - my_spill) >> 5;
-            for (int q = 0; q <= nsp; q++) {
-                const Spill v = my_spill[32 * q];
-                if constexpr (EXACT) add_pair(s_H, s_L, b + q, v.x, v.y);
-                else add_pair(s_H, s_L, b + q, v, 0.f);
+            // The next lane's run continues this one along the row: where it starts in
+            // the bin this run ends in and has a later bin of its own, its first sum is
+            // added to this run's last one here, and that bin goes to the totals once.
+            const float2 first = fast ? my_spill[0] : make_float2(0.f, 0.f);
+            const int info = fast ? (row_t << 8) | (nsp + 1) : 0;  // row, items; 0: no run
+            const int nb_info = __shfl_down_sync(kFull, info, 1);
+            const int nb_b = __shfl_down_sync(kFull, b, 1);
+            const float nfx = __shfl_down_sync(kFull, first.x, 1), nfy = __shfl_down_sync(kFull, first.y, 1);
+            const bool take = fast && lane < 31 && (nb_info >> 8) == row_t && (nb_info & 255) >= 2 &&
+                              nb_b == b + nsp;
+            const bool given = __shfl_up_sync(kFull, take ? 1 : 0, 1) != 0 && lane > 0;
+            if (fast) {
+                for (int q = given ? 1 : 0; q <= nsp; q++) {
+                    Spill v = my_spill[32 * q];
+                    if (q == nsp && take) pair_add(v.x, v.y, nfx, nfy);
+                    add_pair(s_H, s_L, b + q, v.x, v.y);
+                }
             }
         } else if (fast) {
             const int b = bin_of(k2, g.c1, s_thr, g.nrbins);
