@@ -931,6 +931,320 @@ __global__ void __launch_bounds__(WARPS * 32)
     }
 }
 
+// ------------------------------------------------------------------ K1 over mirrored rows
+// The rows ky and -ky of a plane (grid rows j and N - j) hold, at every z, modes of the
+// same |k|, the same window factor and the same multiplicity: they fall in the same bins
+// at the same z.  So a lane takes one 17-mode run of both rows at once.  The two |F|^2
+// (each rounded in float as the reference forms it) are added exactly (Fast2Sum of the
+// larger and the smaller), and the pair goes through the window product, the crossing and
+// the compensated run sum once: the sum of the two double products the reference adds,
+// to float-pair precision.  Crossings come from the run table, as in k_bin_rows; a run
+// and its closed bins now cover 34 modes.
+// A tile is P consecutive |ky| = q of one plane (P = 32 / runs per row): rows q0..q0+P-1
+// (one copy) and their mirrors N-q (one copy, q descending).  q = 0 and q = N/2 are
+// their own mirrors: their lanes read the row twice and halve the run sums (exact).  A
+// copy starts at the 16-byte boundary at or below its first row and ends at the one at
+// or above its last row end (a row is 8 (N/2+1) bytes, so odd rows start 8 bytes past a
+// boundary).  Each warp owns a ring of two stages.
+constexpr int kMirrorTail = 144;  // zeroed bytes after a stage's rows (reads past the last row end)
+constexpr int kMirrorMaxWarps = 12;
+
+struct MirrorTiling {
+    int R;            // 17-mode runs per row
+    int P;            // |ky| values (row pairs) per tile
+    int Rp;           // run-table row length
+    int tpp;          // tiles per plane: ceil((N/2 + 1) / P)
+    FastDiv fd_tpp;
+    int tab_bytes;    // run-table rows of a tile, rounded to 16
+    int blk;          // bytes of the region one copy lands in: P rows + 16, rounded to 16
+    int stage_bytes;  // table rows | rows q | mirror rows | tail
+    int copies;       // copies of the CTA's bin totals: pair p adds to copy p % copies
+};
+
+inline MirrorTiling make_mirror_tiling(int nz) {
+    MirrorTiling t{};
+    t.R = (nz + kRun - 1) / kRun;
+    t.P = t.R <= 32 ? 32 / t.R : 0;
+    if (t.P > nz) t.P = nz;
+    t.Rp = (t.R + 3) & ~3;
+    t.tpp = t.P > 0 ? (nz + t.P - 1) / t.P : 0;
+    t.fd_tpp = make_fastdiv((uint32_t)(t.tpp > 0 ? t.tpp : 1));
+    t.tab_bytes = (t.P * t.Rp * 4 + 15) & ~15;
+    t.blk = (t.P * nz * 8 + 16 + 15) & ~15;
+    t.stage_bytes = (t.tab_bytes + 2 * t.blk + kMirrorTail + 127) & ~127;
+    t.copies = 1;
+    return t;
+}
+
+// stage rings (two stages per warp) | mbarriers | per-warp spill slots | float-pair bin
+// totals (T.copies copies) | thresholds | {w1[z], multiplicity} for z < nz + 17 (zero past nz)
+__host__ __device__ inline StreamPlan plan_bin_mirror(int warps, int nrbins, int nz, bool exact,
+                                                      const MirrorTiling& T) {
+    StreamPlan p{};
+    size_t o = 0;
+    p.stage_off = o;
+    o += (size_t)warps * 2 * T.stage_bytes;
+    p.bar_off = o;
+    o += sizeof(uint64_t) * (size_t)warps * 2;
+    o = (o + 15) & ~size_t(15);
+    p.spill_off = o;
+    o += (size_t)warps * kRun * 32 * (exact ? 8 : 4);
+    p.hist_off = o;
+    o += sizeof(float) * (size_t)totals_stride(nrbins) * T.copies;
+    p.thr_off = o;
+    o += sizeof(int) * (size_t)(nrbins + 1);
+    o = (o + 15) & ~size_t(15);
+    p.tab_off = o;
+    o += sizeof(float2) * (size_t)(nz + kRun);
+    p.total = o + 128;  // alignment slack
+    return p;
+}
+
+__device__ __forceinline__ float spill_hi(float2 v) { return v.x; }
+__device__ __forceinline__ float spill_lo(float2 v) { return v.y; }
+__device__ __forceinline__ float spill_hi(float v) { return v; }
+__device__ __forceinline__ float spill_lo(float) { return 0.f; }
+
+// One mode pair of a fast run (z of row q and of its mirror): close the current bin if
+// the run table marks a crossing, then add m (|F_a|^2 + |F_b|^2) inv^2 to the (new)
+// current bin.  m (0, 1 or 2) multiplies exactly inside the fused multiply-adds.
+template <bool EXACT>
+__device__ __forceinline__ void mirror_step(float2 a, float2 b, float iwxy, float wz, float m, bool c,
+                                            typename SpillOf<EXACT>::type*& sp, float& h, float& l) {
+    const float Fa = __fadd_rn(__fmul_rn(a.x, a.x), __fmul_rn(a.y, a.y));
+    const float Fb = __fadd_rn(__fmul_rn(b.x, b.x), __fmul_rn(b.y, b.y));
+    const float t = __fmul_rn(iwxy, wz);
+    const float inv = __fmul_rn(t, t);
+    const float fh = __fmul_rn(inv, inv);
+    sp += c ? 32 : 0;
+    const float h0 = c ? 0.f : h;
+    if constexpr (EXACT) {
+        const float mx = ptx::fmax_nan(Fa, Fb), mn = ptx::fmin_nan(Fa, Fb);
+        const float sh = __fadd_rn(mx, mn);
+        const float sl = __fsub_rn(mn, __fsub_rn(sh, mx));
+        const float fl = fmaf(inv, inv, -fh);
+        const float hi = __fmul_rn(sh, fh);
+        const float lo = fmaf(sh, fl, fmaf(sl, fh, fmaf(sh, fh, -hi)));
+        const float l0 = c ? 0.f : l;
+        const float s = fmaf(hi, m, h0);
+        const float bb = __fsub_rn(s, h0);
+        const float e = __fadd_rn(__fsub_rn(h0, __fsub_rn(s, bb)), fmaf(hi, m, -bb));
+        h = s;
+        l = __fadd_rn(l0, fmaf(lo, m, e));
+        *sp = make_float2(h, l);
+    } else {
+        h = fmaf(__fmul_rn(__fadd_rn(Fa, Fb), fh), m, h0);
+        *sp = h;
+    }
+}
+
+// Tile t into a stage: its run-table rows, rows q0.. and their mirrors, on one mbarrier.
+__device__ __forceinline__ void issue_mirror_tile(const GridArgs& g, const MirrorTiling& T, const unsigned* runtab,
+                                                  const unsigned char* gsrc, unsigned char* dst, uint64_t* bar,
+                                                  long long t) {
+    const int plane = (int)fdiv((uint32_t)t, T.fd_tpp);
+    const int q0 = ((int)t - plane * T.tpp) * T.P;
+    const int nA = min(T.P, g.nz - q0);
+    const int qlo = max(q0, 1), qhi = min(q0 + nA - 1, g.half - 1);
+    const size_t rb = (size_t)g.nz * 8;
+    const size_t a0 = ((size_t)plane * g.N + q0) * rb;
+    const size_t as = a0 & ~size_t(15), ae = (a0 + (size_t)nA * rb + 15) & ~size_t(15);
+    size_t bs = 0, be = 0;
+    if (qhi >= qlo) {
+        const size_t b0 = ((size_t)plane * g.N + g.N - qhi) * rb;
+        bs = b0 & ~size_t(15);
+        be = (b0 + (size_t)(qhi - qlo + 1) * rb + 15) & ~size_t(15);
+    }
+    const int kx = kval(g.slab0 + plane, g.N), ax = kx < 0 ? -kx : kx;
+    const unsigned tb = (unsigned)(nA * T.Rp * 4);
+    ptx::fence_async_smem();
+    ptx::mbar_expect_tx(bar, (unsigned)(ae - as + be - bs) + tb);
+    ptx::bulk_g2s(dst, runtab + ((size_t)ax * (g.half + 1) + q0) * T.Rp, tb, bar);
+    ptx::bulk_g2s(dst + T.tab_bytes, gsrc + as, (unsigned)(ae - as), bar);
+    if (be > bs) ptx::bulk_g2s(dst + T.tab_bytes + T.blk, gsrc + bs, (unsigned)(be - bs), bar);
+}
+
+template <bool EXACT>
+__global__ void __launch_bounds__(kMirrorMaxWarps * 32)
+    k_bin_mirror(GridArgs g, MirrorTiling T, const int* __restrict__ thresh, const float* __restrict__ w1g,
+                 const float* __restrict__ grid, double* bin_sum, double* F0sq, unsigned* status, long long ntiles,
+                 const unsigned* __restrict__ runtab) {
+    typedef typename SpillOf<EXACT>::type Spill;
+    extern __shared__ unsigned char sm_raw[];
+    const int W = blockDim.x >> 5;
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    const StreamPlan Pl = plan_bin_mirror(W, g.nrbins, g.nz, EXACT, T);
+    unsigned char* base = sm_raw + ((128 - (ptx::smem_u32(sm_raw) & 127)) & 127);
+    unsigned char* wst = base + Pl.stage_off + (size_t)warp * 2 * T.stage_bytes;
+    uint64_t* wbar = reinterpret_cast<uint64_t*>(base + Pl.bar_off) + warp * 2;
+    Spill* my_spill = reinterpret_cast<Spill*>(base + Pl.spill_off) + (size_t)warp * kRun * 32 + lane;
+    float* s_H0 = reinterpret_cast<float*>(base + Pl.hist_off);
+    int* s_thr = reinterpret_cast<int*>(base + Pl.thr_off);
+    float2* s_wt = reinterpret_cast<float2*>(base + Pl.tab_off);
+    const int hstride = totals_stride(g.nrbins);
+    for (int i = tid; i < hstride * T.copies; i += blockDim.x) s_H0[i] = 0.f;
+    for (int i = tid; i < g.nrbins; i += blockDim.x) s_thr[i] = thresh[i];
+    for (int i = tid; i < g.nz + kRun; i += blockDim.x)
+        s_wt[i] = i < g.nz ? make_float2(w1g[i], (i == 0 || i == g.half) ? 1.f : 2.f) : make_float2(0.f, 0.f);
+    // the stages start zeroed: bytes a lane reads past a row end that no copy wrote are 0
+    {
+        uint4* st4 = reinterpret_cast<uint4*>(base + Pl.stage_off);
+        for (int i = tid; i < W * 2 * T.stage_bytes / 16; i += blockDim.x) st4[i] = make_uint4(0, 0, 0, 0);
+        ptx::fence_async_smem();
+    }
+    if (tid == 0) s_thr[g.nrbins] = 0x7fffffff;
+    if (lane == 0) {
+        ptx::mbar_init(&wbar[0], 1);
+        ptx::mbar_init(&wbar[1], 1);
+        ptx::mbar_init_fence();
+    }
+    __syncthreads();
+
+    // this lane's pair and run within every tile; its window factors and multiplicities
+    const int p = lane / T.R, r = lane - p * T.R;
+    const bool lane_ok = p < T.P;
+    const int z0 = r * kRun;
+    float wz[kRun], mz[kRun];
+#pragma unroll
+    for (int i = 0; i < kRun; i++) {
+        const float2 w = s_wt[z0 + i];
+        wz[i] = w.x;
+        mz[i] = w.y;
+    }
+    float* s_H = s_H0 + (size_t)(p % T.copies) * hstride;
+    float* s_L = s_H + g.nrbins;
+    const size_t rb = (size_t)g.nz * 8;
+
+    const long long gw = (long long)blockIdx.x * W + warp, TW = (long long)gridDim.x * W;
+    const long long my_n = gw < ntiles ? (ntiles - 1 - gw) / TW + 1 : 0;
+    const unsigned char* gsrc = reinterpret_cast<const unsigned char*>(grid);
+    if (lane == 0)
+        for (int s = 0; s < 2 && s < my_n; s++)
+            issue_mirror_tile(g, T, runtab, gsrc, wst + s * T.stage_bytes, &wbar[s], gw + s * TW);
+    bool ok = true;
+    long long k = 0;
+    int s = 0;
+    unsigned phase = 0;
+    for (; k < my_n; k++) {
+        const bool got = ptx::mbar_wait_bounded_n(&wbar[s], phase, k == 0 ? g.first_wait : (1 << 22));
+        if (!__all_sync(kFull, got)) {
+            ok = false;
+            break;
+        }
+        const unsigned char* st = wst + s * T.stage_bytes;
+        const uint32_t t = (uint32_t)(gw + k * TW);
+        const int plane = (int)fdiv(t, T.fd_tpp);
+        const int q0 = ((int)t - plane * T.tpp) * T.P;
+        const int nA = min(T.P, g.nz - q0);
+        const bool valid = lane_ok && p < nA;
+        const int q = valid ? q0 + p : 0;
+        const int kx = kval(g.slab0 + plane, g.N), ax = kx < 0 ? -kx : kx;
+        const float iwxy = __fmul_rn(s_wt[ax].x, s_wt[q].x);
+        const bool single = q == 0 || q == g.half;
+        const int qhi = min(q0 + nA - 1, g.half - 1);
+        const size_t a0 = ((size_t)plane * g.N + q0) * rb, b0 = ((size_t)plane * g.N + g.N - qhi) * rb;
+        const unsigned offA = (unsigned)T.tab_bytes + (unsigned)(a0 & 15) + (unsigned)(p * g.nz + z0) * 8u;
+        const unsigned offB = single || !valid ? offA
+                                               : (unsigned)(T.tab_bytes + T.blk) + (unsigned)(b0 & 15) +
+                                                     (unsigned)((qhi - q) * g.nz + z0) * 8u;
+        unsigned e = 1u;
+        if (valid) e = reinterpret_cast<const unsigned*>(st)[p * T.Rp + r];
+        const bool fast = valid && (e & 1u) == 0;
+        const int b = (int)(e >> 17);
+        const int nsp = fast ? __popc(e & 0x1fffeu) : 0;  // the run's closed bins
+        if (fast) {
+            Spill* sp = my_spill;
+            float h = 0.f, l = 0.f;
+            const float2* va = reinterpret_cast<const float2*>(st + offA);
+            const float2* vb = reinterpret_cast<const float2*>(st + offB);
+#pragma unroll
+            for (int i = 0; i < kRun; i++)
+                mirror_step<EXACT>(va[i], vb[i], iwxy, wz[i], mz[i], i > 0 && ((e >> i) & 1u), sp, h, l);
+        }
+        // The next lane's run continues this one: where it starts in the bin this run ends
+        // in and has a later bin of its own, its first sum joins this run's last one here.
+        float fx = 0.f, fy = 0.f;
+        if (fast) {
+            const Spill f0 = my_spill[0];
+            fx = spill_hi(f0);
+            fy = spill_lo(f0);
+        }
+        const int info = fast ? (p << 8) | (nsp + 1) : 0;  // pair, items; 0: no run
+        const int nb_info = __shfl_down_sync(kFull, info, 1);
+        const int nb_b = __shfl_down_sync(kFull, b, 1);
+        const float nfx = __shfl_down_sync(kFull, fx, 1), nfy = __shfl_down_sync(kFull, fy, 1);
+        const bool take = fast && lane < 31 && (nb_info >> 8) == p && (nb_info & 255) >= 2 && nb_b == b + nsp;
+        const bool given = __shfl_up_sync(kFull, take ? 1 : 0, 1) != 0 && lane > 0;
+        if (fast) {
+            const float sc = single ? 0.5f : 1.f;
+            for (int qq = given ? 1 : 0; qq <= nsp; qq++) {
+                const Spill v = my_spill[32 * qq];
+                float vh = spill_hi(v), vl = spill_lo(v);
+                if (qq == nsp && take) pair_add(vh, vl, nfx, nfy);
+                add_pair(s_H, s_L, b + qq, __fmul_rn(vh, sc), __fmul_rn(vl, sc));
+            }
+        }
+        // slow runs (the k = 0 mode; a bin skipped between two modes): one run at a time,
+        // a mode of both rows per lane
+        unsigned slow = __ballot_sync(kFull, valid && !fast);
+        while (slow) {
+            const int L = __ffs(slow) - 1;
+            slow &= slow - 1;
+            const int zL = __shfl_sync(kFull, z0, L);
+            const int kxyL = __shfl_sync(kFull, ax * ax + q * q, L);
+            const float iwL = __shfl_sync(kFull, iwxy, L);
+            const unsigned oaL = __shfl_sync(kFull, offA, L), obL = __shfl_sync(kFull, offB, L);
+            const bool sgL = __shfl_sync(kFull, single ? 1 : 0, L) != 0;
+            int key = -1;
+            float phi = 0.f, plo = 0.f;
+            const int zz = zL + lane;
+            const int k2m = kxyL + zz * zz;
+            if (lane < kRun && zz < g.nz && k2m != 0) {
+                const float2 va = *reinterpret_cast<const float2*>(st + oaL + 8 * lane);
+                mode_value<EXACT>(va.x, va.y, iwL, s_wt[zz], phi, plo);
+                if (!sgL) {
+                    const float2 vb = *reinterpret_cast<const float2*>(st + obL + 8 * lane);
+                    float qh, ql;
+                    mode_value<EXACT>(vb.x, vb.y, iwL, s_wt[zz], qh, ql);
+                    pair_add(phi, plo, qh, ql);
+                }
+                key = bin_of(k2m, g.c1, s_thr, g.nrbins);
+            }
+            bool tail;
+            warp_seg_pair(key, phi, plo, tail);
+            if (tail && key >= 0) add_pair(s_H, s_L, key, phi, plo);
+        }
+        __syncwarp();
+        if (lane == 0 && k + 2 < my_n)
+            issue_mirror_tile(g, T, runtab, gsrc, wst + s * T.stage_bytes, &wbar[s], gw + (k + 2) * TW);
+        if (++s == 2) {
+            s = 0;
+            phase ^= 1;
+        }
+    }
+    if (!ok && lane == 0) {
+        atomicOr(status, kStTimeout);
+        for (long long kk = k; kk < my_n && kk < k + 2; kk++) {
+            ptx::mbar_wait_bounded(&wbar[s], phase);
+            if (++s == 2) {
+                s = 0;
+                phase ^= 1;
+            }
+        }
+    }
+    __syncthreads();
+    if (blockIdx.x == 0 && tid == 0 && g.slab0 == 0 && g.nmodes > 0) {
+        const float re = grid[0], im = grid[1];
+        *F0sq = (double)__fadd_rn(__fmul_rn(re, re), __fmul_rn(im, im));
+    }
+    for (int bb = tid; bb < g.nrbins; bb += blockDim.x) {
+        double v = 0.0;
+        for (int c = 0; c < T.copies; c++)
+            v += (double)s_H0[c * hstride + bb] + (double)s_H0[c * hstride + g.nrbins + bb];
+        if (v != 0.0) atomicAdd(bin_sum + bb, v);
+    }
+}
+
 int sm_count_s() {
     static int n = 0;
     if (!n) {
@@ -946,11 +1260,12 @@ int sm_count_s() {
 // shared memory on the current device, memoised: the occupancy query and the attribute
 // call cost host microseconds, and at every step the device waits for the first launch.
 // The kernel's dynamic shared-memory limit is raised once per device to the largest any
-// of these passes asks for (220 KB); each launch still asks for its own size.  The memo
+// of these passes asks for (226 KB: the 227 KB a block may use, less room for static shared
+// memory); each launch still asks for its own size.  The memo
 // is a fixed table (no host allocation: the allocation-free entry point runs through
 // here): 64 (kernel, device, threads, smem) results, replaced round-robin, and the
 // kernels whose shared-memory limit was raised.
-constexpr int kMaxSmemPass = 220 * 1024;
+constexpr int kMaxSmemPass = 226 * 1024;
 struct OccEntry {
     const void* kern;
     int dev, threads, n;
@@ -1092,6 +1407,52 @@ int run_bin_rows_any(const GridGeom& g, const GridArgs& a, const float* grid, do
     return run_bin_rows<WARPS, STAGES, EXACT, false>(g, a, grid, bin_sum, F0sq, status, st);
 }
 
+// The mirrored-row pass needs the geometry's run table and rows of at most 32 runs
+// (N <= 1086).  Warps per CTA: the most resident warps per SM, then the largest CTA
+// (KSPACE_GPU_MIRROR_WARPS fixes it).
+template <bool EXACT>
+int run_bin_mirror(const GridGeom& g, const GridArgs& a, const float* grid, double* bin_sum, double* F0sq,
+                   unsigned* status, cudaStream_t st) {
+    static const int force_w = [] {
+        const char* e = getenv("KSPACE_GPU_MIRROR_WARPS");
+        return e ? atoi(e) : 0;
+    }();
+    if ((reinterpret_cast<uintptr_t>(grid) & 15) != 0) return -1;
+    MirrorTiling T = make_mirror_tiling(a.nz);
+    if (T.P < 1 || !g.runtab || g.run_Rp != T.Rp || g.nslab <= 0) return -1;
+    const long long ntiles = (long long)g.nslab * T.tpp;
+    if (ntiles >= (1LL << 31)) return -1;
+    auto kern = k_bin_mirror<EXACT>;
+    int best_w = 0, best_occ = 0;
+    for (int w = kMirrorMaxWarps; w >= 2; w -= 2) {
+        if (force_w > 0 && w != force_w) continue;
+        const StreamPlan p = plan_bin_mirror(w, g.nrbins, a.nz, EXACT, T);
+        if (p.total > (size_t)kMaxSmemPass) continue;
+        const int occ = resident_blocks(kern, w * 32, p.total);
+        if (occ * w > best_occ * best_w) {
+            best_w = w;
+            best_occ = occ;
+        }
+    }
+    if (best_w == 0) return -1;
+    // a copy of the totals per pair of a warp (at most 4), while that costs no resident blocks
+    for (int c = T.P < 4 ? T.P : 4; c > 1; c /= 2) {
+        MirrorTiling t2 = T;
+        t2.copies = c;
+        const StreamPlan p = plan_bin_mirror(best_w, g.nrbins, a.nz, EXACT, t2);
+        if (p.total <= (size_t)kMaxSmemPass && resident_blocks(kern, best_w * 32, p.total) == best_occ) {
+            T = t2;
+            break;
+        }
+    }
+    const StreamPlan P = plan_bin_mirror(best_w, g.nrbins, a.nz, EXACT, T);
+    long long n = (long long)sm_count_s() * best_occ;
+    const long long need = (ntiles + best_w - 1) / best_w;
+    if (n > need) n = need > 0 ? need : 1;
+    kern<<<(int)n, best_w * 32, P.total, st>>>(a, T, g.thresh, g.w1, grid, bin_sum, F0sq, status, ntiles, g.runtab);
+    return cudaPeekAtLastError() == cudaSuccess ? 0 : -2;
+}
+
 template <int WARPS, int STAGES>
 int run_corr_stream(const GridArgs& a, float* grid, CorrTable corr, unsigned* status, cudaStream_t st) {
     CUtensorMap map;
@@ -1187,6 +1548,16 @@ int launch_bin_stream(const GridGeom& g, const GridArgs& a, const float* grid, d
 int launch_bin_rows(const GridGeom& g, const GridArgs& a, const float* grid, double* bin_sum, double* F0sq,
                     unsigned* status, int warps, int stages, bool exact, cudaStream_t st) {
     if (a.N >= 32768) return -1;
+    // the mirrored-row pass where it applies (KSPACE_GPU_MIRROR=0: the row pass only)
+    static const int mirror = [] {
+        const char* e = getenv("KSPACE_GPU_MIRROR");
+        return e ? atoi(e) : 1;
+    }();
+    if (mirror) {
+        const int r = exact ? run_bin_mirror<true>(g, a, grid, bin_sum, F0sq, status, st)
+                            : run_bin_mirror<false>(g, a, grid, bin_sum, F0sq, status, st);
+        if (r != -1) return r;
+    }
 #define KSP_BR(W, S)                                                                            \
     if (warps == W && stages == S)                                                              \
         return exact ? run_bin_rows_any<W, S, true>(g, a, grid, bin_sum, F0sq, status, st)      \
