@@ -948,6 +948,9 @@ __global__ void __launch_bounds__(WARPS * 32)
 // boundary).  Each warp owns a ring of two stages.
 constexpr int kMirrorTail = 144;  // zeroed bytes after a stage's rows (reads past the last row end)
 constexpr int kMirrorMaxWarps = 12;
+// Spill slots per lane: a run closing more than kMirrorSlots - 1 bins (low k only) takes
+// the warp-cooperative path; the shared memory saved holds one more warp per SM.
+constexpr int kMirrorSlots = 9;
 
 struct MirrorTiling {
     int R;            // 17-mode runs per row
@@ -988,7 +991,7 @@ __host__ __device__ inline StreamPlan plan_bin_mirror(int warps, int nrbins, int
     o += sizeof(uint64_t) * (size_t)warps * 2;
     o = (o + 15) & ~size_t(15);
     p.spill_off = o;
-    o += (size_t)warps * kRun * 32 * (exact ? 8 : 4);
+    o += (size_t)warps * kMirrorSlots * 32 * (exact ? 8 : 4);
     p.hist_off = o;
     o += sizeof(float) * (size_t)totals_stride(nrbins) * T.copies;
     p.thr_off = o;
@@ -1077,7 +1080,7 @@ __global__ void __launch_bounds__(kMirrorMaxWarps * 32)
     unsigned char* base = sm_raw + ((128 - (ptx::smem_u32(sm_raw) & 127)) & 127);
     unsigned char* wst = base + Pl.stage_off + (size_t)warp * 2 * T.stage_bytes;
     uint64_t* wbar = reinterpret_cast<uint64_t*>(base + Pl.bar_off) + warp * 2;
-    Spill* my_spill = reinterpret_cast<Spill*>(base + Pl.spill_off) + (size_t)warp * kRun * 32 + lane;
+    Spill* my_spill = reinterpret_cast<Spill*>(base + Pl.spill_off) + (size_t)warp * kMirrorSlots * 32 + lane;
     float* s_H0 = reinterpret_cast<float*>(base + Pl.hist_off);
     int* s_thr = reinterpret_cast<int*>(base + Pl.thr_off);
     float2* s_wt = reinterpret_cast<float2*>(base + Pl.tab_off);
@@ -1149,7 +1152,7 @@ __global__ void __launch_bounds__(kMirrorMaxWarps * 32)
                                                      (unsigned)((qhi - q) * g.nz + z0) * 8u;
         unsigned e = 1u;
         if (valid) e = reinterpret_cast<const unsigned*>(st)[p * T.Rp + r];
-        const bool fast = valid && (e & 1u) == 0;
+        const bool fast = valid && (e & 1u) == 0 && __popc(e & 0x1fffeu) < kMirrorSlots;
         const int b = (int)(e >> 17);
         const int nsp = fast ? __popc(e & 0x1fffeu) : 0;  // the run's closed bins
         if (fast) {
@@ -1175,17 +1178,8 @@ __global__ void __launch_bounds__(kMirrorMaxWarps * 32)
         const float nfx = __shfl_down_sync(kFull, fx, 1), nfy = __shfl_down_sync(kFull, fy, 1);
         const bool take = fast && lane < 31 && (nb_info >> 8) == p && (nb_info & 255) >= 2 && nb_b == b + nsp;
         const bool given = __shfl_up_sync(kFull, take ? 1 : 0, 1) != 0 && lane > 0;
-        if (fast) {
-            const float sc = single ? 0.5f : 1.f;
-            for (int qq = given ? 1 : 0; qq <= nsp; qq++) {
-                const Spill v = my_spill[32 * qq];
-                float vh = spill_hi(v), vl = spill_lo(v);
-                if (qq == nsp && take) pair_add(vh, vl, nfx, nfy);
-                add_pair(s_H, s_L, b + qq, __fmul_rn(vh, sc), __fmul_rn(vl, sc));
-            }
-        }
-        // slow runs (the k = 0 mode; a bin skipped between two modes): one run at a time,
-        // a mode of both rows per lane
+        // slow runs (the k = 0 mode; a bin skipped between two modes; more closed bins than
+        // spill slots): one run at a time, a mode of both rows per lane
         unsigned slow = __ballot_sync(kFull, valid && !fast);
         while (slow) {
             const int L = __ffs(slow) - 1;
@@ -1217,6 +1211,17 @@ __global__ void __launch_bounds__(kMirrorMaxWarps * 32)
         __syncwarp();
         if (lane == 0 && k + 2 < my_n)
             issue_mirror_tile(g, T, runtab, gsrc, wst + s * T.stage_bytes, &wbar[s], gw + (k + 2) * TW);
+        // the closed bins of the fast runs go to the totals from the spill slots, after the
+        // stage is on its way again
+        if (fast) {
+            const float sc = single ? 0.5f : 1.f;
+            for (int qq = given ? 1 : 0; qq <= nsp; qq++) {
+                const Spill v = my_spill[32 * qq];
+                float vh = spill_hi(v), vl = spill_lo(v);
+                if (qq == nsp && take) pair_add(vh, vl, nfx, nfy);
+                add_pair(s_H, s_L, b + qq, __fmul_rn(vh, sc), __fmul_rn(vl, sc));
+            }
+        }
         if (++s == 2) {
             s = 0;
             phase ^= 1;
@@ -1424,7 +1429,7 @@ int run_bin_mirror(const GridGeom& g, const GridArgs& a, const float* grid, doub
     if (ntiles >= (1LL << 31)) return -1;
     auto kern = k_bin_mirror<EXACT>;
     int best_w = 0, best_occ = 0;
-    for (int w = kMirrorMaxWarps; w >= 2; w -= 2) {
+    for (int w = kMirrorMaxWarps; w >= 2; w--) {
         if (force_w > 0 && w != force_w) continue;
         const StreamPlan p = plan_bin_mirror(w, g.nrbins, a.nz, EXACT, T);
         if (p.total > (size_t)kMaxSmemPass) continue;
