@@ -364,7 +364,10 @@ def run_gb300(args, cfg):
     k1_gbs = bytes_grid / (k1_ms * 1e-3) / 1e9 if k1_ms > 0 else None
     k3_gbs = 2 * bytes_grid / (k3_ms * 1e-3) / 1e9 if k3_ms > 0 else None
     tma = int(os.environ.get("KSPACE_GPU_TMA", "5"))
-    k1_name = "k_bin_rows" if tma >= 5 else ("k_bin_stream" if tma >= 3 else "k_bin_power_tma")
+    # the mirrored-row binning pass where a grid row is at most 32 runs of 17 modes
+    mirror = tma >= 5 and os.environ.get("KSPACE_GPU_MIRROR", "1") != "0" and (nz + 16) // 17 <= 32
+    k1_name = ("k_bin_mirror" if mirror else "k_bin_rows") if tma >= 5 else (
+        "k_bin_stream" if tma >= 3 else "k_bin_power_tma")
     k3_name = "k_correct_stream" if tma >= 3 else "k_correct_tma"
     if k3_ms >= k1_ms:
         dom = {"kernel": k3_name + " (grid multiply)", "bytes": 2 * bytes_grid, "ms": k3_ms, "gbs": k3_gbs}
@@ -393,6 +396,7 @@ def run_gb300(args, cfg):
         "hbm_frac_step": 3 * bytes_grid / (ms_per_step * 1e-3) / 1e9 / hbm,
         "stage_ms": {"binning_K1": k1_ms, "integrator_K2": k2_ms, "correction_K3": k3_ms, "whole_call": stage[3]},
         "stage_gbs": {"K1": k1_gbs, "K3": k3_gbs},
+        "stage_kernels": {"K1": k1_name, "K2": "k_dnu_qag_blk (+ k_dtot_coeffs, k_combine, k_finish)", "K3": k3_name},
         "stage_frac": {"K1": (k1_gbs / hbm) if k1_gbs else None, "K3": (k3_gbs / hbm) if k3_gbs else None},
         "roofline": {"bound": "hbm", "kernel": dom["kernel"], "achieved": dom["gbs"], "peak": hbm,
                      "peak_kind": peak_kind, "unit": "GB/s", "frac": (dom["gbs"] / hbm) if dom["gbs"] else None,
