@@ -135,7 +135,7 @@ static void free_table(kspace_ctx* c) {
     void* ptrs[] = {I.scalefact, I.dtot, I.coef, I.nu_init, I.nu_last, I.wavenum, I.dcdm, I.dnu_s, I.dnu,
                     I.knot_invdiag, I.knot_fac, I.knot_invh, I.knot_h3, I.knot_ih3, I.nc_g, I.nc_fsl,
                     I.nc_dx, I.nc_j, I.fs_x, I.fs_y, I.fs_c, I.fs_seg, I.t_logk, I.t_T, I.t_c, I.sc,
-                    I.qag_max, I.qag_total};
+                    I.qag_max, I.qag_total, I.coef_unit};
     for (void* p : ptrs)
         if (p) cudaFree(p);
     memset(&I, 0, sizeof(I));
@@ -450,6 +450,7 @@ extern "C" int kspace_gpu_alloc_table(kspace_ctx* c, int nk_alloc, double TimeTr
     CK(dalloc(&I.coef, nk * ld));
     CK(cudaMemset(I.dtot, 0, sizeof(double) * nk * ld));
     CK(cudaMemset(I.coef, 0, sizeof(double) * nk * ld));
+    CK(dalloc(&I.coef_unit, ld));
     CK(dalloc(&I.nu_init, nk));
     CK(dalloc(&I.nu_last, nk));
     CK(dalloc(&I.wavenum, nk));
@@ -745,6 +746,9 @@ static int update_device(kspace_ctx* c, double a, int nk_in, const double* keff_
                          double* dnu_out_d, bool want_corr, const FinalizeArgs* fin = nullptr) {
     NEED(c->table_ready && c->hubble_ready, KSPACE_ERR_ORDER);
     IntegratorDev& I = c->I;
+    // side-stream work queued by start_prep writes the integrator's tables (the row
+    // splines among them): nothing below runs before it, used or not
+    if (c->prep_valid) CK(cudaStreamWaitEvent(c->stream, c->ev_join, 0));
     if (fin && fin->active) {
         const double la = log(a);
         const bool will_prepare = c->prep_valid && c->init_done && nk_in == c->nk && c->nk >= 2 && c->ia >= 1 &&
@@ -803,7 +807,7 @@ static int update_device(kspace_ctx* c, double a, int nk_in, const double* keff_
     if (prepared) {
         CK(cudaStreamWaitEvent(c->stream, c->ev_join, 0));
         launch_integrator_rest(I, c->nk, Na, c->nspec, c->spec_ids, c->qag_warps, c->stream, c->qag_split, prov_row,
-                               true, fin);
+                               true, fin, c->prep_base);
     } else {
         launch_delta_nu_combined(I, c->nk, Na, a, loga, c->loga0, c->TimeTransfer, c->fact_valid, c->nspec,
                                  c->spec_ids, c->qag_warps, c->stream, c->qag_split);
@@ -1229,8 +1233,9 @@ static int start_prep(kspace_ctx* c, const Geo* G, double Time) {
     const int Na = c->ia + 1;
     CK(cudaStreamWaitEvent(c->side, c->ev_fork, 0));  // recorded before the binning pass
     launch_integrator_prepare(c->I, Na, Time, loga, c->loga0, c->TimeTransfer, c->fact_valid, 1, false, c->side);
+    c->prep_base = launch_dtot_base(c->I, c->nk, Na, c->side);
     CK(cudaEventRecord(c->ev_join, c->side));
-    g_launches += 5;
+    g_launches += c->prep_base ? 6 : 5;
     c->prep_valid = true;
     c->prep_Na = Na;
     c->prep_loga = loga;

@@ -93,6 +93,7 @@ struct kspace_ctx {
     bool prep_valid = false;
     int prep_Na = 0;
     double prep_loga = 0;
+    bool prep_base = false;  // launch_dtot_base ran with the preparation
     // the binning pass's normalisation, deferred into the row-spline kernel of a prepared
     // step (active = 0: already done)
     ksp::FinalizeArgs fin{};

@@ -405,6 +405,68 @@ __global__ void k_dtot_coeffs(IntegratorDev I, int nk, int Na, int staged, int u
     }
 }
 
+// ------------------------------------------------------------------ row splines in two parts
+// A history row's natural spline is linear in the row, and the provisional (last) knot
+// enters the spline system through its last right-hand side only, so
+//   c = c_base + (y_new - y_base) c_unit,
+// with c_base the coefficients of the row whose last knot is y_base (the knot before it)
+// and c_unit those of a unit last knot with all other knots zero.  Both depend only on
+// the committed rows and the knots: k_dtot_base solves them beside the binning pass
+// (block nk: c_unit).  After it, k_row_update forms y_new (update_delta_tot,
+// delta_tot_table.c:177-191) from this step's delta_cdm and adds the correction, in
+// place of the solve.  y_new - y_base is one step's growth of delta_tot, so the sum does
+// not cancel.
+__global__ void k_dtot_base(IntegratorDev I, int nk, int Na) {
+    // in place in the coefficient rows (global memory, L1-cached): the binning pass holds
+    // nearly all of every SM's shared memory, and these blocks run beside it
+    const int lane = threadIdx.x & 31;
+    const int m = Na - 2;  // unknowns c[1..m]
+    const double* ih = I.knot_invh;
+    double* c;
+    if (blockIdx.x == nk) {
+        c = I.coef_unit;
+        for (int u = lane; u < m; u += 32) c[u + 1] = u == m - 1 ? 3.0 * ih[m] : 0.0;
+    } else {
+        const double* y = I.dtot + (size_t)blockIdx.x * I.ld;
+        c = I.coef + (size_t)blockIdx.x * I.ld;
+        for (int u = lane; u < m; u += 32) {
+            const double y2 = u == m - 1 ? y[m] : y[u + 2];  // the last knot taken equal to the one before
+            c[u + 1] = 3.0 * ((y2 - y[u + 1]) * ih[u + 1] - (y[u + 1] - y[u]) * ih[u]);
+        }
+    }
+    __syncwarp();
+    spline_solve_scan(I, m, c);
+    if (lane == 0) {
+        c[0] = 0.0;
+        c[Na - 1] = 0.0;
+    }
+}
+
+// block per bin: this bin's delta_cdm (a deferred normalisation), the provisional row
+// `row` = Na - 1, and its spline as c_base + (y_new - y_base) c_unit
+__global__ void k_row_update(IntegratorDev I, int nk, int Na, int row, FinalizeArgs fin) {
+    __shared__ double s_dy;
+    const int ik = blockIdx.x;
+    if (threadIdx.x == 0) {
+        if (fin.active) finalize_bin(fin, ik);
+        const StepScalars& S = *I.sc;
+        double* y = I.dtot + (size_t)ik * I.ld;
+        const double yn = get_delta_tot(I.nu_last[ik], I.dcdm[ik], S.OmegaNua3, S.Omeganonu, S.OmegaNu1, S.partnu);
+        y[row] = yn;
+        s_dy = yn - y[Na - 2];
+    }
+    __syncthreads();
+    const double dy = s_dy;
+    double* c = I.coef + (size_t)ik * I.ld;
+    for (int k = 1 + threadIdx.x; k < Na - 1; k += blockDim.x) c[k] = fma(dy, __ldg(I.coef_unit + k), c[k]);
+}
+
+bool launch_dtot_base(const IntegratorDev& I, int nk, int Na, cudaStream_t st) {
+    if (Na <= 2 || nk <= 0) return false;
+    k_dtot_base<<<nk + 1, 32, 0, st>>>(I, nk, Na);
+    return cudaPeekAtLastError() == cudaSuccess;
+}
+
 // ------------------------------------------------------------------ node table
 // The k-independent terms of the delta_nu integrand at the 61 nodes of the first
 // kNcLevels levels of QAG's bisection of [log a0, log a]: thread per (slot, node).
@@ -766,7 +828,7 @@ void launch_integrator_prepare(const IntegratorDev& I, int Na, double a, double 
 // integrals, the species sum.
 void launch_integrator_rest(const IntegratorDev& I, int nk, int Na, int nspec, const int* spec_ids,
                             int warps_per_block, cudaStream_t st, int qag_split, int update_row, bool defer_combine,
-                            const FinalizeArgs* fin) {
+                            const FinalizeArgs* fin, bool base_ready) {
     // a deferred normalisation runs in the row-spline kernel, or on its own without one
     FinalizeArgs fa{};
     if (fin && fin->active) {
@@ -779,7 +841,9 @@ void launch_integrator_rest(const IntegratorDev& I, int nk, int Na, int nspec, c
         launch_update_row_scalars(I, nk, update_row, st);
         update_row = -1;
     }
-    if (Na > 2) {
+    if (Na > 2 && base_ready && update_row == Na - 1) {
+        k_row_update<<<nk, 128, 0, st>>>(I, nk, Na, update_row, fa);
+    } else if (Na > 2) {
         static bool dc_attr = false;
         if (!dc_attr) {
             raise_dynamic_smem_limit(reinterpret_cast<const void*>(k_dtot_coeffs));

@@ -64,6 +64,8 @@ struct IntegratorDev {
     long long* qag_total;
     double* ivals;                   // optional: final QAG intervals [kNuSpecies][nk_alloc][kQagLimit][2]
     int* nivals;                     // [kNuSpecies][nk_alloc]
+    double* coef_unit;               // [ld] spline coefficients of a unit provisional (last) knot,
+                                     // the other knots zero (k_dtot_base)
 };
 
 #ifdef __CUDACC__
@@ -499,9 +501,16 @@ void launch_integrator_prepare(const IntegratorDev& I, int Na, double a, double 
 // update_row >= 0: write the provisional row `update_row` (update_delta_tot, from
 // delta_nu_last and delta_cdm with the call's scalars) as each row's spline is solved;
 // defer_combine: leave the species sum to launch_finish_update(..., combine = true)
+// base_ready: launch_dtot_base ran for this Na (the rows' splines then take the
+// provisional row as a correction)
 void launch_integrator_rest(const IntegratorDev& I, int nk, int Na, int nspec, const int* spec_ids,
                             int warps_per_block, cudaStream_t st, int qag_split, int update_row = -1,
-                            bool defer_combine = false, const FinalizeArgs* fin = nullptr);
+                            bool defer_combine = false, const FinalizeArgs* fin = nullptr,
+                            bool base_ready = false);
+// Before the provisional row is known (beside the binning pass, after
+// launch_integrator_prepare): every row's spline with its last knot equal to the one
+// before, and the spline of a unit last knot.  False for histories of two knots or fewer.
+bool launch_dtot_base(const IntegratorDev& I, int nk, int Na, cudaStream_t st);
 size_t dnu_qag_smem(int ld, int wpb);
 // end of get_delta_nu_update (delta_tot_table.c:226-248) + interface_common.c:134-146:
 // delta_nu_last, committed row, NaN check, clamp, ratio/log k/kspace_prefac, grid table
