@@ -942,11 +942,13 @@ __global__ void __launch_bounds__(WARPS * 32)
 // and its closed bins now cover 34 modes.
 // A tile is P consecutive |ky| = q of one plane (P = 32 / runs per row): rows q0..q0+P-1
 // (one copy) and their mirrors N-q (one copy, q descending).  q = 0 and q = N/2 are
-// their own mirrors: their lanes read the row twice and halve the run sums (exact).  A
+// their own mirrors: their lanes pair the row with zeros (the stage's zeroed tail).  A
 // copy starts at the 16-byte boundary at or below its first row and ends at the one at
 // or above its last row end (a row is 8 (N/2+1) bytes, so odd rows start 8 bytes past a
 // boundary).  Each warp owns a ring of two stages.
-constexpr int kMirrorTail = 144;  // zeroed bytes after a stage's rows (reads past the last row end)
+// zeroed bytes after a stage's rows: reads past the last row end, and the zero partner
+// (17 modes) of a row that is its own mirror
+constexpr int kMirrorTail = 144;
 constexpr int kMirrorMaxWarps = 12;
 // Spill slots per lane: a run closing more than kMirrorSlots - 1 bins (low k only) takes
 // the warp-cooperative path; the shared memory saved holds one more warp per SM.
@@ -1147,9 +1149,11 @@ __global__ void __launch_bounds__(kMirrorMaxWarps * 32)
         const int qhi = min(q0 + nA - 1, g.half - 1);
         const size_t a0 = ((size_t)plane * g.N + q0) * rb, b0 = ((size_t)plane * g.N + g.N - qhi) * rb;
         const unsigned offA = (unsigned)T.tab_bytes + (unsigned)(a0 & 15) + (unsigned)(p * g.nz + z0) * 8u;
-        const unsigned offB = single || !valid ? offA
-                                               : (unsigned)(T.tab_bytes + T.blk) + (unsigned)(b0 & 15) +
-                                                     (unsigned)((qhi - q) * g.nz + z0) * 8u;
+        // a row that is its own mirror pairs with the stage's zeroed tail
+        const unsigned offB = !valid ? offA
+                              : single ? (unsigned)(T.tab_bytes + 2 * T.blk)
+                                       : (unsigned)(T.tab_bytes + T.blk) + (unsigned)(b0 & 15) +
+                                             (unsigned)((qhi - q) * g.nz + z0) * 8u;
         unsigned e = 1u;
         if (valid) e = reinterpret_cast<const unsigned*>(st)[p * T.Rp + r];
         const bool fast = valid && (e & 1u) == 0 && __popc(e & 0x1fffeu) < kMirrorSlots;
@@ -1178,6 +1182,13 @@ __global__ void __launch_bounds__(kMirrorMaxWarps * 32)
         const float nfx = __shfl_down_sync(kFull, fx, 1), nfy = __shfl_down_sync(kFull, fy, 1);
         const bool take = fast && lane < 31 && (nb_info >> 8) == p && (nb_info & 255) >= 2 && nb_b == b + nsp;
         const bool given = __shfl_up_sync(kFull, take ? 1 : 0, 1) != 0 && lane > 0;
+        if (take) {
+            const Spill v = my_spill[32 * nsp];
+            float vh = spill_hi(v), vl = spill_lo(v);
+            pair_add(vh, vl, nfx, nfy);
+            if constexpr (EXACT) my_spill[32 * nsp] = make_float2(vh, vl);
+            else my_spill[32 * nsp] = vh;
+        }
         // slow runs (the k = 0 mode; a bin skipped between two modes; more closed bins than
         // spill slots): one run at a time, a mode of both rows per lane
         unsigned slow = __ballot_sync(kFull, valid && !fast);
@@ -1214,12 +1225,9 @@ __global__ void __launch_bounds__(kMirrorMaxWarps * 32)
         // the closed bins of the fast runs go to the totals from the spill slots, after the
         // stage is on its way again
         if (fast) {
-            const float sc = single ? 0.5f : 1.f;
             for (int qq = given ? 1 : 0; qq <= nsp; qq++) {
                 const Spill v = my_spill[32 * qq];
-                float vh = spill_hi(v), vl = spill_lo(v);
-                if (qq == nsp && take) pair_add(vh, vl, nfx, nfy);
-                add_pair(s_H, s_L, b + qq, __fmul_rn(vh, sc), __fmul_rn(vl, sc));
+                add_pair(s_H, s_L, b + qq, spill_hi(v), spill_lo(v));
             }
         }
         if (++s == 2) {
