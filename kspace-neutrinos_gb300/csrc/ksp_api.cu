@@ -742,8 +742,11 @@ static int delta_tot_init(kspace_ctx* c, int nk_in, const double* keff_d, const 
 // produces the correction table of interface_common.c:134-146.
 // fin: the binning pass's normalisation when it was deferred (see bin_grid): folded into
 // the row-spline kernel of a prepared step, else launched first.
+// sync = false (a step whose correction pass follows on the stream): no host round trip
+// at the end; the correction pass reads the status word itself and leaves the grid as it
+// is after an error, which the step's final status check reports.
 static int update_device(kspace_ctx* c, double a, int nk_in, const double* keff_d, const double* dcdm_d,
-                         double* dnu_out_d, bool want_corr, const FinalizeArgs* fin = nullptr) {
+                         double* dnu_out_d, bool want_corr, const FinalizeArgs* fin = nullptr, bool sync = true) {
     NEED(c->table_ready && c->hubble_ready, KSPACE_ERR_ORDER);
     IntegratorDev& I = c->I;
     // side-stream work queued by start_prep writes the integrator's tables (the row
@@ -826,7 +829,7 @@ static int update_device(kspace_ctx* c, double a, int nk_in, const double* keff_
         c->ia--;
         c->fact_valid = Na - 3 > 0 ? Na - 3 : 0;
     }
-    return sync_status(c);
+    return sync ? sync_status(c) : KSPACE_OK;
 }
 
 extern "C" int kspace_gpu_get_delta_nu_update(kspace_ctx* c, double a, int nk, const double* keff,
@@ -1402,16 +1405,21 @@ extern "C" int kspace_gpu_add_nu_power_to_rhogrid(kspace_ctx* c, double Time, do
     CK(cudaEventRecord(c->ev_fork, c->stream));
     st = bin_grid(c, G, gd, pmgrid, slab0, nslab, BoxSize, staged ? &ch : nullptr, Time);
     if (st) return st;
-    // the integrator (interface_common.c:125-148)
-    st = update_device(c, Time, G->nk, c->keff_d, c->I.dcdm, c->dnu_out_d, true, c->fin.active ? &c->fin : nullptr);
+    // the integrator (interface_common.c:125-148), then the multiply (interface_gadget.c:
+    // 163-188) on the same stream without a host round trip: an error of the integrator
+    // leaves the grid as it is (the correction kernels read the status word) and comes
+    // back from the status check below
+    st = update_device(c, Time, G->nk, c->keff_d, c->I.dcdm, c->dnu_out_d, true, c->fin.active ? &c->fin : nullptr,
+                       false);
     c->fin.active = 0;
     if (st) return st;
-    c->last_nk = G->nk;
-    c->last_BoxSize = BoxSize;
-    // the multiply (interface_gadget.c:163-188)
     st = correct_grid(c, G, gd, BoxSize, G->nk, staged ? &ch : nullptr, staged ? grid : nullptr);
     if (st) return st;
     st = sync_status(c);
+    if (st == KSPACE_OK) {
+        c->last_nk = G->nk;
+        c->last_BoxSize = BoxSize;
+    }
     if (c->prof) {
         cudaEventElapsedTime(&c->stage_ms[0], c->ev[0], c->ev[1]);
         cudaEventElapsedTime(&c->stage_ms[1], c->ev[1], c->ev[2]);

@@ -39,6 +39,9 @@ enum : unsigned {
     kStKWarn = 1u << 4,      // k < keff_0 / 2 (reference prints to stderr, continues)
     kStTimeout = 1u << 5,    // a bounded wait expired
 };
+// the errors after which the reference terminates before it corrects the grid: the
+// correction pass leaves the grid as it is when one of them is set
+constexpr unsigned kStAbort = kStGsl | kStDnuNaN | kStGridNaN | kStKmax | kStTimeout;
 
 // omega_nu_single.h:27-34: tabulated rho_nu(a) of one species (natural cubic spline in log a)
 struct RhoTable {

@@ -229,6 +229,8 @@ k_correct_tma(const __grid_constant__ CUtensorMap tmap, GridArgs g, const int* _
               const int* __restrict__ cmapg, CorrTable corr, float* grid, unsigned* status, int ntiles) {
     constexpr int TPR = 16 / MPT, NT = ROWS * TPR;
     extern __shared__ unsigned char sm_raw[];
+    // an error of the step so far: the grid stays as it is (as in k_correct_stream)
+    if (*reinterpret_cast<volatile unsigned*>(status) & kStAbort) return;
     __shared__ int s_abort;
     __shared__ long long s_rowbase;
     __shared__ int s_zbase;
@@ -352,6 +354,8 @@ k_correct_tma(const __grid_constant__ CUtensorMap tmap, GridArgs g, const int* _
 __global__ void k_correct_plain(GridArgs g, const int* __restrict__ thresh, const int* __restrict__ cmapg,
                                 CorrTable corr, float* grid, unsigned* status) {
     extern __shared__ unsigned char sm_raw[];
+    // an error of the step so far: the grid stays as it is (as in k_correct_stream)
+    if (*reinterpret_cast<volatile unsigned*>(status) & kStAbort) return;
     int* s_thr = reinterpret_cast<int*>(sm_raw);
     int* s_cmap = s_thr + g.nrbins + 1;
     float* s_tab = reinterpret_cast<float*>(s_cmap + g.nrbins);

@@ -549,6 +549,7 @@ void launch_k2_histogram(int N, int slab0, int nslab, unsigned long long* hist, 
 int launch_bin_power(const GridGeom& g, const float* grid, double* bin_sum, double* F0sq, unsigned* status, int tma,
                      int rows_per_cta, int stages, cudaStream_t st);
 // K3: grid *= 1 + norm * interp(log k)
+// Every variant leaves the grid as it is when the status word holds an error (kStAbort).
 int launch_apply_correction(const GridGeom& g, float* grid, CorrTable corr, float lnscale, unsigned* status, int tma,
                             int rows_per_cta, int stages, cudaStream_t st);
 // normalisation of K1's sums into P(k), delta_cdm, keff (powerspectrum.c:98-115,

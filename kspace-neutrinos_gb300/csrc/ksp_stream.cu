@@ -435,7 +435,7 @@ __global__ void __launch_bounds__(WARPS * 32)
     k_correct_stream(const __grid_constant__ CUtensorMap tmap, GridArgs g, CorrTable corr, float* grid,
                      unsigned* status, long long ntiles, int adv_r, int adv_z) {
     extern __shared__ unsigned char sm_raw[];
-    __shared__ int s_gap;
+    __shared__ int s_gap, s_abort;
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
     const int nk = g.nk;
     const StreamPlan P = plan_corr_stream(WARPS, STAGES, nk);
@@ -444,6 +444,23 @@ __global__ void __launch_bounds__(WARPS * 32)
     uint64_t* my_bar = reinterpret_cast<uint64_t*>(base + P.bar_off) + warp * STAGES;
     float4* s_seg = reinterpret_cast<float4*>(base + P.tab_off);
     int* s_k2t = reinterpret_cast<int*>(base + P.thr_off);
+    // the first tiles' loads go out first, and land while the tables are built; the grid
+    // is read and written once, so its lines leave L2 first
+    const uint64_t pol = ptx::policy_evict_first();
+    const int gw = blockIdx.x * WARPS + warp;
+    const long long TW = (long long)gridDim.x * WARPS;
+    const long long my_n = gw < ntiles ? (ntiles - 1 - gw) / TW + 1 : 0;
+    if (lane == 0) {
+        for (int s = 0; s < STAGES; s++) ptx::mbar_init(&my_bar[s], 1);
+        ptx::mbar_init_fence();
+        for (int s = 0; s < STAGES - 1 && s < my_n; s++) {
+            ptx::mbar_expect_tx(&my_bar[s], kTileBytes);
+            ptx::tma_load_2d_hint(my_stage + s * kTileBytes, &tmap, &my_bar[s], 0, (int)((gw + s * TW) * kRowsPerWarp), pol);
+        }
+    }
+    // an error of the step so far (the reference terminates before the multiply): the
+    // grid stays as it is
+    if (tid == 0) s_abort = (*reinterpret_cast<volatile unsigned*>(status) & kStAbort) != 0u;
     // segment s covers k^2 in [k2t[s-1], k2t[s]): s = 0 below the first node (value of
     // node 0), 1..nk-1 the linear pieces between nodes, nk from the last node on (its
     // value) -- the clamped interpolation of delta_pow.c:19-37 in log k.  k2t[j]: the
@@ -457,11 +474,12 @@ __global__ void __launch_bounds__(WARPS * 32)
         s_k2t[nk] = 0x7fffffff;
         s_gap = -1;
     }
-    if (lane == 0) {
-        for (int s = 0; s < STAGES; s++) ptx::mbar_init(&my_bar[s], 1);
-        ptx::mbar_init_fence();
-    }
     __syncthreads();
+    if (s_abort) {
+        if (lane == 0)
+            for (int s = 0; s < STAGES - 1 && s < my_n; s++) ptx::mbar_wait_bounded(&my_bar[s], 0);
+        return;
+    }
     for (int s = tid; s <= nk; s += blockDim.x) {
         float4 v;
         if (s == 0) v = make_float4(0.f, 0.f, corr.rn[0], 0.f);
@@ -479,14 +497,6 @@ __global__ void __launch_bounds__(WARPS * 32)
     const int ksafe = s_gap >= 0 ? s_k2t[s_gap] : 1;
     const float xwarn = corr.xf[0] - 0.69314718f;
 
-    const int gw = blockIdx.x * WARPS + warp;
-    const long long TW = (long long)gridDim.x * WARPS;
-    const long long my_n = gw < ntiles ? (ntiles - 1 - gw) / TW + 1 : 0;
-    if (lane == 0)
-        for (int s = 0; s < STAGES - 1 && s < my_n; s++) {
-            ptx::mbar_expect_tx(&my_bar[s], kTileBytes);
-            ptx::tma_load_2d(my_stage + s * kTileBytes, &tmap, &my_bar[s], 0, (int)((gw + s * TW) * kRowsPerWarp));
-        }
     const uint32_t mb = (uint32_t)gw * (kRowsPerWarp * 16);
     int rb = (int)fdiv(mb, g.fd_nz);
     int zb = (int)(mb - (uint32_t)rb * (uint32_t)g.nz);
@@ -568,13 +578,13 @@ __global__ void __launch_bounds__(WARPS * 32)
         ptx::fence_async_smem();
         __syncwarp();
         if (lane == 0) {
-            ptx::tma_store_2d(&tmap, tb, 0, (int)(tile * kRowsPerWarp));
+            ptx::tma_store_2d_hint(&tmap, tb, 0, (int)(tile * kRowsPerWarp), pol);
             ptx::bulk_commit();
             if (k + STAGES - 1 < my_n) {
                 ptx::bulk_wait_read_le1();  // the store from stage s2 (one tile ago) has read it
                 ptx::mbar_expect_tx(&my_bar[s2], kTileBytes);
-                ptx::tma_load_2d(my_stage + s2 * kTileBytes, &tmap, &my_bar[s2], 0,
-                                 (int)((gw + (k + STAGES - 1) * TW) * kRowsPerWarp));
+                ptx::tma_load_2d_hint(my_stage + s2 * kTileBytes, &tmap, &my_bar[s2], 0,
+                                 (int)((gw + (k + STAGES - 1) * TW) * kRowsPerWarp), pol);
             }
         }
         if (++s == STAGES) {
@@ -1065,8 +1075,10 @@ __device__ __forceinline__ void issue_mirror_tile(const GridArgs& g, const Mirro
     ptx::fence_async_smem();
     ptx::mbar_expect_tx(bar, (unsigned)(ae - as + be - bs) + tb);
     ptx::bulk_g2s(dst, runtab + ((size_t)ax * (g.half + 1) + q0) * T.Rp, tb, bar);
-    ptx::bulk_g2s(dst + T.tab_bytes, gsrc + as, (unsigned)(ae - as), bar);
-    if (be > bs) ptx::bulk_g2s(dst + T.tab_bytes + T.blk, gsrc + bs, (unsigned)(be - bs), bar);
+    // grid rows are read once: their lines leave L2 first (the run table's stay)
+    const uint64_t pol = ptx::policy_evict_first();
+    ptx::bulk_g2s_hint(dst + T.tab_bytes, gsrc + as, (unsigned)(ae - as), bar, pol);
+    if (be > bs) ptx::bulk_g2s_hint(dst + T.tab_bytes + T.blk, gsrc + bs, (unsigned)(be - bs), bar, pol);
 }
 
 template <bool EXACT>

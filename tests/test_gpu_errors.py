@@ -16,6 +16,8 @@ no GPU fault is provoked.  The context stays usable afterwards.
        grid.  The reference as built by its own Makefile (-ffast-math) compiles both
        isnan checks away and returns without an error.
      5 NaN correction factor                      interface_gadget.c:183-184
+  A step that fails in the integrator leaves the grid as it was (the multiply does not
+  run; the reference terminates before it).
 """
 import math
 
@@ -116,6 +118,33 @@ def test_nan_grid_mode(gpu, oracle):
     k = cases.gpu_instance(gpu, c)
     code = _code(gpu, lambda: k.add_nu_power_to_rhogrid(0.51, c["L"], torch.as_tensor(g).cuda(), 16))
     assert code in (2001, 2004) and st in (2001, 2004), (code, st)
+    k.close()
+
+
+def test_failed_step_leaves_grid(gpu):
+    """An integrator error inside add_nu_power_to_rhogrid (a NaN in the history) stops the
+    step before the multiply, as the reference's terminate does: the grid comes back bit
+    for bit as it went in, from device memory and from host memory.  (delta_nu_last is NaN
+    after such a step, as in the reference, where set_nu_state does not reset it:
+    interface_common.c:166-179, delta_tot_table.c:225-228.)  A fresh context with the good
+    history then steps the untouched grid normally."""
+    import torch
+    c = cases.make_case(16, 16, 6, 0.5, (0.1, 0.1, 0.1))
+    dt = c["delta_tot"].copy()
+    dt[2, 3] = np.nan
+    k = cases.gpu_instance(gpu, c)
+    k.set_nu_state(c["scalefact"], dt)
+    g0 = c["grid"].copy()
+    gd = torch.as_tensor(g0).cuda()
+    assert _code(gpu, lambda: k.add_nu_power_to_rhogrid(0.51, c["L"], gd, 16)) in (2001, 2004)
+    assert np.array_equal(gd.cpu().numpy(), g0)
+    gh = g0.copy()
+    assert _code(gpu, lambda: k.add_nu_power_to_rhogrid(0.51, c["L"], gh, 16)) in (2001, 2004)
+    assert np.array_equal(gh, g0)
+    k.close()
+    k = cases.gpu_instance(gpu, c)
+    k.add_nu_power_to_rhogrid(0.51, c["L"], gd, 16)
+    assert not np.array_equal(gd.cpu().numpy(), g0)
     k.close()
 
 
