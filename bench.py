@@ -355,7 +355,8 @@ def run_gb300(args, cfg):
         t_e2e = float(tt.item())
     e2e_value = N * N * nz * args.steps / t_e2e
     step_ms = sorted(1e3 * x for x in step_s)
-    e2e_steps = {"median": step_ms[len(step_ms) // 2], "min": step_ms[0], "max": step_ms[-1]}
+    e2e_steps = {"median": step_ms[len(step_ms) // 2], "min": step_ms[0], "max": step_ms[-1],
+                 "in_order": [round(1e3 * x, 2) for x in step_s]}
     del host
     link = link_bandwidth(bytes_grid) if rank == 0 else None
     # roofline of the dominant grid kernel
