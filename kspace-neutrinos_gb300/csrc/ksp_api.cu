@@ -1291,6 +1291,8 @@ static int bin_grid(kspace_ctx* c, Geo* G, const float* gd, int pmgrid, int slab
     }
     c->fin = FinalizeArgs{c->bin_sum_d, c->F0sq_d, G->count_d, G->ksum_d, G->compact_d, BoxSize, c->power_d,
                           c->keffg_d, c->I.dcdm, c->keff_d, 1};
+    c->fin.scale = pow(BoxSize, -3.0);
+    c->fin.kfac = 2 * kPi / BoxSize;
     if (!(prep_time > 0 && c->prep_valid)) {
         // a prepared step does it in its row-spline kernel instead (update_device)
         launch_finalize_power(c->bin_sum_d, c->F0sq_d, G->count_d, G->ksum_d, G->compact_d, G->nk, BoxSize,

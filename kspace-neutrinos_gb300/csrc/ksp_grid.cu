@@ -411,11 +411,12 @@ void launch_k2_histogram(int N, int slab0, int nslab, unsigned long long* hist, 
 // powerspectrum.c:98-115 + interface_gadget.c:96-100
 __global__ void k_finalize_power(const double* bin_sum, const double* F0sq, const long long* count,
                                  const double* ksum, const int* compact_bins, int nk, double BoxSize,
-                                 double* power_out, double* keff_out, double* dcdm_out, double* keffphys_out) {
+                                 double* power_out, double* keff_out, double* dcdm_out, double* keffphys_out,
+                                 double scale, double kfac) {
     const int c = blockIdx.x * blockDim.x + threadIdx.x;
     if (c >= nk) return;
-    const FinalizeArgs f{bin_sum, F0sq, count, ksum, compact_bins, BoxSize, power_out, keff_out, dcdm_out,
-                         keffphys_out, 1};
+    const FinalizeArgs f{bin_sum, F0sq,   count,   ksum,         compact_bins, BoxSize, power_out,
+                         keff_out, dcdm_out, keffphys_out, 1, scale, kfac};
     finalize_bin(f, c);
 }
 void launch_finalize_power(const double* bin_sum, const double* F0sq, const long long* count, const double* ksum,
@@ -423,7 +424,8 @@ void launch_finalize_power(const double* bin_sum, const double* F0sq, const long
                            double* dcdm_out, double* keffphys_out, cudaStream_t st) {
     // a warp per block: the FP64 pow, sqrt and divisions of the bins spread over SMs
     k_finalize_power<<<(nk + 31) / 32, 32, 0, st>>>(bin_sum, F0sq, count, ksum, compact_bins, nk, BoxSize, power_out,
-                                                    keff_out, dcdm_out, keffphys_out);
+                                                    keff_out, dcdm_out, keffphys_out, pow(BoxSize, -3.0),
+                                                    2 * 3.14159265358979323846 / BoxSize);
 }
 
 // ------------------------------------------------------------------ host launchers

@@ -437,6 +437,9 @@ struct FinalizeArgs {
     double* dcdm_out;
     double* keffphys_out;
     int active;  // 0: nothing to do
+    // formed on the host, as the reference forms them there (interface_gadget.c:84,96-99):
+    // scale = BoxSize^-3 (pow), kfac = 2 pi / BoxSize
+    double scale, kfac;
 };
 #ifdef __CUDACC__
 __device__ __forceinline__ void finalize_bin(const FinalizeArgs& f, int c) {
@@ -448,9 +451,8 @@ __device__ __forceinline__ void finalize_bin(const FinalizeArgs& f, int c) {
     p /= cnt;
     if (f.power_out) f.power_out[c] = p;
     if (f.keff_out) f.keff_out[c] = ke;
-    const double scale = pow(f.BoxSize, -3.0);
-    if (f.dcdm_out) f.dcdm_out[c] = sqrt(p / scale);
-    if (f.keffphys_out) f.keffphys_out[c] = ke * (2 * 3.14159265358979323846 / f.BoxSize);
+    if (f.dcdm_out) f.dcdm_out[c] = sqrt(p / f.scale);
+    if (f.keffphys_out) f.keffphys_out[c] = ke * f.kfac;
 }
 #endif
 
