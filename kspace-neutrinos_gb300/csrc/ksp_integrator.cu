@@ -646,7 +646,7 @@ __global__ void __launch_bounds__(SPEC ? 256 : 128, SPEC ? 2 : 4)
     if (tid == 0) {
         ptx::mbar_init(bar, 1);
         ptx::mbar_init_fence();
-        if (blockIdx.x < ntask) start_task(blockIdx.x);
+        if (blockIdx.x < ntask) start_task(ntask - 1 - (int)blockIdx.x);
     }
     gk61_fill(N, tid, blockDim.x);
     for (int i = tid; i < Na; i += blockDim.x) knots[i] = I.scalefact[i];
@@ -654,13 +654,16 @@ __global__ void __launch_bounds__(SPEC ? 256 : 128, SPEC ? 2 : 4)
     unsigned phase = 0;
     int my_max = 0;
     long long my_tot = 0;
+    // Blocks take the tasks from the last: the high-k bins of the last species, among the
+    // deepest QAG subdivisions, start first, and the blocks that wait for a free slot
+    // (more tasks than resident blocks) get the shallow low-k bins of the first species.
     for (int task = blockIdx.x; task < ntask; task += gridDim.x) {
-        const int si = task / nk, ik = task % nk;
+        const int si = (ntask - 1 - task) / nk, ik = (ntask - 1 - task) % nk;
         const int mi = si == 0 ? spec_ids.x : (si == 1 ? spec_ids.y : spec_ids.z);
         const double k = I.kq ? I.kq[ik] : I.wavenum[ik];
         if (task != (int)blockIdx.x) {  // later tasks: after the previous task's reads of row / rc
             __syncthreads();
-            if (tid == 0) start_task(task);
+            if (tid == 0) start_task(ntask - 1 - task);
             __syncthreads();
         }
         const double mnubykT = s_task[0];
