@@ -1443,6 +1443,8 @@ int run_bin_mirror(const GridGeom& g, const GridArgs& a, const float* grid, doub
         return e ? atoi(e) : 0;
     }();
     if ((reinterpret_cast<uintptr_t>(grid) & 15) != 0) return -1;
+    // rows q = 0 and N/2 are their own mirrors only for even N (the geometry requires it)
+    if (a.N & 1) return -1;
     MirrorTiling T = make_mirror_tiling(a.nz);
     if (T.P < 1 || !g.runtab || g.run_Rp != T.Rp || g.nslab <= 0) return -1;
     const long long ntiles = (long long)g.nslab * T.tpp;
