@@ -154,3 +154,48 @@ def test_full_step_host_grid_chunks(gpu, N, nb, Na):
         g_host[...] = gd  # continue both from the same grid
     k_dev.close()
     k_host.close()
+
+
+_ROW_KERNEL = r"""
+import json, sys
+sys.path[:0] = [sys.argv[1], sys.argv[1] + "/tests", sys.argv[1] + "/kspace-neutrinos_gb300"]
+import torch
+import cases, kspace_gpu as kg
+import workloads as W
+out = []
+for N, nb in ((64, 48), (96, 80), (128, 128)):
+    g = W.make_grid(N, seed=300 + N)
+    k = kg.KspaceNeutrinos()
+    k.init_omega_nu((0.1, 0.1, 0.1), 0.01, 0.7)
+    k.alloc_table(max(nb, 16), 0.01, 1.0, 0.3, cases.UT, cases.UL)
+    gd = torch.as_tensor(g).cuda()
+    for tma in (5, 6):
+        k.set_tuning(tma=tma)
+        nk, p, c, _ = k.total_powerspectrum(N, gd, nb)
+        out.append([N, nb, tma, int(nk), p.tolist(), c.tolist()])
+    k.close()
+print(json.dumps(out))
+"""
+
+
+def test_row_kernel_without_mirrors(gpu, oracle):
+    """The row-aligned binning kernel (k_bin_rows with the run table, and its lean variant):
+    the pass for grids of more than 32 runs per row (N > 1086), and with
+    KSPACE_GPU_MIRROR=0 (read once per process, hence a child process), against the
+    oracle: counts bit for bit, exact P(k) within 1e-12, lean within 1e-6."""
+    import json
+    import os
+    import subprocess
+    import sys
+    root = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+    env = dict(os.environ, KSPACE_GPU_MIRROR="0")
+    r = subprocess.run([sys.executable, "-c", _ROW_KERNEL, root], capture_output=True, text=True, timeout=600,
+                       env=env)
+    assert r.returncode == 0, r.stderr[-2000:]
+    res = json.loads(r.stdout.strip().splitlines()[-1])
+    assert len(res) == 6
+    for N, nb, tma, nk, p, c in res:
+        g = W.make_grid(N, seed=300 + N)
+        nk_o, p_o, c_o, _ = oracle.total_powerspectrum(g, N, nb)
+        assert nk == nk_o and np.array_equal(np.asarray(c), c_o)
+        assert cases.rel_err(np.asarray(p), p_o) < (TOL_EXACT if tma == 5 else TOL_LEAN), (N, tma)
