@@ -22,9 +22,11 @@
 // hand each closed run to the CTA's float-pair totals (compensated atomics) and the
 // CTA totals to the global FP64 sums once.
 //
-// The default binning kernel is k_bin_rows (further down): the same per-mode arithmetic
-// over tiles of whole grid rows moved by 1-D bulk copies, 17-mode runs that never cross
-// a row end, and a copy of the CTA's totals per tile row.
+// The default binning kernel is k_bin_mirror (further down): 17-mode runs of a grid row
+// and of its mirror row (ky and -ky fall in the same bins), moved by 1-D bulk copies
+// with their run-table rows, the two modes of a pair summed exactly before they are
+// binned.  k_bin_rows, over tiles of whole grid rows and runs of one row, bins grids of
+// more than 32 runs per row (N > 1086) and works without a run table.
 #include <cuda.h>
 #include <cuda_runtime.h>
 #include <stdint.h>
